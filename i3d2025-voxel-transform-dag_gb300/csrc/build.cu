@@ -1,0 +1,611 @@
+// build.cu — constructTransformDAG driver and the C ABI of libtdag.so.
+//
+// Driver restates constructTransformDAG (tools/lib/src/voxel/transform_dag.cpp:138-240):
+//   1. hierarchical symmetry/permutation pass with midLevel = maxTranslationLevel + 1 (:144);
+//   2. if translation is on: drop levels 2..maxTranslationLevel, re-seed the mid level with the
+//      original nodes of its canonical entries (:147-160);
+//   3. for level = maxTranslationLevel .. 2 (:165-238): collect the items referenced by the level
+//      above in ascending order (:177-192), flatten them into dense grids (FlatGridGenerator,
+//      transform_dag.cpp:44-116, 417-441), run the matcher, keep the unique items (:208-221) and
+//      rewrite the parents' child pointers through the mapping (:224-233; the lower_bound lookup is
+//      a rank array here).
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.cuh"
+
+namespace tdag {
+
+// ------------------------------------------------------------------------------------------------
+// Transform tables
+// ------------------------------------------------------------------------------------------------
+const TransformTables& hostTables()
+{
+    static TransformTables t = [] {
+        TransformTables tt {};
+        auto perm = [](uint32_t id, int k) { return (permBitsOf(id) >> (2 * k)) & 3; };
+        auto applyPerm = [&](uint32_t bits3, uint32_t id) {
+            uint32_t o = 0;
+            for (int k = 0; k < 3; ++k)
+                o |= ((bits3 >> perm(id, k)) & 1u) << k;
+            return o;
+        };
+        for (uint32_t a = 0; a < 48; ++a) {
+            const uint32_t sa = a & 7, pa = a >> 3;
+            for (uint32_t i = 0; i < 8; ++i)
+                tt.pos[a][i] = (uint8_t)(applyPerm(i, pa) ^ sa);
+            for (uint32_t b = 0; b < 48; ++b) {
+                const uint32_t sb = b & 7, pb = b >> 3;
+                // (a∘b)(v) = Pa(Pb(v)) ^ Pa(Sb) ^ Sa ; (Pa∘Pb)[k] = pb[pa[k]]
+                uint32_t pc = 0;
+                for (int k = 0; k < 3; ++k)
+                    pc |= perm(pb, (int)perm(pa, k)) << (2 * k);
+                const uint32_t sc = applyPerm(sb, pa) ^ sa;
+                tt.compose[a][b] = (uint8_t)(sc | (permIdOfBits(pc) << 3));
+            }
+            for (uint32_t byte = 0; byte < 256; ++byte) {
+                uint32_t o = 0;
+                for (uint32_t i = 0; i < 8; ++i)
+                    if ((byte >> i) & 1)
+                        o |= 1u << tt.pos[a][i];
+                tt.byteMap[a][byte] = (uint8_t)o;
+            }
+        }
+        for (uint32_t a = 0; a < 48; ++a)
+            for (uint32_t b = 0; b < 48; ++b)
+                if (tt.compose[a][b] == 0)
+                    tt.inverse[a] = (uint8_t)b;
+        return tt;
+    }();
+    return t;
+}
+
+void Context::checkStatus(const std::string& where)
+{
+    TDAG_CUDA(cudaMemcpyAsync(hostStatus, status, 16, cudaMemcpyDeviceToHost, stream));
+    TDAG_CUDA(cudaStreamSynchronize(stream));
+    if (hostStatus[0] != 0) {
+        const uint32_t code = hostStatus[0], aux = hostStatus[1];
+        TDAG_CUDA(cudaMemsetAsync(status, 0, 16, stream));
+        TDAG_CUDA(cudaStreamSynchronize(stream));
+        throw Error((int)code, where + ": device reported error " + std::to_string(code) + " (aux " + std::to_string(aux) + ")");
+    }
+}
+
+namespace {
+
+// ------------------------------------------------------------------------------------------------
+// Kernels of the driver
+// ------------------------------------------------------------------------------------------------
+struct LevelPtrs {
+    const uint32_t* nodes[6]; // levels 0..5 (3..5 used)
+    const uint64_t* leaves;
+};
+
+// Dense grid of a level-L item: thread per output word; 16 x-runs of 4 voxels per word.
+template <int L>
+__global__ void flattenKernel(LevelPtrs lp, const uint32_t* __restrict__ indices, uint32_t n, uint64_t* __restrict__ grids, uint32_t* status)
+{
+    constexpr int R = 1 << L;
+    constexpr int W = R * R * R / 64;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)n * W)
+        return;
+    const uint32_t item = (uint32_t)(gid / W), w = (uint32_t)(gid % W);
+    const uint32_t orig = indices[item];
+    uint64_t word = 0;
+    uint32_t cachedKey = 0xFFFFFFFFu;
+    uint64_t cachedLeaf = 0;
+#pragma unroll 4
+    for (uint32_t g = 0; g < 16; ++g) {
+        const uint32_t b = 64 * w + 4 * g;
+        const uint32_t x = b % R, y = (b / R) % R, z = b / (R * R);
+        const uint32_t lkey = (x >> 2) | ((y >> 2) << 4) | ((z >> 2) << 8);
+        if (lkey != cachedKey) {
+            cachedKey = lkey;
+            uint32_t idx = orig;
+            bool empty = false;
+            for (int lvl = L; lvl > 2; --lvl) {
+                const uint32_t c = ((x >> (lvl - 1)) & 1) | (((y >> (lvl - 1)) & 1) << 1) | (((z >> (lvl - 1)) & 1) << 2);
+                idx = lp.nodes[lvl][(size_t)idx * 8 + c];
+                if (idx == kEmpty32) {
+                    empty = true;
+                    break;
+                }
+            }
+            cachedLeaf = empty ? 0 : lp.leaves[idx];
+        }
+        const uint32_t ly = y & 3, lz = z & 3;
+        const uint32_t base = ((ly & 1) << 1) | ((lz & 1) << 2) | ((ly >> 1) << 4) | ((lz >> 1) << 5);
+        const uint64_t m = cachedLeaf;
+        const uint64_t row = ((m >> base) & 1) | (((m >> (base + 1)) & 1) << 1) | (((m >> (base + 8)) & 1) << 2) | (((m >> (base + 9)) & 1) << 3);
+        word |= row << (4 * g);
+    }
+    grids[gid] = word;
+}
+
+__global__ void markReferencedKernel(const uint64_t* __restrict__ parents, uint64_t count8, uint32_t* __restrict__ ref, uint64_t numItems, uint32_t* status)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count8)
+        return;
+    const uint64_t c = parents[i];
+    if (c == tpSentinel())
+        return;
+    const uint64_t p = tpPtr(c);
+    if (p >= numItems) {
+        setDeviceError(status, TDAG_ERR_CORRUPT, 300);
+        return;
+    }
+    ref[p] = 1;
+}
+
+__global__ void rankKernel(const uint32_t* __restrict__ indices, uint32_t n, uint32_t* __restrict__ rankOf)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        rankOf[indices[i]] = i;
+}
+
+__global__ void remapParentsKernel(uint64_t* __restrict__ parents, uint64_t count8, const uint32_t* __restrict__ rankOf, const uint64_t* __restrict__ mapping)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count8)
+        return;
+    const uint64_t c = parents[i];
+    if (c == tpSentinel())
+        return;
+    parents[i] = mapping[rankOf[tpPtr(c)]];
+}
+
+// Output nodes of a translation level: original nodes of the kept items, children as TransformPointers.
+__global__ void emitOriginalNodesKernel(const uint32_t* __restrict__ nodes, const uint32_t* __restrict__ indices, const uint32_t* __restrict__ kept, uint32_t u,
+    uint64_t* __restrict__ out)
+{
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)u * 8)
+        return;
+    const uint32_t h = (uint32_t)(gid >> 3), k = (uint32_t)(gid & 7);
+    const uint32_t orig = kept ? indices[kept[h]] : indices[h];
+    const uint32_t c = nodes[(size_t)orig * 8 + k];
+    out[gid] = (c == kEmpty32) ? tpSentinel() : tpCreate(c, 0, 0);
+}
+
+__global__ void emitOriginalLeavesKernel(const uint64_t* __restrict__ leaves, const uint32_t* __restrict__ indices, const uint32_t* __restrict__ kept, uint32_t u,
+    uint64_t* __restrict__ out)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < u)
+        out[h] = leaves[indices[kept[h]]];
+}
+
+__global__ void validateChildrenKernel(const uint32_t* __restrict__ nodes, uint64_t count8, uint64_t childCount, uint32_t level, uint32_t* status)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count8)
+        return;
+    const uint32_t c = nodes[i];
+    if (c != kEmpty32 && c >= childCount)
+        setDeviceError(status, TDAG_ERR_CORRUPT, level);
+}
+
+struct DeviceResult {
+    std::vector<DevBuf<uint64_t>> levels;
+    DevBuf<uint64_t> leaves;
+};
+
+template <int L>
+static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& out, const tdag_config& cfg, tdag_stats* stats)
+{
+    cudaStream_t s = ctx.stream;
+    const uint64_t numItems = (L == 2) ? in.leafCount : in.nodeCounts[L];
+    DevBuf<uint64_t>& parents = out.levels[L + 1];
+    const uint64_t count8 = parents.n;
+    DevBuf<uint32_t> ref(numItems, s);
+    if (numItems)
+        TDAG_CUDA(cudaMemsetAsync(ref.get(), 0, numItems * 4, s));
+    if (count8) {
+        markReferencedKernel<<<gridFor(count8, 256), 256, 0, s>>>(parents.get(), count8, ref.get(), numItems, ctx.status);
+        TDAG_CUDA(cudaGetLastError());
+    }
+    DevBuf<uint32_t> indices(numItems, s);
+    const uint32_t m = compactFlags(ref.get(), indices.get(), numItems, s);
+    ref.release();
+    ctx.checkStatus("referenced items");
+    constexpr int R = 1 << L;
+    constexpr int W = R * R * R / 64;
+    DevBuf<uint64_t> grids((size_t)m * W, s);
+    LevelPtrs lp {};
+    for (int l = 3; l <= 5 && l <= (int)in.rootLevel; ++l)
+        lp.nodes[l] = in.nodes[l];
+    lp.leaves = in.leaves;
+    if (m) {
+        flattenKernel<L><<<gridFor((size_t)m * W, 256), 256, 0, s>>>(lp, indices.get(), m, grids.get(), ctx.status);
+        TDAG_CUDA(cudaGetLastError());
+    }
+    tdag_level_stats* ls = stats ? &stats->translation[L] : nullptr;
+    MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls);
+    grids.release();
+    const uint32_t u = mo.numUnique;
+    if (L == 2) {
+        out.leaves = DevBuf<uint64_t>(u, s);
+        if (u) {
+            emitOriginalLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(in.leaves, indices.get(), mo.uniques.get(), u, out.leaves.get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+    } else {
+        out.levels[L] = DevBuf<uint64_t>((size_t)u * 8, s);
+        if (u) {
+            emitOriginalNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(in.nodes[L], indices.get(), mo.uniques.get(), u, out.levels[L].get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+    }
+    if (count8 && m) {
+        DevBuf<uint32_t> rankOf(numItems, s);
+        rankKernel<<<gridFor(m, 256), 256, 0, s>>>(indices.get(), m, rankOf.get());
+        TDAG_CUDA(cudaGetLastError());
+        remapParentsKernel<<<gridFor(count8, 256), 256, 0, s>>>(parents.get(), count8, rankOf.get(), mo.mapping.get());
+        TDAG_CUDA(cudaGetLastError());
+    }
+}
+
+static void validateInput(Context& ctx, const DeviceSvdag& in)
+{
+    cudaStream_t s = ctx.stream;
+    for (uint32_t level = 3; level <= in.rootLevel; ++level) {
+        const uint64_t childCount = (level == 3) ? in.leafCount : in.nodeCounts[level - 1];
+        const uint64_t count8 = in.nodeCounts[level] * 8;
+        if (count8) {
+            validateChildrenKernel<<<gridFor(count8, 256), 256, 0, s>>>(in.nodes[level], count8, childCount, level, ctx.status);
+            TDAG_CUDA(cudaGetLastError());
+        }
+    }
+    ctx.checkStatus("input validation");
+}
+
+static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, tdag_stats* stats)
+{
+    TDAG_CHECK(in.rootLevel >= 2 && in.rootLevel < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "root_level out of range");
+    TDAG_CHECK(in.resolution == (1u << in.rootLevel), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
+    if (cfg.translation) {
+        TDAG_CHECK(cfg.max_translation_level >= 2 && cfg.max_translation_level <= 4, TDAG_ERR_ARG, "max_translation_level must be 2..4 when translation is on");
+        TDAG_CHECK(in.rootLevel >= cfg.max_translation_level + 1, TDAG_ERR_ARG, "root_level must exceed max_translation_level");
+    }
+    for (uint32_t l = 3; l <= in.rootLevel; ++l)
+        TDAG_CHECK(in.nodeCounts[l] < (1ull << 31), TDAG_ERR_ARG, "level too large");
+    TDAG_CHECK(in.leafCount < (1ull << 31), TDAG_ERR_ARG, "too many leaves");
+    validateInput(ctx, in);
+    cudaStream_t s = ctx.stream;
+    TDAG_CUDA(cudaEventRecord(ctx.ev[2], s));
+    const uint32_t midLevel = cfg.max_translation_level + 1;
+    HierOutput h = runHierarchical(ctx, in, cfg, cfg.translation ? midLevel : 0xFFFFFFFFu, stats);
+    TDAG_CUDA(cudaEventRecord(ctx.ev[3], s));
+    DeviceResult out;
+    out.levels.resize(in.rootLevel + 1);
+    for (uint32_t l = 3; l <= in.rootLevel; ++l)
+        out.levels[l] = std::move(h.levels[l]);
+    out.leaves = std::move(h.leaves);
+    if (cfg.translation) {
+        out.leaves.release();
+        for (uint32_t l = 3; l <= cfg.max_translation_level; ++l)
+            out.levels[l].release();
+        const uint32_t u = (uint32_t)(out.levels[midLevel].n / 8);
+        TDAG_CHECK(h.midInv.n == u, TDAG_ERR_CORRUPT, "mid level size mismatch");
+        if (u) {
+            emitOriginalNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(in.nodes[midLevel], h.midInv.get(), nullptr, u, out.levels[midLevel].get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+        h.midInv.release();
+        for (int L = (int)cfg.max_translation_level; L >= 2; --L) {
+            if (L == 4)
+                translationLevel<4>(ctx, in, out, cfg, stats);
+            else if (L == 3)
+                translationLevel<3>(ctx, in, out, cfg, stats);
+            else
+                translationLevel<2>(ctx, in, out, cfg, stats);
+        }
+    }
+    TDAG_CUDA(cudaEventRecord(ctx.ev[4], s));
+    ctx.checkStatus("build");
+    if (stats) {
+        TDAG_CUDA(cudaEventElapsedTime(&stats->hierarchical_ms, ctx.ev[2], ctx.ev[3]));
+        TDAG_CUDA(cudaEventElapsedTime(&stats->translation_ms, ctx.ev[3], ctx.ev[4]));
+        TDAG_CUDA(cudaEventElapsedTime(&stats->total_ms, ctx.ev[2], ctx.ev[4]));
+    }
+    return out;
+}
+
+} // namespace
+} // namespace tdag
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+using namespace tdag;
+
+struct tdag_ctx {
+    Context c;
+};
+
+namespace {
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+template <typename F>
+int guarded(F&& f)
+{
+    try {
+        f();
+        return TDAG_OK;
+    } catch (const Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(TDAG_ERR_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(TDAG_ERR_ARG, e.what());
+    }
+}
+
+struct Upload {
+    std::vector<DevBuf<uint32_t>> nodes;
+    DevBuf<uint64_t> leaves;
+};
+
+DeviceSvdag viewToDevice(const tdag_svdag_view* v)
+{
+    DeviceSvdag d;
+    d.resolution = v->resolution;
+    d.rootLevel = v->root_level;
+    for (uint32_t l = 0; l < TDAG_MAX_LEVELS; ++l) {
+        d.nodes[l] = v->nodes[l];
+        d.nodeCounts[l] = v->node_counts[l];
+    }
+    d.leaves = v->leaves;
+    d.leafCount = v->leaf_count;
+    return d;
+}
+
+void checkView(const tdag_svdag_view* v)
+{
+    TDAG_CHECK(v != nullptr, TDAG_ERR_ARG, "null input view");
+    TDAG_CHECK(v->root_level >= 2 && v->root_level < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "root_level out of range");
+    TDAG_CHECK(v->structure_type == 1, TDAG_ERR_ARG, "constructTransformDAG requires a DAG (structure_type == 1)");
+    for (uint32_t l = 3; l <= v->root_level; ++l)
+        TDAG_CHECK(v->node_counts[l] == 0 || v->nodes[l] != nullptr, TDAG_ERR_ARG, "null node array with non-zero count");
+    TDAG_CHECK(v->leaf_count == 0 || v->leaves != nullptr, TDAG_ERR_ARG, "null leaf array with non-zero count");
+    TDAG_CHECK(v->node_counts[v->root_level] <= 1, TDAG_ERR_ARG, "root level must hold at most one node");
+}
+
+tdag_result* newResult(uint32_t res, uint32_t root, bool onDevice)
+{
+    auto* r = new tdag_result;
+    std::memset(r, 0, sizeof(*r));
+    r->resolution = res;
+    r->root_level = root;
+    r->structure_type = 0;
+    r->on_device = onDevice ? 1u : 0u;
+    return r;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* tdag_version(void) { return "tdag-gb300 0.1 (sm_103a)"; }
+const char* tdag_last_error_message(void) { return g_lastError.c_str(); }
+
+int tdag_ctx_create(int device, const tdag_tuning* tuning, tdag_ctx** out)
+{
+    if (!out)
+        return fail(TDAG_ERR_ARG, "null out pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(TDAG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count)
+        return fail(TDAG_ERR_ARG, "device index out of range");
+    auto holder = std::make_unique<tdag_ctx>();
+    const int rc = guarded([&] {
+        Context& c = holder->c;
+        c.device = device;
+        TDAG_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        TDAG_CUDA(cudaGetDeviceProperties(&prop, device));
+        c.numSMs = prop.multiProcessorCount;
+        if (tuning)
+            c.tuning = *tuning;
+        TDAG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        cudaMemPool_t pool;
+        TDAG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t threshold = ~0ull;
+        TDAG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+        TDAG_CUDA(cudaMalloc(&c.tables, sizeof(TransformTables)));
+        TDAG_CUDA(cudaMemcpy(c.tables, &hostTables(), sizeof(TransformTables), cudaMemcpyHostToDevice));
+        TDAG_CUDA(cudaMalloc(&c.status, 16));
+        TDAG_CUDA(cudaMemset(c.status, 0, 16));
+        TDAG_CUDA(cudaMallocHost(&c.hostStatus, 16));
+        for (auto& e : c.ev)
+            TDAG_CUDA(cudaEventCreate(&e));
+        // Probe that the kernels load on this device (fails loudly on a non-sm_103 GPU).
+        cudaFuncAttributes fa;
+        TDAG_CUDA(cudaFuncGetAttributes(&fa, flattenKernel<2>));
+    });
+    if (rc != TDAG_OK) {
+        tdag_ctx_destroy(holder.release());
+        return rc;
+    }
+    *out = holder.release();
+    return TDAG_OK;
+}
+
+int tdag_ctx_destroy(tdag_ctx* ctx)
+{
+    if (!ctx)
+        return TDAG_OK;
+    Context& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (c.stream)
+        cudaStreamSynchronize(c.stream);
+    for (auto& e : c.ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (c.tables)
+        cudaFree(c.tables);
+    if (c.status)
+        cudaFree(c.status);
+    if (c.hostStatus)
+        cudaFreeHost(c.hostStatus);
+    if (c.stream)
+        cudaStreamDestroy(c.stream);
+    delete ctx;
+    return TDAG_OK;
+}
+
+int tdag_ctx_stream(tdag_ctx* ctx, void** out)
+{
+    if (!ctx || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = (void*)ctx->c.stream;
+    return TDAG_OK;
+}
+
+int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
+{
+    if (!ctx || !cfg || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        checkView(in);
+        Context& c = ctx->c;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, true));
+        DeviceResult dr = buildDevice(c, viewToDevice(in), *cfg, &r->stats);
+        // hand ownership of the device buffers to the result (freed by tdag_result_free)
+        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+        for (uint32_t l = 3; l <= in->root_level; ++l) {
+            r->node_counts[l] = dr.levels[l].n / 8;
+            r->nodes[l] = dr.levels[l].p;
+            dr.levels[l].p = nullptr;
+        }
+        r->leaf_count = dr.leaves.n;
+        r->leaves = dr.leaves.p;
+        dr.leaves.p = nullptr;
+        *out = r.release();
+    });
+}
+
+int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
+{
+    if (!ctx || !cfg || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        checkView(in);
+        Context& c = ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        Upload up;
+        up.nodes.resize(in->root_level + 1);
+        tdag_svdag_view dv = *in;
+        for (uint32_t l = 3; l <= in->root_level; ++l) {
+            const uint64_t cnt = in->node_counts[l];
+            up.nodes[l] = DevBuf<uint32_t>(cnt * 8, s);
+            if (cnt)
+                TDAG_CUDA(cudaMemcpyAsync(up.nodes[l].get(), in->nodes[l], cnt * 32, cudaMemcpyHostToDevice, s));
+            dv.nodes[l] = up.nodes[l].get();
+        }
+        up.leaves = DevBuf<uint64_t>(in->leaf_count, s);
+        if (in->leaf_count)
+            TDAG_CUDA(cudaMemcpyAsync(up.leaves.get(), in->leaves, in->leaf_count * 8, cudaMemcpyHostToDevice, s));
+        dv.leaves = up.leaves.get();
+        std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, false));
+        DeviceResult dr = buildDevice(c, viewToDevice(&dv), *cfg, &r->stats);
+        for (uint32_t l = 3; l <= in->root_level; ++l) {
+            const size_t cnt = dr.levels[l].n / 8;
+            r->node_counts[l] = cnt;
+            r->nodes[l] = (uint64_t*)std::malloc(cnt ? cnt * 64 : 1);
+            TDAG_CHECK(r->nodes[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
+            if (cnt)
+                TDAG_CUDA(cudaMemcpyAsync(r->nodes[l], dr.levels[l].get(), cnt * 64, cudaMemcpyDeviceToHost, s));
+        }
+        r->leaf_count = dr.leaves.n;
+        r->leaves = (uint64_t*)std::malloc(dr.leaves.n ? dr.leaves.n * 8 : 1);
+        TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
+        if (dr.leaves.n)
+            TDAG_CUDA(cudaMemcpyAsync(r->leaves, dr.leaves.get(), dr.leaves.n * 8, cudaMemcpyDeviceToHost, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        *out = r.release();
+    });
+}
+
+int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
+{
+    if (!cfg)
+        return fail(TDAG_ERR_ARG, "null argument");
+    tdag_config c = *cfg;
+    c.translation = 0;
+    return tdag_build(ctx, in, &c, out);
+}
+
+int tdag_result_free(tdag_result* r)
+{
+    if (!r)
+        return TDAG_OK;
+    for (uint32_t l = 0; l < TDAG_MAX_LEVELS; ++l) {
+        if (!r->nodes[l])
+            continue;
+        if (r->on_device)
+            cudaFree(r->nodes[l]);
+        else
+            std::free(r->nodes[l]);
+    }
+    if (r->leaves) {
+        if (r->on_device)
+            cudaFree(r->leaves);
+        else
+            std::free(r->leaves);
+    }
+    delete r;
+    return TDAG_OK;
+}
+
+int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config* cfg, uint64_t* outMapping,
+    uint32_t* outUnique, uint32_t* nUnique, tdag_level_stats* stats)
+{
+    if (!ctx || !cfg || !nUnique || (n && (!grids || !outMapping || !outUnique)))
+        return fail(TDAG_ERR_ARG, "null argument");
+    return guarded([&] {
+        TDAG_CHECK(level >= 2 && level <= 4, TDAG_ERR_ARG, "level must be 2..4");
+        Context& c = ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        const size_t W = ((size_t)1 << (3 * level)) / 64;
+        DevBuf<uint64_t> g(n * W, s);
+        if (n)
+            TDAG_CUDA(cudaMemcpyAsync(g.get(), grids, n * W * 8, cudaMemcpyHostToDevice, s));
+        tdag_level_stats ls {};
+        MatchOutput mo = runMatcher(c, level, g.get(), n, *cfg, &ls);
+        if (n) {
+            TDAG_CUDA(cudaMemcpyAsync(outMapping, mo.mapping.get(), (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+            if (mo.numUnique)
+                TDAG_CUDA(cudaMemcpyAsync(outUnique, mo.uniques.get(), (size_t)mo.numUnique * 4, cudaMemcpyDeviceToHost, s));
+        }
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        *nUnique = mo.numUnique;
+        if (stats)
+            *stats = ls;
+    });
+}
+
+} // extern "C"

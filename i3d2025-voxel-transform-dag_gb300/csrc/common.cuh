@@ -1,0 +1,235 @@
+// common.cuh — shared device/host definitions for the GB300 Transform-DAG library (libtdag.so).
+//
+// Integer/bitwise only. Semantics follow the reference's Transform-Aware SVDAG construction:
+//   TransformPointer bit layout ............ tools/lib/include/voxcom/voxel/transform_dag.h:19-33
+//   encodeFixed64 / decodeFixed64 .......... transform_dag.h:349-397
+//   transform IDs (sym | perm << 3) ........ tools/lib/src/voxel/transform_dag_hierarchical.cpp:23-46
+//   hash_combine ........................... tools/lib/include/voxcom/utility/hash.h:10-20
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "../../include/tdag.h"
+
+namespace tdag {
+
+// ------------------------------------------------------------------------------------------------
+// Errors. Host code throws tdag::Error(code, message); the C-ABI layer converts to a status code.
+// Device code never traps: it records the first error in a status word the host reads after the
+// stage (TDAG_ERR_TABLE_FULL etc.) and returns.
+// ------------------------------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m)
+        : std::runtime_error(m)
+        , code(c)
+    {
+    }
+};
+
+#define TDAG_CUDA(call)                                                                                         \
+    do {                                                                                                        \
+        cudaError_t e_ = (call);                                                                                \
+        if (e_ != cudaSuccess)                                                                                  \
+            throw ::tdag::Error(TDAG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " @" + __FILE__ + ":" + std::to_string(__LINE__)); \
+    } while (0)
+
+#define TDAG_CHECK(cond, code, msg)                \
+    do {                                           \
+        if (!(cond))                               \
+            throw ::tdag::Error((code), (msg));    \
+    } while (0)
+
+// Device status word layout: [0] = first error code, [1] = aux (e.g. the level), [2..3] spare.
+__device__ __forceinline__ void setDeviceError(uint32_t* status, uint32_t code, uint32_t aux = 0)
+{
+    if (atomicCAS(status, 0u, code) == 0u)
+        status[1] = aux;
+}
+
+// ------------------------------------------------------------------------------------------------
+// hash_combine with the identity hasher, 64-bit (size_t) wrap-around.
+// ------------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t hashCombine(uint64_t seed, uint64_t key)
+{
+    return seed ^ (key + 0x9e3779b9ull + (seed << 6) + (seed >> 2));
+}
+
+// A strong 64-bit mixer for table slot selection (splitmix64 finaliser constants are public domain).
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Morton codes (x in bit 0), libmorton morton3D_32 semantics.
+// ------------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t part1by2(uint32_t v)
+{
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000FF;
+    v = (v | (v << 8)) & 0x0300F00F;
+    v = (v | (v << 4)) & 0x030C30C3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t compact1by2(uint32_t v)
+{
+    v &= 0x09249249;
+    v = (v ^ (v >> 2)) & 0x030C30C3;
+    v = (v ^ (v >> 4)) & 0x0300F00F;
+    v = (v ^ (v >> 8)) & 0x030000FF;
+    v = (v ^ (v >> 16)) & 0x000003FF;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) { return part1by2(x) | (part1by2(y) << 1) | (part1by2(z) << 2); }
+
+// ------------------------------------------------------------------------------------------------
+// TransformPointer (compact 64-bit layout): ptr:37 | sx:1 sy:1 sz:1 | p0:2 p1:2 p2:2 | tx:6 ty:6 tz:6,
+// translations biased by +32. The 48 rotations/mirrors are numbered sym | permId << 3, where
+// permId indexes kPermTable = {012, 021, 102, 120, 201, 210}.
+// ------------------------------------------------------------------------------------------------
+constexpr uint64_t kPtrMask = (1ull << 37) - 1;
+constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
+
+__host__ __device__ __forceinline__ uint32_t permBitsOf(uint32_t permId)
+{
+    // packed p0 | p1 << 2 | p2 << 4 for each permutation ID
+    constexpr uint32_t packed[6] = { 0 | 1 << 2 | 2 << 4, 0 | 2 << 2 | 1 << 4, 1 | 0 << 2 | 2 << 4, 1 | 2 << 2 | 0 << 4, 2 | 0 << 2 | 1 << 4, 2 | 1 << 2 | 0 << 4 };
+    return packed[permId];
+}
+__host__ __device__ __forceinline__ uint32_t permIdOfBits(uint32_t pbits)
+{
+    const uint32_t p0 = pbits & 3, p1 = (pbits >> 2) & 3, p2 = (pbits >> 4) & 3;
+    return 2 * p0 + (p2 < p1 ? 1 : 0);
+}
+__host__ __device__ __forceinline__ uint64_t tpCreate(uint64_t ptr, uint32_t sym, uint32_t permId, int tx = 0, int ty = 0, int tz = 0)
+{
+    uint64_t v = ptr & kPtrMask;
+    v |= (uint64_t)(sym & 7) << 37;
+    v |= (uint64_t)permBitsOf(permId) << 40;
+    v |= (uint64_t)((unsigned)(tx + 32) & 63) << 46;
+    v |= (uint64_t)((unsigned)(ty + 32) & 63) << 52;
+    v |= (uint64_t)((unsigned)(tz + 32) & 63) << 58;
+    return v;
+}
+__host__ __device__ __forceinline__ uint64_t tpCreateT(uint64_t ptr, uint32_t transformId) { return tpCreate(ptr, transformId & 7, transformId >> 3); }
+__host__ __device__ __forceinline__ uint64_t tpSentinel() { return tpCreate(0xFFFFFFFFull, 0, 0); }
+__host__ __device__ __forceinline__ uint64_t tpPtr(uint64_t v) { return v & kPtrMask; }
+__host__ __device__ __forceinline__ uint32_t tpSym(uint64_t v) { return (uint32_t)(v >> 37) & 7; }
+__host__ __device__ __forceinline__ uint32_t tpPermId(uint64_t v) { return permIdOfBits((uint32_t)(v >> 40) & 63); }
+__host__ __device__ __forceinline__ uint32_t tpTransformId(uint64_t v) { return tpSym(v) | (tpPermId(v) << 3); }
+__host__ __device__ __forceinline__ int tpT(uint64_t v, int axis) { return (int)((v >> (46 + 6 * axis)) & 63) - 32; }
+__host__ __device__ __forceinline__ uint64_t tpWithPtr(uint64_t v, uint64_t ptr) { return (v & ~kPtrMask) | (ptr & kPtrMask); }
+
+// encodeFixed64(level): ptr | permCode | sym, then (level+1)-bit z, y, x translations biased by 1 << level.
+__host__ __device__ __forceinline__ uint64_t encodeFixed64(uint64_t ptr, uint32_t permId, uint32_t sym, int tx, int ty, int tz, uint32_t level)
+{
+    uint64_t out = ((ptr << 3 | permId) << 3) | sym;
+    const uint32_t sb = level + 1;
+    const int bias = 1 << level;
+    out = (out << sb) | (uint64_t)(unsigned)(tz + bias);
+    out = (out << sb) | (uint64_t)(unsigned)(ty + bias);
+    out = (out << sb) | (uint64_t)(unsigned)(tx + bias);
+    return out;
+}
+__host__ __device__ __forceinline__ uint64_t decodeFixed64(uint64_t e, uint32_t level)
+{
+    const uint32_t sb = level + 1;
+    const uint64_t m = (1ull << sb) - 1;
+    const int bias = 1 << level;
+    const int tx = (int)(e & m) - bias;
+    e >>= sb;
+    const int ty = (int)(e & m) - bias;
+    e >>= sb;
+    const int tz = (int)(e & m) - bias;
+    e >>= sb;
+    const uint32_t sym = (uint32_t)(e & 7);
+    e >>= 3;
+    const uint32_t pc = (uint32_t)(e & 7);
+    e >>= 3;
+    return tpCreate(e, sym, pc, tx, ty, tz);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Transform algebra tables (computed on the host once; copied into shared memory by kernels).
+// A transform t maps position v to P(v) ^ S, P(v) = (v[p0], v[p1], v[p2]).
+// ------------------------------------------------------------------------------------------------
+struct TransformTables {
+    uint8_t compose[48][48]; // compose[a][b] = a ∘ b
+    uint8_t inverse[48];
+    uint8_t pos[48][8]; // image of a 2x2x2 child index
+    uint8_t byteMap[48][256]; // image of a 2x2x2 occupancy byte (bit i = child i)
+};
+const TransformTables& hostTables();
+
+// ------------------------------------------------------------------------------------------------
+// Small device-memory helpers (stream-ordered allocations from the context's pool).
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = 0;
+    DevBuf() = default;
+    DevBuf(size_t count, cudaStream_t stream)
+        : n(count)
+        , s(stream)
+    {
+        if (count)
+            TDAG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), stream));
+    }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            s = o.s;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p)
+            cudaFreeAsync(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    T* get() const { return p; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+inline unsigned gridFor(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+// ------------------------------------------------------------------------------------------------
+// Primitives (primitives.cu): exclusive scan of u32, stable LSD radix sort of (u64 key, u32 value).
+// ------------------------------------------------------------------------------------------------
+void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
+// Returns total (sum of in) by copying the last element; synchronises the stream.
+uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
+void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s);
+// Compact indices i in [0, n) with flags[i] != 0 into out (ascending); returns the count.
+uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s);
+
+// Statistics accumulated over one build (device counters for the matcher).
+struct LevelStats {
+    uint64_t items = 0, unique = 0, probes = 0, filterPass = 0, hits = 0, candidates = 0, verifications = 0, verified = 0, tableEntries = 0;
+    float searchMs = 0;
+};
+
+} // namespace tdag

@@ -1,0 +1,579 @@
+// hierarchical.cu — GPU symmetry + axis-permutation canonicalisation of an SVDAG, bottom-up.
+//
+// Restates constructTransformDAGHierarchical (tools/lib/src/voxel/transform_dag_hierarchical.cpp:304-523)
+// without its sequential per-range search. The reference, per level:
+//   1. groups nodes by a hash of their sorted child pointers and sorts (hash, index) (:365-378);
+//   2. inside a group, in index order, a node becomes canonical unless some allowed transform, tried
+//      in ID order 0..47, maps it onto an earlier canonical (:326-357, :403-414);
+//   3. emits canonical nodes in (hash, index) order; a non-canonical node maps to
+//      (handle(canonical), inverse(t)) (:343-344, :417-430).
+// Equivalence under the allowed transforms is a content equality, so the canonical of a node is the
+// smallest index of its equivalence class, and the group hash is a class invariant. This file
+// computes an exact class signature per node (the lexicographic minimum of its transformed child
+// codes), finds the class minimum with a bounded-probe hash table that compares full signatures,
+// then finds the first transform ID that maps each node onto its canonical, exactly as step 2 does.
+//
+// Child codes: a child pointer (h, tau) with canonical invariance group Inv(h) is represented by
+// (h, min ID of the coset tau * Inv(h)), which is equal for two pointers exactly when
+// TaggedPointer::operator== (:79-122) says they are equal.
+#include "common.cuh"
+#include "internal.cuh"
+
+namespace tdag {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint64_t kEmptySlot = ~0ull;
+
+struct SmemTables {
+    uint8_t compose[48][48];
+    uint8_t inverse[48];
+    uint8_t pos[48][8];
+};
+
+__device__ __forceinline__ void loadTables(SmemTables& s, const TransformTables* g)
+{
+    const uint8_t* src = &g->compose[0][0];
+    uint8_t* dst = &s.compose[0][0];
+    for (int i = threadIdx.x; i < 48 * 48; i += blockDim.x)
+        dst[i] = src[i];
+    for (int i = threadIdx.x; i < 48; i += blockDim.x)
+        s.inverse[i] = g->inverse[i];
+    for (int i = threadIdx.x; i < 48 * 8; i += blockDim.x)
+        (&s.pos[0][0])[i] = (&g->pos[0][0])[i];
+}
+
+// Transform of a 4x4x4 Morton mask: byte k is the 2x2x2 block at child position k; the transform
+// moves it to pos[t][k] and maps its content with the 2x2x2 byte map.
+__device__ __forceinline__ uint64_t transformLeaf(uint64_t m, uint32_t t, const uint8_t (*byteMap)[256], const uint8_t (*pos)[8])
+{
+    uint64_t out = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t b = (uint32_t)(m >> (8 * k)) & 0xFF;
+        out |= (uint64_t)byteMap[t][b] << (8 * pos[t][k]);
+    }
+    return out;
+}
+
+__device__ __forceinline__ uint64_t sortedPtrHash(uint64_t p[8])
+{
+    // insertion sort of 8 values, then hash_combine over them (:365-377)
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        uint64_t v = p[i];
+        int j = i - 1;
+        while (j >= 0 && p[j] > v) {
+            p[j + 1] = p[j];
+            --j;
+        }
+        p[j + 1] = v;
+    }
+    uint64_t seed = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        seed = hashCombine(seed, p[i]);
+    return seed;
+}
+
+// ---------------------------------------------------------------------------- leaves (level 2)
+__global__ void __launch_bounds__(kThreads) leafSigKernel(const uint64_t* __restrict__ leaves, uint32_t n, const TransformTables* __restrict__ tables,
+    const uint8_t* __restrict__ canonByte, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key)
+{
+    __shared__ uint8_t byteMap[48][256];
+    __shared__ uint8_t pos[48][8];
+    __shared__ uint8_t cb[256];
+    for (int i = threadIdx.x; i < 48 * 256; i += blockDim.x)
+        (&byteMap[0][0])[i] = (&tables->byteMap[0][0])[i];
+    for (int i = threadIdx.x; i < 48 * 8; i += blockDim.x)
+        (&pos[0][0])[i] = (&tables->pos[0][0])[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        cb[i] = canonByte[i];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint64_t m = leaves[i];
+    uint64_t best = m;
+    for (uint32_t t = 1; t < 48; ++t) {
+        if (!((allowed >> t) & 1))
+            continue;
+        const uint64_t v = transformLeaf(m, t, byteMap, pos);
+        best = v < best ? v : best;
+    }
+    sig[i] = best;
+    uint64_t p[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        p[k] = cb[(m >> (8 * k)) & 0xFF];
+    key[i] = sortedPtrHash(p);
+}
+
+// For each leaf: canonical = class minimum; canonical leaves get their invariance mask, the others
+// the first transform ID t with T_t(leaf) == canonical (transform_dag_hierarchical.cpp:329-355).
+__global__ void __launch_bounds__(kThreads) leafResolveKernel(const uint64_t* __restrict__ leaves, uint32_t n, const TransformTables* __restrict__ tables,
+    uint64_t allowed, const uint32_t* __restrict__ slotOf, const uint32_t* __restrict__ minIdx, uint32_t* __restrict__ canonOf,
+    uint8_t* __restrict__ tOf, uint64_t* __restrict__ invOf, uint32_t* __restrict__ isCanon, uint32_t* status)
+{
+    __shared__ uint8_t byteMap[48][256];
+    __shared__ uint8_t pos[48][8];
+    for (int i = threadIdx.x; i < 48 * 256; i += blockDim.x)
+        (&byteMap[0][0])[i] = (&tables->byteMap[0][0])[i];
+    for (int i = threadIdx.x; i < 48 * 8; i += blockDim.x)
+        (&pos[0][0])[i] = (&tables->pos[0][0])[i];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t c = minIdx[slotOf[i]];
+    const uint64_t m = leaves[i];
+    canonOf[i] = c;
+    if (c == i) {
+        uint64_t inv = 0;
+        for (uint32_t t = 0; t < 48; ++t)
+            if (((allowed >> t) & 1) && transformLeaf(m, t, byteMap, pos) == m)
+                inv |= 1ull << t;
+        invOf[i] = inv;
+        tOf[i] = 0;
+        isCanon[i] = 1;
+    } else {
+        const uint64_t mc = leaves[c];
+        uint32_t found = 0xFF;
+        for (uint32_t t = 0; t < 48; ++t) {
+            if (((allowed >> t) & 1) && transformLeaf(m, t, byteMap, pos) == mc) {
+                found = t;
+                break;
+            }
+        }
+        if (found == 0xFF)
+            setDeviceError(status, TDAG_ERR_CORRUPT, 2);
+        tOf[i] = (uint8_t)(found == 0xFF ? 0 : found);
+        isCanon[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------- inner nodes
+struct Child {
+    uint32_t h; // handle at the level below (0xFFFFFFFF: empty)
+    uint32_t tau; // transform ID of the child pointer
+    uint64_t inv; // invariance mask of the child's canonical
+};
+
+__device__ __forceinline__ Child loadChild(const uint32_t* __restrict__ node, int k, const uint64_t* __restrict__ prevMap, const uint64_t* __restrict__ prevInv)
+{
+    const uint32_t c = node[k];
+    if (c == kEmpty32)
+        return Child { kEmpty32, 0, ~0ull };
+    const uint64_t tp = prevMap[c];
+    const uint32_t h = (uint32_t)tpPtr(tp);
+    return Child { h, tpTransformId(tp), prevInv[h] };
+}
+
+// code of child (h, t ∘ tau) with coset normalisation
+__device__ __forceinline__ uint64_t childCode(const Child& c, uint32_t t, const SmemTables& st, uint64_t allowed)
+{
+    if (c.h == kEmpty32)
+        return (uint64_t)kEmpty32 << 6;
+    const uint32_t tau = st.compose[t][c.tau];
+    uint32_t rep;
+    if (c.inv == allowed) {
+        rep = 0;
+    } else {
+        rep = 63;
+        uint64_t bits = c.inv;
+        while (bits) {
+            const uint32_t g = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const uint32_t v = st.compose[tau][g];
+            rep = v < rep ? v : rep;
+        }
+    }
+    return ((uint64_t)c.h << 6) | rep;
+}
+
+__device__ __forceinline__ void transformedCodes(const Child ch[8], uint32_t t, const SmemTables& st, uint64_t allowed, uint64_t out[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        out[st.pos[t][k]] = childCode(ch[k], t, st, allowed);
+}
+
+__device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (a[k] != b[k])
+            return a[k] < b[k];
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
+    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key)
+{
+    __shared__ SmemTables st;
+    loadTables(st, tables);
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t* node = nodes + (size_t)i * 8;
+    Child ch[8];
+    uint64_t p[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        ch[k] = loadChild(node, k, prevMap, prevInv);
+        p[k] = ch[k].h;
+    }
+    key[i] = sortedPtrHash(p);
+    uint64_t best[8], cur[8];
+    transformedCodes(ch, 0, st, allowed, best);
+    for (uint32_t t = 1; t < 48; ++t) {
+        if (!((allowed >> t) & 1))
+            continue;
+        transformedCodes(ch, t, st, allowed, cur);
+        if (lexLess(cur, best)) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                best[k] = cur[k];
+        }
+    }
+    uint64_t* out = sig + (size_t)i * 8;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        out[k] = best[k];
+}
+
+__global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
+    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, const uint32_t* __restrict__ slotOf,
+    const uint32_t* __restrict__ minIdx, uint32_t* __restrict__ canonOf, uint8_t* __restrict__ tOf, uint64_t* __restrict__ invOf,
+    uint32_t* __restrict__ isCanon, uint32_t level, uint32_t* status)
+{
+    __shared__ SmemTables st;
+    loadTables(st, tables);
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t c = minIdx[slotOf[i]];
+    canonOf[i] = c;
+    Child ch[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        ch[k] = loadChild(nodes + (size_t)i * 8, k, prevMap, prevInv);
+    uint64_t target[8], cur[8];
+    if (c == i) {
+        transformedCodes(ch, 0, st, allowed, target);
+        uint64_t inv = 1; // identity
+        for (uint32_t t = 1; t < 48; ++t) {
+            if (!((allowed >> t) & 1))
+                continue;
+            transformedCodes(ch, t, st, allowed, cur);
+            bool eq = true;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                eq &= (cur[k] == target[k]);
+            if (eq)
+                inv |= 1ull << t;
+        }
+        invOf[i] = inv;
+        tOf[i] = 0;
+        isCanon[i] = 1;
+    } else {
+        Child cc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            cc[k] = loadChild(nodes + (size_t)c * 8, k, prevMap, prevInv);
+        transformedCodes(cc, 0, st, allowed, target);
+        uint32_t found = 0xFF;
+        for (uint32_t t = 0; t < 48; ++t) {
+            if (!((allowed >> t) & 1))
+                continue;
+            transformedCodes(ch, t, st, allowed, cur);
+            bool eq = true;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                eq &= (cur[k] == target[k]);
+            if (eq) {
+                found = t;
+                break;
+            }
+        }
+        if (found == 0xFF)
+            setDeviceError(status, TDAG_ERR_CORRUPT, level);
+        tOf[i] = (uint8_t)(found == 0xFF ? 0 : found);
+        isCanon[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------- class table
+// Slot = tag << 32 | claimer index. A node belongs to a slot when its full signature equals the
+// claimer's. minIdx[slot] collects the class minimum. Probing is bounded by the capacity.
+template <int W>
+__global__ void __launch_bounds__(kThreads) classInsertKernel(const uint64_t* __restrict__ sig, uint32_t n, uint64_t* __restrict__ slots,
+    uint32_t* __restrict__ minIdx, uint32_t* __restrict__ slotOf, uint64_t capMask, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint64_t s[W];
+    uint64_t fp = 0x5bd1e995ull;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        s[k] = sig[(size_t)i * W + k];
+        fp = mix64(fp ^ s[k]);
+    }
+    const uint32_t tag = (uint32_t)(fp >> 32);
+    uint64_t slot = fp & capMask;
+    for (uint64_t probe = 0; probe <= capMask; ++probe) {
+        uint64_t cur = slots[slot];
+        if (cur == kEmptySlot) {
+            const uint64_t mine = ((uint64_t)tag << 32) | i;
+            cur = atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine);
+            if (cur == kEmptySlot) {
+                slotOf[i] = (uint32_t)slot;
+                atomicMin(&minIdx[slot], i);
+                return;
+            }
+        }
+        if ((uint32_t)(cur >> 32) == tag) {
+            const uint32_t j = (uint32_t)cur;
+            bool eq = true;
+#pragma unroll
+            for (int k = 0; k < W; ++k)
+                eq &= (sig[(size_t)j * W + k] == s[k]);
+            if (eq) {
+                slotOf[i] = (uint32_t)slot;
+                atomicMin(&minIdx[slot], i);
+                return;
+            }
+        }
+        slot = (slot + 1) & capMask;
+    }
+    setDeviceError(status, TDAG_ERR_TABLE_FULL, 100);
+}
+
+// ---------------------------------------------------------------------------- emission
+__global__ void gatherSortInputKernel(const uint32_t* __restrict__ canonList, uint32_t u, const uint64_t* __restrict__ key, uint64_t* __restrict__ sk, uint32_t* __restrict__ sv)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= u)
+        return;
+    const uint32_t idx = canonList[h];
+    sk[h] = key[idx];
+    sv[h] = idx;
+}
+
+__global__ void handleKernel(const uint32_t* __restrict__ emitOrder, uint32_t u, const uint64_t* __restrict__ invOf, uint32_t* __restrict__ handleOf, uint64_t* __restrict__ invOut)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= u)
+        return;
+    const uint32_t idx = emitOrder[h];
+    handleOf[idx] = h;
+    invOut[h] = invOf[idx];
+}
+
+__global__ void mappingKernel(uint32_t n, const uint32_t* __restrict__ canonOf, const uint8_t* __restrict__ tOf, const uint32_t* __restrict__ handleOf,
+    const TransformTables* __restrict__ tables, uint64_t* __restrict__ mapOut, uint32_t* __restrict__ midInv)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t c = canonOf[i];
+    const uint32_t h = handleOf[c];
+    const uint32_t t = (c == i) ? 0u : (uint32_t)tables->inverse[tOf[i]];
+    mapOut[i] = tpCreateT(h, t);
+    if (midInv && t == 0)
+        atomicMax(&midInv[h], i); // storeMidLevelMapping keeps the last identity-mapped index (:312-320)
+}
+
+__global__ void emitLeavesKernel(const uint32_t* __restrict__ emitOrder, uint32_t u, const uint64_t* __restrict__ leaves, uint64_t* __restrict__ out)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < u)
+        out[h] = leaves[emitOrder[h]];
+}
+
+__global__ void emitNodesKernel(const uint32_t* __restrict__ emitOrder, uint32_t u, const uint32_t* __restrict__ nodes, const uint64_t* __restrict__ prevMap,
+    uint64_t* __restrict__ out)
+{
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)u * 8)
+        return;
+    const uint32_t h = (uint32_t)(gid >> 3), k = (uint32_t)(gid & 7);
+    const uint32_t c = nodes[(size_t)emitOrder[h] * 8 + k];
+    out[gid] = (c == kEmpty32) ? tpSentinel() : prevMap[c];
+}
+
+__global__ void fillU64Kernel(uint64_t* p, uint64_t v, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        p[i] = v;
+}
+__global__ void fillU32Kernel(uint32_t* p, uint32_t v, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        p[i] = v;
+}
+
+uint64_t pow2AtLeast(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v)
+        p <<= 1;
+    return p;
+}
+
+} // namespace
+
+void fillU64(uint64_t* p, uint64_t v, size_t n, cudaStream_t s)
+{
+    if (n)
+        fillU64Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
+    TDAG_CUDA(cudaGetLastError());
+}
+void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s)
+{
+    if (n)
+        fillU32Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
+    TDAG_CUDA(cudaGetLastError());
+}
+
+// Shared tail of one level: class table -> canonicals -> emission order -> mapping.
+// sigWords = 1 (leaves) or 8 (nodes). Produces mapping (n), inv per handle (u) and the emit order.
+static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, const uint64_t* sig, int sigWords, const uint64_t* key,
+    const std::function<void(const uint32_t*, const uint32_t*, uint32_t*, uint8_t*, uint64_t*, uint32_t*)>& resolve, DevBuf<uint64_t>& mapOut,
+    DevBuf<uint64_t>& invOut, DevBuf<uint32_t>& emitOrder, DevBuf<uint32_t>* midInv)
+{
+    cudaStream_t s = ctx.stream;
+    const uint64_t cap = pow2AtLeast((uint64_t)n * 2 + 16);
+    DevBuf<uint64_t> slots(cap, s);
+    DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
+    fillU64(slots.get(), kEmptySlot, cap, s);
+    fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
+    if (sigWords == 1)
+        classInsertKernel<1><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    else
+        classInsertKernel<8><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    TDAG_CUDA(cudaGetLastError());
+    slots.release();
+
+    DevBuf<uint32_t> canonOf(n, s), isCanon(n, s);
+    DevBuf<uint8_t> tOf(n, s);
+    DevBuf<uint64_t> invOf(n, s);
+    resolve(slotOf.get(), minIdx.get(), canonOf.get(), tOf.get(), invOf.get(), isCanon.get());
+    slotOf.release();
+    minIdx.release();
+    ctx.checkStatus("hierarchical level " + std::to_string(level));
+
+    DevBuf<uint32_t> canonList(n, s);
+    const uint32_t u = compactFlags(isCanon.get(), canonList.get(), n, s);
+    isCanon.release();
+    DevBuf<uint64_t> sk(u, s);
+    emitOrder = DevBuf<uint32_t>(u, s);
+    gatherSortInputKernel<<<gridFor(u, 256), 256, 0, s>>>(canonList.get(), u, key, sk.get(), emitOrder.get());
+    TDAG_CUDA(cudaGetLastError());
+    canonList.release();
+    radixSortPairs(sk.get(), emitOrder.get(), u, 0, 64, s);
+    sk.release();
+
+    DevBuf<uint32_t> handleOf(n, s);
+    invOut = DevBuf<uint64_t>(u, s);
+    handleKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, invOf.get(), handleOf.get(), invOut.get());
+    TDAG_CUDA(cudaGetLastError());
+    mapOut = DevBuf<uint64_t>(n, s);
+    uint32_t* mid = nullptr;
+    if (midInv) {
+        *midInv = DevBuf<uint32_t>(u, s);
+        fillU32(midInv->get(), 0, u, s);
+        mid = midInv->get();
+    }
+    mappingKernel<<<gridFor(n, 256), 256, 0, s>>>(n, canonOf.get(), tOf.get(), handleOf.get(), ctx.tables, mapOut.get(), mid);
+    TDAG_CUDA(cudaGetLastError());
+    return u;
+}
+
+HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, uint32_t midLevel, tdag_stats* stats)
+{
+    cudaStream_t s = ctx.stream;
+    const uint64_t allowed = allowedMask(cfg);
+    const TransformTables& ht = hostTables();
+    // canonical 2x2x2 byte per occupancy byte: the smallest byte of its orbit under the allowed transforms
+    uint8_t canonByte[256];
+    for (uint32_t b = 0; b < 256; ++b) {
+        uint32_t best = b;
+        for (uint32_t t = 0; t < 48; ++t)
+            if ((allowed >> t) & 1)
+                best = ht.byteMap[t][b] < best ? ht.byteMap[t][b] : best;
+        canonByte[b] = (uint8_t)best;
+    }
+    DevBuf<uint8_t> dCanonByte(256, s);
+    TDAG_CUDA(cudaMemcpyAsync(dCanonByte.get(), canonByte, 256, cudaMemcpyHostToDevice, s));
+
+    HierOutput out;
+    out.levels.resize(in.rootLevel + 1);
+    DevBuf<uint64_t> prevMap, prevInv;
+    {
+        const uint32_t n = (uint32_t)in.leafCount;
+        DevBuf<uint64_t> sig(n, s), key(n, s);
+        if (n) {
+            leafSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(in.leaves, n, ctx.tables, dCanonByte.get(), allowed, sig.get(), key.get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+        const uint64_t* leaves = in.leaves;
+        auto resolve = [&](const uint32_t* slotOf, const uint32_t* minIdx, uint32_t* canonOf, uint8_t* tOf, uint64_t* invOf, uint32_t* isCanon) {
+            leafResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(leaves, n, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, ctx.status);
+            TDAG_CUDA(cudaGetLastError());
+        };
+        DevBuf<uint32_t> emitOrder;
+        const uint32_t u = n ? canonicaliseLevel(ctx, 2, n, sig.get(), 1, key.get(), resolve, prevMap, prevInv, emitOrder, midLevel == 2 ? &out.midInv : nullptr) : 0;
+        out.leaves = DevBuf<uint64_t>(u, s);
+        if (u) {
+            emitLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, in.leaves, out.leaves.get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+        if (stats) {
+            stats->hierarchical[2].items = n;
+            stats->hierarchical[2].unique = u;
+        }
+    }
+    for (uint32_t level = 3; level <= in.rootLevel; ++level) {
+        const uint32_t n = (uint32_t)in.nodeCounts[level];
+        const uint32_t* nodes = in.nodes[level];
+        DevBuf<uint64_t> sig((size_t)n * 8, s), key(n, s);
+        if (n) {
+            nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevInv.get(), ctx.tables, allowed, sig.get(), key.get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+        const uint64_t* pm = prevMap.get();
+        const uint64_t* pi = prevInv.get();
+        auto resolve = [&](const uint32_t* slotOf, const uint32_t* minIdx, uint32_t* canonOf, uint8_t* tOf, uint64_t* invOf, uint32_t* isCanon) {
+            nodeResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, pm, pi, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, level, ctx.status);
+            TDAG_CUDA(cudaGetLastError());
+        };
+        DevBuf<uint64_t> map, inv;
+        DevBuf<uint32_t> emitOrder;
+        const uint32_t u = n ? canonicaliseLevel(ctx, level, n, sig.get(), 8, key.get(), resolve, map, inv, emitOrder, level == midLevel ? &out.midInv : nullptr) : 0;
+        sig.release();
+        key.release();
+        auto& lvl = out.levels[level];
+        lvl = DevBuf<uint64_t>((size_t)u * 8, s);
+        if (u) {
+            emitNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(emitOrder.get(), u, nodes, prevMap.get(), lvl.get());
+            TDAG_CUDA(cudaGetLastError());
+        }
+        prevMap = std::move(map);
+        prevInv = std::move(inv);
+        if (stats) {
+            stats->hierarchical[level].items = n;
+            stats->hierarchical[level].unique = u;
+        }
+    }
+    return out;
+}
+
+} // namespace tdag

@@ -1,0 +1,259 @@
+// primitives.cu — hand-written device scan, stream compaction and stable LSD radix sort.
+//
+// The reference sorts with std::sort / std::stable_sort (find_translation.cpp:639,727;
+// transform_dag_hierarchical.cpp:378). These kernels give the same orders: a stable sort on the key,
+// with values fed in ascending index order, yields (key, index) order.
+#include "common.cuh"
+
+namespace tdag {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16; // per thread
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warpInclusiveScan(uint32_t v)
+{
+    const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= (uint32_t)d)
+            v += o;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns exclusive prefix, writes block total.
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* smem, uint32_t& total)
+{
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warpInclusiveScan(v);
+    if (lane == 31)
+        smem[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        uint32_t w = lane < nw ? smem[lane] : 0;
+        const uint32_t wi = warpInclusiveScan(w);
+        if (lane < nw)
+            smem[lane] = wi - w;
+        if (lane == nw - 1)
+            smem[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t res = smem[warp] + inc - v;
+    total = smem[32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void scanReduceKernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ blockSums, size_t n)
+{
+    __shared__ uint32_t smem[33];
+    const size_t base = (size_t)blockIdx.x * kScanTile;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + (size_t)k * kScanThreads + threadIdx.x;
+        if (i < n)
+            s += in[i];
+    }
+    uint32_t total;
+    blockExclusiveScan(s, smem, total);
+    if (threadIdx.x == 0)
+        blockSums[blockIdx.x] = total;
+}
+
+__global__ void scanDownKernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, const uint32_t* __restrict__ blockOffsets, size_t n)
+{
+    __shared__ uint32_t smem[33];
+    const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = blockExclusiveScan(s, smem, total) + (blockOffsets ? blockOffsets[blockIdx.x] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const size_t i = base + k;
+        if (i < n)
+            out[i] = run;
+        run += v[k];
+    }
+}
+
+} // namespace
+
+void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    const size_t blocks = (n + kScanTile - 1) / kScanTile;
+    if (blocks == 1) {
+        scanDownKernel<<<1, kScanThreads, 0, s>>>(in, out, nullptr, n);
+        TDAG_CUDA(cudaGetLastError());
+        return;
+    }
+    DevBuf<uint32_t> sums(blocks, s), offs(blocks, s);
+    scanReduceKernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(in, sums.get(), n);
+    TDAG_CUDA(cudaGetLastError());
+    exclusiveScanU32(sums.get(), offs.get(), blocks, s);
+    scanDownKernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(in, out, offs.get(), n);
+    TDAG_CUDA(cudaGetLastError());
+}
+
+uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s)
+{
+    if (n == 0)
+        return 0;
+    exclusiveScanU32(in, out, n, s);
+    uint32_t lastIn = 0, lastOut = 0;
+    TDAG_CUDA(cudaMemcpyAsync(&lastIn, in + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    TDAG_CUDA(cudaMemcpyAsync(&lastOut, out + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    return (uint64_t)lastIn + lastOut;
+}
+
+namespace {
+__global__ void scatterFlagsKernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ offs, uint32_t* __restrict__ out, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flags[i])
+        out[offs[i]] = (uint32_t)i;
+}
+} // namespace
+
+uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s)
+{
+    if (n == 0)
+        return 0;
+    DevBuf<uint32_t> offs(n, s);
+    const uint64_t total = exclusiveScanU32Total(flags, offs.get(), n, s);
+    scatterFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(flags, offs.get(), out, n);
+    TDAG_CUDA(cudaGetLastError());
+    return (uint32_t)total;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits. Per pass: tile histograms -> exclusive scan over the
+// digit-major count matrix -> stable scatter (ranks from __match_any_sync within each 32-item round,
+// warps own contiguous sub-tiles so tile order == (warp, round, lane) order).
+// ------------------------------------------------------------------------------------------------
+namespace {
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortRounds = 16; // items per lane
+constexpr int kSortTile = kSortThreads * kSortRounds; // 4096
+
+__global__ void radixHistKernel(const uint64_t* __restrict__ keys, size_t n, uint32_t shift, uint32_t* __restrict__ counts, uint32_t numTiles)
+{
+    __shared__ uint32_t hist[256];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kSortTile;
+#pragma unroll 4
+    for (int k = 0; k < kSortRounds; ++k) {
+        const size_t i = base + (size_t)k * kSortThreads + threadIdx.x;
+        if (i < n)
+            atomicAdd(&hist[(uint32_t)(keys[i] >> shift) & 0xFF], 1u);
+    }
+    __syncthreads();
+    counts[(size_t)threadIdx.x * numTiles + blockIdx.x] = hist[threadIdx.x];
+}
+
+__global__ void radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn, uint64_t* __restrict__ keysOut,
+    uint32_t* __restrict__ valsOut, size_t n, uint32_t shift, const uint32_t* __restrict__ offsets, uint32_t numTiles)
+{
+    __shared__ uint32_t warpHist[kSortWarps][256];
+    __shared__ uint32_t base[kSortWarps][256];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads)
+        (&warpHist[0][0])[d] = 0;
+    __syncthreads();
+    const size_t warpBase = (size_t)blockIdx.x * kSortTile + (size_t)warp * (32 * kSortRounds);
+    uint64_t key[kSortRounds];
+    uint32_t val[kSortRounds];
+    const uint32_t ltMask = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const size_t i = warpBase + (size_t)r * 32 + lane;
+        const bool valid = i < n;
+        key[r] = valid ? keysIn[i] : 0;
+        val[r] = valid ? valsIn[i] : 0;
+        const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+        if (valid && (peers & ltMask) == 0)
+            warpHist[warp][digit] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x; // 256 threads == 256 digits
+        uint32_t run = offsets[(size_t)d * numTiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            base[w][d] = run;
+            run += warpHist[w][d];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const size_t i = warpBase + (size_t)r * 32 + lane;
+        const bool valid = i < n;
+        const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+        uint32_t pos = 0;
+        if (valid)
+            pos = base[warp][digit] + __popc(peers & ltMask);
+        __syncwarp();
+        if (valid && (peers & ltMask) == 0)
+            base[warp][digit] += __popc(peers);
+        __syncwarp();
+        if (valid) {
+            keysOut[pos] = key[r];
+            valsOut[pos] = val[r];
+        }
+    }
+}
+} // namespace
+
+void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s)
+{
+    if (n <= 1 || beginBit >= endBit)
+        return;
+    TDAG_CHECK(n < (1ull << 32), TDAG_ERR_ARG, "radix sort size exceeds 2^32");
+    const uint32_t numTiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    DevBuf<uint64_t> k2(n, s);
+    DevBuf<uint32_t> v2(n, s);
+    DevBuf<uint32_t> counts((size_t)256 * numTiles, s), offs((size_t)256 * numTiles, s);
+    uint64_t* kin = keys;
+    uint32_t* vin = vals;
+    uint64_t* kout = k2.get();
+    uint32_t* vout = v2.get();
+    uint32_t passes = 0;
+    for (uint32_t shift = beginBit; shift < endBit; shift += 8, ++passes) {
+        radixHistKernel<<<numTiles, kSortThreads, 0, s>>>(kin, n, shift, counts.get(), numTiles);
+        TDAG_CUDA(cudaGetLastError());
+        exclusiveScanU32(counts.get(), offs.get(), (size_t)256 * numTiles, s);
+        radixScatterKernel<<<numTiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
+        TDAG_CUDA(cudaGetLastError());
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    if (passes & 1) {
+        TDAG_CUDA(cudaMemcpyAsync(keys, kin, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+        TDAG_CUDA(cudaMemcpyAsync(vals, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    }
+}
+
+} // namespace tdag

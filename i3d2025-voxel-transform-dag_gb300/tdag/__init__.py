@@ -1,0 +1,330 @@
+"""Host-side mirror of the reference's Transform-DAG construction interface, on libtdag.so.
+
+The names follow tools/lib/include/voxcom/voxel/transform_dag.h and structure.h:
+
+* :class:`EditStructure` mirrors ``EditStructure<void, uint32_t>`` (structure.h:159-211) and
+  ``EditStructure<void, TransformPointer>`` (``child_type="transform"``), with the reference's
+  binary layout (``writeTo``/``readFrom``, structure.h:483-501) and the ``.svo`` wrapper
+  (export_import_structure.cpp:12-45).
+* :class:`TransformDAGConfig` mirrors ``TransformDAGConfig`` (transform_dag.h:157-160).
+* :func:`construct_transform_dag` mirrors ``constructTransformDAG`` (transform_dag.h:161-162),
+  :func:`construct_transform_dag_hierarchical` mirrors ``constructTransformDAGHierarchical``
+  (transform_dag.h:168-169) and :func:`find_duplicates_among_flattened_items` mirrors
+  ``findDuplicatesAmongFlattenedItems_cpp2`` (transform_dag.h:307-308).
+
+Every computation runs in libtdag.so on the GPU. There is no CPU fallback: if the library is
+missing or no CUDA device is present, the call raises :class:`TDagError`.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+import struct
+from typing import List, Optional
+
+import numpy as np
+
+from . import _abi
+from ._abi import TDagError, lib, library_path  # noqa: F401
+
+SVO_MAGIC = 72198382
+SVO_VERSION = 2
+EMPTY_CHILD = 0xFFFFFFFF
+
+
+# ------------------------------------------------------------------------------------------------
+# TransformPointer (transform_dag.h:19-151)
+# ------------------------------------------------------------------------------------------------
+PERMUTATIONS = ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0))
+PTR_MASK = (1 << 37) - 1
+
+
+def tp_create(ptr: int, symmetry=(False, False, False), axis_permutation=(0, 1, 2), translation=(0, 0, 0)) -> int:
+    """TransformPointer::create (transform_dag.h:46-54) as a raw uint64."""
+    v = ptr & PTR_MASK
+    v |= (int(symmetry[0]) | int(symmetry[1]) << 1 | int(symmetry[2]) << 2) << 37
+    v |= (axis_permutation[0] | axis_permutation[1] << 2 | axis_permutation[2] << 4) << 40
+    for k in range(3):
+        v |= ((translation[k] + 32) & 63) << (46 + 6 * k)
+    return v
+
+
+def tp_decode(v: int):
+    """(ptr, symmetry bools, axis permutation, translation) of a raw TransformPointer."""
+    v = int(v)
+    sym = (v >> 37) & 7
+    return (v & PTR_MASK, (bool(sym & 1), bool(sym & 2), bool(sym & 4)),
+            ((v >> 40) & 3, (v >> 42) & 3, (v >> 44) & 3),
+            tuple(((v >> (46 + 6 * k)) & 63) - 32 for k in range(3)))
+
+
+TP_SENTINEL = tp_create(0xFFFFFFFF)
+
+
+def encode_fixed64(v: int, level: int) -> int:
+    """TransformPointer::encodeFixed64 (transform_dag.h:375-397)."""
+    ptr, sym, perm, t = tp_decode(v)
+    out = ptr
+    out = (out << 3) | (2 * perm[0] + (1 if perm[2] < perm[1] else 0))
+    out = (out << 3) | (int(sym[0]) | int(sym[1]) << 1 | int(sym[2]) << 2)
+    if level:
+        sb = level + 1
+        for k in (2, 1, 0):
+            out = (out << sb) | (t[k] + (1 << level))
+    return out & 0xFFFFFFFFFFFFFFFF
+
+
+@dataclasses.dataclass
+class TransformDAGConfig:
+    """TransformDAGConfig (transform_dag.h:157-160)."""
+
+    symmetry: bool = True
+    axis_permutation: bool = True
+    translation: bool = True
+    max_translation_level: int = 4
+
+    def to_bytes(self) -> bytes:
+        # three bools, one padding byte (written as zero), uint32
+        return struct.pack("<???xI", self.symmetry, self.axis_permutation, self.translation, self.max_translation_level)
+
+    @classmethod
+    def from_bytes(cls, b: bytes) -> "TransformDAGConfig":
+        s, a, t, m = struct.unpack("<???xI", b[:8])
+        return cls(s, a, t, m)
+
+
+# ------------------------------------------------------------------------------------------------
+# EditStructure
+# ------------------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class EditStructure:
+    """EditStructure<void, Child>. ``nodes_per_level[l]`` is an (n, 8) array: uint32 children
+    (empty = 0xFFFFFFFF) for ``child_type="u32"``, uint64 TransformPointers for ``"transform"``.
+    ``sub_grids`` holds the level-2 4x4x4 Morton bitmasks."""
+
+    nodes_per_level: List[np.ndarray]
+    sub_grids: np.ndarray
+    resolution: int
+    root_level: int
+    structure_type: int = 0  # 0 = Tree, 1 = DAG
+    child_type: str = "u32"
+
+    SUB_GRID_LEVEL = 2
+
+    @property
+    def child_dtype(self):
+        return np.uint32 if self.child_type == "u32" else np.uint64
+
+    # ---- reference binary layout (BinaryWriter, binary_writer.h:48-78)
+    def to_bytes(self) -> bytes:
+        out = [struct.pack("<Q", len(self.nodes_per_level))]
+        for lvl in self.nodes_per_level:
+            a = np.ascontiguousarray(lvl, dtype=self.child_dtype).reshape(-1, 8)
+            out.append(struct.pack("<Q", a.shape[0]))
+            out.append(a.tobytes())
+        sg = np.ascontiguousarray(self.sub_grids, dtype=np.uint64)
+        out.append(struct.pack("<Q", sg.shape[0]))
+        out.append(sg.tobytes())
+        out.append(struct.pack("<III", self.resolution, self.root_level, self.structure_type))
+        return b"".join(out)
+
+    @classmethod
+    def from_bytes(cls, buf: bytes, offset: int = 0, child_type: str = "u32"):
+        """Parse a structure; returns (structure, offset after it)."""
+        dt = np.uint32 if child_type == "u32" else np.uint64
+        esz = 8 * np.dtype(dt).itemsize
+
+        def take(n):
+            nonlocal offset
+            if offset + n > len(buf):
+                raise TDagError(_abi.TDAG_ERR_CORRUPT, "truncated structure")
+            b = buf[offset: offset + n]
+            offset += n
+            return b
+
+        (nl,) = struct.unpack("<Q", take(8))
+        if nl > 64:
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "corrupt level count")
+        levels = []
+        for _ in range(nl):
+            (cnt,) = struct.unpack("<Q", take(8))
+            levels.append(np.frombuffer(take(cnt * esz), dtype=dt).reshape(cnt, 8).copy())
+        (cnt,) = struct.unpack("<Q", take(8))
+        sg = np.frombuffer(take(cnt * 8), dtype=np.uint64).copy()
+        res, root, st = struct.unpack("<III", take(12))
+        if root + 1 != nl:
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "root level does not match level count")
+        return cls(levels, sg, res, root, st, child_type), offset
+
+    # ---- .svo (export_import_structure.cpp:15-45)
+    def to_svo_bytes(self) -> bytes:
+        assert self.child_type == "u32"
+        return struct.pack("<II", SVO_MAGIC, SVO_VERSION) + self.to_bytes()
+
+    @classmethod
+    def from_svo_bytes(cls, buf: bytes) -> "EditStructure":
+        if len(buf) < 8:
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "truncated .svo")
+        magic, version = struct.unpack("<II", buf[:8])
+        if magic != SVO_MAGIC or version != SVO_VERSION:
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "bad .svo magic/version")
+        s, off = cls.from_bytes(buf, 8)
+        if off != len(buf):
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "trailing bytes in .svo")
+        return s
+
+    def compute_voxel_count(self) -> int:
+        """computeVoxelCount (structure.h:453-481): voxels of the expanded tree."""
+        if self.root_level < 3 or len(self.nodes_per_level[self.root_level]) == 0:
+            return 0
+        leaf_pc = np.array([bin(int(v)).count("1") for v in self.sub_grids], dtype=np.int64) if len(self.sub_grids) else np.zeros(0, np.int64)
+        counts = leaf_pc
+        for lvl in range(3, self.root_level + 1):
+            nodes = self.nodes_per_level[lvl].astype(np.int64)
+            empty = nodes == EMPTY_CHILD
+            safe = np.where(empty, 0, nodes)
+            counts = np.where(empty, 0, counts[safe] if len(counts) else 0).sum(axis=1)
+        return int(counts[0])
+
+
+def write_tdag(structure: EditStructure, config: TransformDAGConfig) -> bytes:
+    """.tdag: EditStructure<void, TransformPointer> then the raw TransformDAGConfig
+    (voxelizer/src/main.cpp:144-151)."""
+    assert structure.child_type == "transform"
+    return structure.to_bytes() + config.to_bytes()
+
+
+def read_tdag(buf: bytes):
+    s, off = EditStructure.from_bytes(buf, 0, child_type="transform")
+    cfg = TransformDAGConfig.from_bytes(buf[off: off + 8]) if len(buf) >= off + 8 else None
+    return s, cfg
+
+
+# ------------------------------------------------------------------------------------------------
+# Context + construction entry points
+# ------------------------------------------------------------------------------------------------
+class Context:
+    """One CUDA device + stream (tdag_ctx)."""
+
+    def __init__(self, device: int = 0, tuning: Optional[dict] = None):
+        L = lib()
+        t = _abi.Tuning()
+        for k, v in (tuning or {}).items():
+            setattr(t, k, v)
+        self._ptr = ctypes.c_void_p()
+        _abi.check(L.tdag_ctx_create(device, ctypes.byref(t), ctypes.byref(self._ptr)))
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._ptr
+
+    def close(self):
+        if self._ptr:
+            lib().tdag_ctx_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("TDAG_DEVICE", "0")))
+    return _default_ctx
+
+
+def _config_struct(cfg: TransformDAGConfig) -> _abi.Config:
+    c = _abi.Config()
+    c.symmetry = int(cfg.symmetry)
+    c.axis_permutation = int(cfg.axis_permutation)
+    c.translation = int(cfg.translation)
+    c.max_translation_level = int(cfg.max_translation_level)
+    return c
+
+
+def _view_of(dag: EditStructure, keep: list) -> _abi.SvdagView:
+    v = _abi.SvdagView()
+    v.resolution = dag.resolution
+    v.root_level = dag.root_level
+    v.structure_type = dag.structure_type
+    for lvl in range(3, dag.root_level + 1):
+        a = np.ascontiguousarray(dag.nodes_per_level[lvl], dtype=np.uint32)
+        keep.append(a)
+        v.nodes[lvl] = a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        v.node_counts[lvl] = a.shape[0]
+    sg = np.ascontiguousarray(dag.sub_grids, dtype=np.uint64)
+    keep.append(sg)
+    v.leaves = sg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    v.leaf_count = sg.shape[0]
+    return v
+
+
+def _take_result(rp) -> (EditStructure, dict):
+    r = rp.contents
+    try:
+        levels = []
+        for lvl in range(r.root_level + 1):
+            cnt = r.node_counts[lvl]
+            if lvl >= 3 and cnt:
+                a = np.ctypeslib.as_array(r.nodes[lvl], shape=(cnt * 8,)).copy().reshape(cnt, 8)
+            else:
+                a = np.zeros((0, 8), dtype=np.uint64)
+            levels.append(a)
+        leaves = np.ctypeslib.as_array(r.leaves, shape=(r.leaf_count,)).copy() if r.leaf_count else np.zeros(0, np.uint64)
+        stats = _abi.stats_to_dict(r.stats, r.root_level)
+        return EditStructure(levels, leaves, r.resolution, r.root_level, r.structure_type, "transform"), stats
+    finally:
+        lib().tdag_result_free(rp)
+
+
+def construct_transform_dag(in_dag: EditStructure, config: TransformDAGConfig = TransformDAGConfig(),
+                            ctx: Optional[Context] = None, return_stats: bool = False):
+    """constructTransformDAG (transform_dag.h:161-162): returns EditStructure<void, TransformPointer>.
+    Raises TDagError like the reference's assert_always when the input is not a DAG."""
+    ctx = ctx or default_context()
+    keep = []
+    view = _view_of(in_dag, keep)
+    rp = ctypes.POINTER(_abi.Result)()
+    _abi.check(lib().tdag_build(ctx.handle, ctypes.byref(view), ctypes.byref(_config_struct(config)), ctypes.byref(rp)))
+    out, stats = _take_result(rp)
+    return (out, stats) if return_stats else out
+
+
+def construct_transform_dag_hierarchical(in_dag: EditStructure, config: TransformDAGConfig = TransformDAGConfig(),
+                                         ctx: Optional[Context] = None) -> EditStructure:
+    """constructTransformDAGHierarchical(inDag, config) (transform_dag.h:168-169)."""
+    ctx = ctx or default_context()
+    keep = []
+    view = _view_of(in_dag, keep)
+    rp = ctypes.POINTER(_abi.Result)()
+    _abi.check(lib().tdag_build_hierarchical(ctx.handle, ctypes.byref(view), ctypes.byref(_config_struct(config)), ctypes.byref(rp)))
+    return _take_result(rp)[0]
+
+
+def find_duplicates_among_flattened_items(level: int, grids: np.ndarray, config: TransformDAGConfig = TransformDAGConfig(),
+                                          ctx: Optional[Context] = None, return_stats: bool = False):
+    """findDuplicatesAmongFlattenedItems_cpp2<level> (transform_dag.h:307-308) on dense grids
+    (n x R^3/64 uint64, bit x + R*y + R*R*z). Returns (unique positions, mapping TransformPointers)."""
+    ctx = ctx or default_context()
+    g = np.ascontiguousarray(grids, dtype=np.uint64)
+    n = g.shape[0]
+    mapping = np.zeros(n, np.uint64)
+    uniq = np.zeros(max(n, 1), np.uint32)
+    nu = ctypes.c_uint32()
+    st = _abi.LevelStats()
+    _abi.check(lib().tdag_find_duplicates_level(ctx.handle, level, g.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n,
+                                                ctypes.byref(_config_struct(config)),
+                                                mapping.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                                uniq.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(nu),
+                                                ctypes.byref(st)))
+    res = (uniq[: nu.value].copy(), mapping)
+    return (res + (_abi.level_stats_to_dict(st),)) if return_stats else res

@@ -1,0 +1,123 @@
+"""ctypes declarations of the C ABI in include/tdag.h (libtdag.so)."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+_LIB_FILE = os.path.join(PKG, "build", "libtdag.so")
+
+TDAG_OK = 0
+TDAG_ERR_ARG = 1
+TDAG_ERR_OOM = 2
+TDAG_ERR_TABLE_FULL = 3
+TDAG_ERR_ALLOC = 4
+TDAG_ERR_CUDA = 5
+TDAG_ERR_CORRUPT = 6
+TDAG_ERR_NO_DEVICE = 7
+MAX_LEVELS = 32
+
+ERROR_NAMES = {1: "ARG", 2: "OOM", 3: "TABLE_FULL", 4: "ALLOC", 5: "CUDA", 6: "CORRUPT", 7: "NO_DEVICE"}
+
+
+class TDagError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"tdag error {code} ({ERROR_NAMES.get(code, '?')}): {message}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("symmetry", ctypes.c_int32), ("axis_permutation", ctypes.c_int32),
+                ("translation", ctypes.c_int32), ("max_translation_level", ctypes.c_uint32)]
+
+
+class SvdagView(ctypes.Structure):
+    _fields_ = [("resolution", ctypes.c_uint32), ("root_level", ctypes.c_uint32),
+                ("structure_type", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("nodes", ctypes.POINTER(ctypes.c_uint32) * MAX_LEVELS),
+                ("node_counts", ctypes.c_uint64 * MAX_LEVELS),
+                ("leaves", ctypes.POINTER(ctypes.c_uint64)), ("leaf_count", ctypes.c_uint64)]
+
+
+class LevelStats(ctypes.Structure):
+    _fields_ = [("items", ctypes.c_uint64), ("unique", ctypes.c_uint64), ("probes", ctypes.c_uint64),
+                ("filter_pass", ctypes.c_uint64), ("hits", ctypes.c_uint64), ("candidates", ctypes.c_uint64),
+                ("verifications", ctypes.c_uint64), ("verified", ctypes.c_uint64),
+                ("table_entries", ctypes.c_uint64), ("search_ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("hierarchical", LevelStats * MAX_LEVELS), ("translation", LevelStats * MAX_LEVELS),
+                ("total_ms", ctypes.c_float), ("hierarchical_ms", ctypes.c_float),
+                ("translation_ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("resolution", ctypes.c_uint32), ("root_level", ctypes.c_uint32),
+                ("structure_type", ctypes.c_uint32), ("on_device", ctypes.c_uint32),
+                ("nodes", ctypes.POINTER(ctypes.c_uint64) * MAX_LEVELS),
+                ("node_counts", ctypes.c_uint64 * MAX_LEVELS),
+                ("leaves", ctypes.POINTER(ctypes.c_uint64)), ("leaf_count", ctypes.c_uint64),
+                ("stats", Stats)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("filter_bits_per_key", ctypes.c_uint32), ("table_load_percent", ctypes.c_uint32),
+                ("search_ctas_per_sm", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+# Every symbol include/tdag.h declares (checked by the CPU test-suite).
+EXPORTED = (
+    "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
+    "tdag_build", "tdag_build_device", "tdag_result_free", "tdag_find_duplicates_level", "tdag_build_hierarchical",
+)
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_FILE
+
+
+def lib(path: str = None):
+    """Load libtdag.so. Raises TDagError if it has not been built (no fallback path exists)."""
+    global _lib
+    if _lib is None:
+        p = path or _LIB_FILE
+        if not os.path.exists(p):
+            raise TDagError(TDAG_ERR_NO_DEVICE, f"libtdag.so not built at {p}; run build_lib.py (or __graft_entry__.build())")
+        L = ctypes.CDLL(p)
+        vp = ctypes.c_void_p
+        L.tdag_version.restype = ctypes.c_char_p
+        L.tdag_last_error_message.restype = ctypes.c_char_p
+        L.tdag_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(Tuning), ctypes.POINTER(vp)]
+        L.tdag_ctx_destroy.argtypes = [vp]
+        L.tdag_ctx_stream.argtypes = [vp, ctypes.POINTER(vp)]
+        L.tdag_build.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), ctypes.POINTER(ctypes.POINTER(Result))]
+        L.tdag_build_device.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), ctypes.POINTER(ctypes.POINTER(Result))]
+        L.tdag_build_hierarchical.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), ctypes.POINTER(ctypes.POINTER(Result))]
+        L.tdag_result_free.argtypes = [ctypes.POINTER(Result)]
+        L.tdag_find_duplicates_level.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                                 ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_uint64),
+                                                 ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                                 ctypes.POINTER(LevelStats)]
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != TDAG_OK:
+        raise TDagError(rc, lib().tdag_last_error_message().decode(errors="replace"))
+
+
+def level_stats_to_dict(s: LevelStats) -> dict:
+    return {k: getattr(s, k) for k, _ in LevelStats._fields_ if k != "reserved"}
+
+
+def stats_to_dict(s: Stats, root_level: int) -> dict:
+    return {
+        "total_ms": s.total_ms, "hierarchical_ms": s.hierarchical_ms, "translation_ms": s.translation_ms,
+        "hierarchical": {l: level_stats_to_dict(s.hierarchical[l]) for l in range(2, root_level + 1)},
+        "translation": {l: level_stats_to_dict(s.translation[l]) for l in range(2, 5)},
+    }

@@ -1,0 +1,147 @@
+/* tdag.h — C ABI of libtdag.so, the GB300 (sm_103a) Transform-Aware SVDAG construction library.
+ *
+ * Plain C: fixed-width integers, plain pointers and sizes; no C++ or torch types.
+ * Every entry point returns an int status (TDAG_OK = 0). The message of the last failure on the
+ * calling thread is returned by tdag_last_error_message().
+ *
+ * The layouts mirror the reference's in-memory structures, so a caller can hand its vectors over
+ * without conversion:
+ *   EditNode<uint32_t>           = 8 x uint32_t, empty child 0xFFFFFFFF
+ *                                  (tools/lib/include/voxcom/voxel/structure.h:44-69)
+ *   EditSubGrid<void>            = uint64_t Morton-order 4x4x4 occupancy mask (structure.h:116-125)
+ *   EditNode<TransformPointer>   = 8 x uint64_t TransformPointer (transform_dag.h:19-33)
+ *   TransformDAGConfig           = {bool symmetry, axisPermutation, translation; uint32_t maxTranslationLevel}
+ *                                  (tools/lib/include/voxcom/voxel/transform_dag.h:157-160)
+ */
+#ifndef TDAG_H_
+#define TDAG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDAG_OK 0
+#define TDAG_ERR_ARG 1 /* invalid argument / unsupported configuration */
+#define TDAG_ERR_OOM 2 /* device or host allocation failed */
+#define TDAG_ERR_TABLE_FULL 3 /* a bounded hash-table probe sequence ran out (never spins) */
+#define TDAG_ERR_ALLOC 4 /* a bounded device sub-allocation failed */
+#define TDAG_ERR_CUDA 5 /* a CUDA runtime call failed */
+#define TDAG_ERR_CORRUPT 6 /* malformed input structure (dangling child pointer, bad sizes) */
+#define TDAG_ERR_NO_DEVICE 7 /* no CUDA device / kernels not loadable for this GPU */
+
+#define TDAG_MAX_LEVELS 32
+
+typedef struct tdag_ctx tdag_ctx;
+
+/* TransformDAGConfig (transform_dag.h:157-160). */
+typedef struct tdag_config {
+    int32_t symmetry; /* search mirror transforms */
+    int32_t axis_permutation; /* search axis permutations */
+    int32_t translation; /* run the translation matcher on levels 2..max_translation_level */
+    uint32_t max_translation_level; /* 2..4 when translation != 0 (reference default 4) */
+} tdag_config;
+
+/* Read-only view of an EditStructure<void, uint32_t> (structure.h:159-211). Pointers are host
+ * memory for tdag_build() and device memory for tdag_build_device(). nodes[l] holds node_counts[l]
+ * EditNode<uint32_t> (8 x u32 each) for l in [3, root_level]; leaves holds the level-2 subgrids. */
+typedef struct tdag_svdag_view {
+    uint32_t resolution;
+    uint32_t root_level;
+    uint32_t structure_type; /* 0 = Tree, 1 = DAG (constructTransformDAG requires DAG) */
+    uint32_t reserved;
+    const uint32_t* nodes[TDAG_MAX_LEVELS];
+    uint64_t node_counts[TDAG_MAX_LEVELS];
+    const uint64_t* leaves;
+    uint64_t leaf_count;
+} tdag_svdag_view;
+
+/* Per-level statistics of one build. Index = tree level (2 = leaves). */
+typedef struct tdag_level_stats {
+    uint64_t items; /* items entering the stage at this level */
+    uint64_t unique; /* items kept */
+    uint64_t probes; /* non-empty directional hash values looked up (translation levels) */
+    uint64_t filter_pass; /* lookups that passed the membership filter */
+    uint64_t hits; /* lookups that found a corner-hash range */
+    uint64_t candidates; /* candidate (target, corner) pairs examined */
+    uint64_t verifications; /* exact grid comparisons */
+    uint64_t verified; /* comparisons that matched */
+    uint64_t table_entries; /* non-zero corner hashes in the table */
+    float search_ms; /* device time of the search kernel(s) */
+    float reserved;
+} tdag_level_stats;
+
+typedef struct tdag_stats {
+    tdag_level_stats hierarchical[TDAG_MAX_LEVELS];
+    tdag_level_stats translation[TDAG_MAX_LEVELS];
+    float total_ms; /* device time of the whole construction (tdag_build*: without host copies) */
+    float hierarchical_ms;
+    float translation_ms;
+    float reserved;
+} tdag_stats;
+
+/* EditStructure<void, TransformPointer> result. Arrays are owned by the library: host memory from
+ * tdag_build(), device memory from tdag_build_device(). Release with tdag_result_free(). */
+typedef struct tdag_result {
+    uint32_t resolution;
+    uint32_t root_level;
+    uint32_t structure_type; /* 0 (the reference's output EditStructure is default-constructed) */
+    uint32_t on_device;
+    uint64_t* nodes[TDAG_MAX_LEVELS]; /* node_counts[l] x 8 TransformPointer (u64) */
+    uint64_t node_counts[TDAG_MAX_LEVELS];
+    uint64_t* leaves;
+    uint64_t leaf_count;
+    tdag_stats stats;
+} tdag_result;
+
+/* Tuning knobs (0 = library default). */
+typedef struct tdag_tuning {
+    uint32_t filter_bits_per_key; /* membership filter size (power of two rounded) */
+    uint32_t table_load_percent; /* corner-hash table load factor in percent (50..85) */
+    uint32_t search_ctas_per_sm; /* persistent search CTAs per SM */
+    uint32_t reserved;
+} tdag_tuning;
+
+/* Library/version information. */
+const char* tdag_version(void);
+const char* tdag_last_error_message(void);
+
+/* Context = one CUDA device + one stream + a stream-ordered memory pool. Calls on one context are
+ * serialised by the caller; separate contexts may be used from separate threads. */
+int tdag_ctx_create(int device, const tdag_tuning* tuning, tdag_ctx** out_ctx);
+int tdag_ctx_destroy(tdag_ctx* ctx);
+/* Underlying cudaStream_t (as void*) for callers that want to order their own work with the library's. */
+int tdag_ctx_stream(tdag_ctx* ctx, void** out_stream);
+
+/* constructTransformDAG<Structure>(inDag, config)
+ * (tools/lib/include/voxcom/voxel/transform_dag.h:161-162; tools/lib/src/voxel/transform_dag.cpp:138-240).
+ * Input in host memory; result in host memory. Host<->device copies are part of the call. */
+int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in_host, const tdag_config* config, tdag_result** out);
+
+/* Same as tdag_build with the input already resident in device memory and the result left there. */
+int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, const tdag_config* config, tdag_result** out);
+
+int tdag_result_free(tdag_result* result);
+
+/* findDuplicatesAmongFlattenedItems_cpp2<Level>(items, grids, outPrevLevelMapping, config)
+ * (transform_dag.h:307-308; tools/lib/src/voxel/find_translation.cpp:616-1000), on dense grids:
+ * grids = n x (R^3 / 64) uint64 words, R = 1 << level, bit index x + R*y + R*R*z
+ * (LargeSubGrid, tools/lib/include/voxcom/voxel/large_sub_grid.h:80-97). Host pointers.
+ * out_mapping[n]: TransformPointer of every item into the unique list; out_unique[n]: positions of
+ * the kept items (ascending); *n_unique: their count. stats may be NULL. */
+int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* grids, uint32_t n,
+    const tdag_config* config, uint64_t* out_mapping, uint32_t* out_unique, uint32_t* n_unique,
+    tdag_level_stats* stats);
+
+/* constructTransformDAGHierarchical(inDag, config) (transform_dag.h:168-169;
+ * tools/lib/src/voxel/transform_dag_hierarchical.cpp:304-529): symmetry + permutation only.
+ * Host in, host out. */
+int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in_host, const tdag_config* config, tdag_result** out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDAG_H_ */

@@ -1,0 +1,166 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+The oracle (``tdag_oracle.cpp``) is a from-scratch CPU restatement of the reference's
+Transform-DAG construction path. Only the test-suite, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg / reference arm may import this module; the product library
+(``libtdag.so``) never links or calls it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++ -O3 -fopenmp)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "tdag_oracle.cpp"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        u8pp = ctypes.POINTER(u8p)
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_svo_from_dense.argtypes = [u8p, ctypes.c_uint32, u8pp, u64p]
+        L.orc_to_dag.argtypes = [u8p, ctypes.c_uint64, u8pp, u64p]
+        L.orc_construct_tdag.argtypes = [u8p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_uint32, u8pp, u64p, u64p, u64p]
+        L.orc_find_duplicates.argtypes = [ctypes.c_uint32, u64p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, u64p, u32p, u32p, u64p]
+        L.orc_hierarchical.argtypes = [u8p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, u8pp, u64p]
+        L.orc_tdag_decode.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
+        L.orc_transform_tables.argtypes = [u8p, u8p, u8p]
+        L.orc_encode_fixed64.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
+        L.orc_encode_fixed64.restype = ctypes.c_uint64
+        L.orc_decode_fixed64.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
+        L.orc_decode_fixed64.restype = ctypes.c_uint64
+        L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _u8(buf: bytes):
+    a = np.frombuffer(buf, dtype=np.uint8)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def _take(out, n) -> bytes:
+    try:
+        return ctypes.string_at(out, n.value)
+    finally:
+        lib().orc_free(out)
+
+
+def _chk(rc):
+    if rc != 0:
+        raise OracleError(lib().orc_last_error().decode())
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def svo_from_dense(dense: np.ndarray) -> bytes:
+    """A1: EditStructure(VoxelGrid) -> .svo bytes. ``dense[z, y, x]`` (x fastest), bool/uint8."""
+    d = np.ascontiguousarray(dense, dtype=np.uint8)
+    res = d.shape[0]
+    assert d.shape == (res, res, res)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    _chk(lib().orc_svo_from_dense(d.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), res, ctypes.byref(out), ctypes.byref(n)))
+    return _take(out, n)
+
+
+def to_dag(svo: bytes) -> bytes:
+    """A2: EditStructure::toDAG on .svo bytes."""
+    a, p = _u8(svo)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    _chk(lib().orc_to_dag(p, len(svo), ctypes.byref(out), ctypes.byref(n)))
+    return _take(out, n)
+
+
+STAT_KEYS = ("items", "probes", "hits", "candidates", "verifications", "verified", "table_entries", "unique")
+
+
+def construct_tdag(svo: bytes, symmetry=True, axis=True, translation=True, max_level=4):
+    """A6: constructTransformDAG -> (.tdag bytes incl. trailing config, stats dict, times_ns)."""
+    a, p = _u8(svo)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    st = (ctypes.c_uint64 * 8)()
+    tm = (ctypes.c_uint64 * 4)()
+    _chk(lib().orc_construct_tdag(p, len(svo), int(symmetry), int(axis), int(translation), int(max_level),
+                                  ctypes.byref(out), ctypes.byref(n), st, tm))
+    return _take(out, n), dict(zip(STAT_KEYS, list(st))), list(tm)
+
+
+def hierarchical(svo: bytes, symmetry=True, axis=True) -> bytes:
+    a, p = _u8(svo)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    _chk(lib().orc_hierarchical(p, len(svo), int(symmetry), int(axis), ctypes.byref(out), ctypes.byref(n)))
+    return _take(out, n)
+
+
+def find_duplicates(level: int, grids: np.ndarray, symmetry=True, axis=True, translation=True):
+    """Inner seam findDuplicatesAmongFlattenedItems_cpp2<level> on dense grids (n x W uint64)."""
+    g = np.ascontiguousarray(grids, dtype=np.uint64)
+    n = g.shape[0]
+    mapping = np.zeros(n, dtype=np.uint64)
+    uniq = np.zeros(max(n, 1), dtype=np.uint32)
+    nu = ctypes.c_uint32()
+    st = (ctypes.c_uint64 * 8)()
+    _chk(lib().orc_find_duplicates(level, g.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n, int(symmetry), int(axis),
+                                   int(translation), mapping.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                   uniq.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(nu), st))
+    return mapping, uniq[: nu.value].copy(), dict(zip(STAT_KEYS, list(st)))
+
+
+def tdag_decode(tdag: bytes, res: int) -> np.ndarray:
+    a, p = _u8(tdag)
+    dense = np.zeros((res, res, res), dtype=np.uint8)
+    _chk(lib().orc_tdag_decode(p, len(tdag), dense.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), res))
+    return dense
+
+
+def transform_tables():
+    c = np.zeros((48, 48), np.uint8)
+    i = np.zeros(48, np.uint8)
+    p = np.zeros((48, 8), np.uint8)
+    f = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    lib().orc_transform_tables(f(c), f(i), f(p))
+    return c, i, p
+
+
+def encode_fixed64(tp: int, level: int) -> int:
+    return int(lib().orc_encode_fixed64(tp, level))
+
+
+def decode_fixed64(e: int, level: int) -> int:
+    return int(lib().orc_decode_fixed64(e, level))

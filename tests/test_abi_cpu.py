@@ -1,0 +1,77 @@
+"""CPU tests of the product's host side: the C ABI's symbol table and the reference formats."""
+import ctypes
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def header_functions():
+    src = open(os.path.join(REPO, "include", "tdag.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(tdag_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(tdaglib):
+    lib = ctypes.CDLL(tdaglib.library_path())
+    names = header_functions()
+    assert names, "no functions parsed from include/tdag.h"
+    for n in names:
+        assert hasattr(lib, n), f"libtdag.so does not export {n}"
+    from tdag import _abi
+    assert set(_abi.EXPORTED) == set(names)
+
+
+def test_version_string(tdaglib):
+    assert b"sm_103a" in tdaglib.lib().tdag_version()
+
+
+def test_context_without_gpu_fails_loudly(tdaglib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(tdaglib.TDagError) as ei:
+        tdaglib.Context(0)
+    assert ei.value.code == 7  # TDAG_ERR_NO_DEVICE
+
+
+def test_config_bytes_layout(tdaglib):
+    c = tdaglib.TransformDAGConfig(True, False, True, 4)
+    b = c.to_bytes()
+    assert len(b) == 8 and b[:4] == b"\x01\x00\x01\x00" and struct.unpack("<I", b[4:])[0] == 4
+    assert tdaglib.TransformDAGConfig.from_bytes(b) == c
+
+
+def test_tdag_format_roundtrip(oracle, tdaglib):
+    from helpers import blocky_grid, dag_svo_bytes
+    svo = dag_svo_bytes(oracle, blocky_grid(32, 4))
+    ref, _, _ = oracle.construct_tdag(svo)
+    s, cfg = tdaglib.read_tdag(ref)
+    assert cfg == tdaglib.TransformDAGConfig()
+    assert tdaglib.write_tdag(s, cfg) == ref
+
+
+def test_corrupt_svo_rejected(tdaglib):
+    with pytest.raises(tdaglib.TDagError):
+        tdaglib.EditStructure.from_svo_bytes(b"\x00" * 4)
+    with pytest.raises(tdaglib.TDagError):
+        tdaglib.EditStructure.from_svo_bytes(struct.pack("<II", 72198382, 2) + struct.pack("<Q", 3))
+
+
+def test_tp_sentinel_layout(tdaglib):
+    # create(0xFFFFFFFF): identity permutation (0,1,2) and translations biased by 32
+    v = tdaglib.TP_SENTINEL
+    assert v & ((1 << 37) - 1) == 0xFFFFFFFF
+    assert (v >> 40) & 63 == (0 | 1 << 2 | 2 << 4)
+    assert all(((v >> (46 + 6 * k)) & 63) == 32 for k in range(3))
+
+
+def test_voxel_count(oracle, tdaglib):
+    from helpers import blocky_grid
+    d = blocky_grid(32, 8)
+    s = tdaglib.EditStructure.from_svo_bytes(oracle.to_dag(oracle.svo_from_dense(d)))
+    assert s.compute_voxel_count() == int(d.sum())
