@@ -20,6 +20,8 @@
 
 namespace tdag {
 
+std::atomic<uint64_t> g_kernelLaunches { 0 };
+
 // ------------------------------------------------------------------------------------------------
 // Transform tables
 // ------------------------------------------------------------------------------------------------
@@ -210,7 +212,7 @@ static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& 
         TDAG_CUDA(cudaMemsetAsync(ref.get(), 0, numItems * 4, s));
     if (count8) {
         markReferencedKernel<<<gridFor(count8, 256), 256, 0, s>>>(parents.get(), count8, ref.get(), numItems, ctx.status);
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
     }
     DevBuf<uint32_t> indices(numItems, s);
     const uint32_t m = compactFlags(ref.get(), indices.get(), numItems, s);
@@ -225,7 +227,7 @@ static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& 
     lp.leaves = in.leaves;
     if (m) {
         flattenKernel<L><<<gridFor((size_t)m * W, 256), 256, 0, s>>>(lp, indices.get(), m, grids.get(), ctx.status);
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
     }
     tdag_level_stats* ls = stats ? &stats->translation[L] : nullptr;
     MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls);
@@ -235,21 +237,21 @@ static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& 
         out.leaves = DevBuf<uint64_t>(u, s);
         if (u) {
             emitOriginalLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(in.leaves, indices.get(), mo.uniques.get(), u, out.leaves.get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
     } else {
         out.levels[L] = DevBuf<uint64_t>((size_t)u * 8, s);
         if (u) {
             emitOriginalNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(in.nodes[L], indices.get(), mo.uniques.get(), u, out.levels[L].get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
     }
     if (count8 && m) {
         DevBuf<uint32_t> rankOf(numItems, s);
         rankKernel<<<gridFor(m, 256), 256, 0, s>>>(indices.get(), m, rankOf.get());
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
         remapParentsKernel<<<gridFor(count8, 256), 256, 0, s>>>(parents.get(), count8, rankOf.get(), mo.mapping.get());
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
     }
 }
 
@@ -261,7 +263,7 @@ static void validateInput(Context& ctx, const DeviceSvdag& in)
         const uint64_t count8 = in.nodeCounts[level] * 8;
         if (count8) {
             validateChildrenKernel<<<gridFor(count8, 256), 256, 0, s>>>(in.nodes[level], count8, childCount, level, ctx.status);
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
     }
     ctx.checkStatus("input validation");
@@ -280,6 +282,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
     TDAG_CHECK(in.leafCount < (1ull << 31), TDAG_ERR_ARG, "too many leaves");
     validateInput(ctx, in);
     cudaStream_t s = ctx.stream;
+    const uint64_t launches0 = g_kernelLaunches.load();
     TDAG_CUDA(cudaEventRecord(ctx.ev[2], s));
     const uint32_t midLevel = cfg.max_translation_level + 1;
     HierOutput h = runHierarchical(ctx, in, cfg, cfg.translation ? midLevel : 0xFFFFFFFFu, stats);
@@ -297,7 +300,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
         TDAG_CHECK(h.midInv.n == u, TDAG_ERR_CORRUPT, "mid level size mismatch");
         if (u) {
             emitOriginalNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(in.nodes[midLevel], h.midInv.get(), nullptr, u, out.levels[midLevel].get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
         h.midInv.release();
         for (int L = (int)cfg.max_translation_level; L >= 2; --L) {
@@ -315,6 +318,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
         TDAG_CUDA(cudaEventElapsedTime(&stats->hierarchical_ms, ctx.ev[2], ctx.ev[3]));
         TDAG_CUDA(cudaEventElapsedTime(&stats->translation_ms, ctx.ev[3], ctx.ev[4]));
         TDAG_CUDA(cudaEventElapsedTime(&stats->total_ms, ctx.ev[2], ctx.ev[4]));
+        stats->kernel_launches = g_kernelLaunches.load() - launches0;
     }
     return out;
 }
@@ -397,6 +401,11 @@ tdag_result* newResult(uint32_t res, uint32_t root, bool onDevice)
 }
 
 } // namespace
+
+// Shared with the other C-ABI translation units.
+Context& ctxOf(tdag_ctx* c) { return c->c; }
+int guardedCall(const std::function<void()>& f) { return guarded(f); }
+int failWith(int code, const char* msg) { return fail(code, msg); }
 
 extern "C" {
 

@@ -7,6 +7,7 @@
 //   hash_combine ........................... tools/lib/include/voxcom/utility/hash.h:10-20
 #pragma once
 #include <cstdint>
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -35,6 +36,15 @@ struct Error : std::runtime_error {
         cudaError_t e_ = (call);                                                                                \
         if (e_ != cudaSuccess)                                                                                  \
             throw ::tdag::Error(TDAG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " @" + __FILE__ + ":" + std::to_string(__LINE__)); \
+    } while (0)
+
+// Every kernel launch of the library is followed by TDAG_LAUNCHED(): it checks the launch and
+// counts it (the count is reported per build as tdag_stats::kernel_launches).
+extern std::atomic<uint64_t> g_kernelLaunches;
+#define TDAG_LAUNCHED()                                                              \
+    do {                                                                             \
+        TDAG_CUDA(cudaGetLastError());                                               \
+        ::tdag::g_kernelLaunches.fetch_add(1, std::memory_order_relaxed);             \
     } while (0)
 
 #define TDAG_CHECK(cond, code, msg)                \

@@ -18,13 +18,13 @@
 // TaggedPointer::operator== (:79-122) says they are equal.
 #include "common.cuh"
 #include "internal.cuh"
+#include "class_table.cuh"
 
 namespace tdag {
 
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint64_t kEmptySlot = ~0ull;
 
 struct SmemTables {
     uint8_t compose[48][48];
@@ -307,53 +307,6 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
     }
 }
 
-// ---------------------------------------------------------------------------- class table
-// Slot = tag << 32 | claimer index. A node belongs to a slot when its full signature equals the
-// claimer's. minIdx[slot] collects the class minimum. Probing is bounded by the capacity.
-template <int W>
-__global__ void __launch_bounds__(kThreads) classInsertKernel(const uint64_t* __restrict__ sig, uint32_t n, uint64_t* __restrict__ slots,
-    uint32_t* __restrict__ minIdx, uint32_t* __restrict__ slotOf, uint64_t capMask, uint32_t* status)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    uint64_t s[W];
-    uint64_t fp = 0x5bd1e995ull;
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-        s[k] = sig[(size_t)i * W + k];
-        fp = mix64(fp ^ s[k]);
-    }
-    const uint32_t tag = (uint32_t)(fp >> 32);
-    uint64_t slot = fp & capMask;
-    for (uint64_t probe = 0; probe <= capMask; ++probe) {
-        uint64_t cur = slots[slot];
-        if (cur == kEmptySlot) {
-            const uint64_t mine = ((uint64_t)tag << 32) | i;
-            cur = atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine);
-            if (cur == kEmptySlot) {
-                slotOf[i] = (uint32_t)slot;
-                atomicMin(&minIdx[slot], i);
-                return;
-            }
-        }
-        if ((uint32_t)(cur >> 32) == tag) {
-            const uint32_t j = (uint32_t)cur;
-            bool eq = true;
-#pragma unroll
-            for (int k = 0; k < W; ++k)
-                eq &= (sig[(size_t)j * W + k] == s[k]);
-            if (eq) {
-                slotOf[i] = (uint32_t)slot;
-                atomicMin(&minIdx[slot], i);
-                return;
-            }
-        }
-        slot = (slot + 1) & capMask;
-    }
-    setDeviceError(status, TDAG_ERR_TABLE_FULL, 100);
-}
-
 // ---------------------------------------------------------------------------- emission
 __global__ void gatherSortInputKernel(const uint32_t* __restrict__ canonList, uint32_t u, const uint64_t* __restrict__ key, uint64_t* __restrict__ sk, uint32_t* __restrict__ sv)
 {
@@ -432,15 +385,17 @@ uint64_t pow2AtLeast(uint64_t v)
 
 void fillU64(uint64_t* p, uint64_t v, size_t n, cudaStream_t s)
 {
-    if (n)
-        fillU64Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
-    TDAG_CUDA(cudaGetLastError());
+    if (!n)
+        return;
+    fillU64Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
+    TDAG_LAUNCHED();
 }
 void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s)
 {
-    if (n)
-        fillU32Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
-    TDAG_CUDA(cudaGetLastError());
+    if (!n)
+        return;
+    fillU32Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
+    TDAG_LAUNCHED();
 }
 
 // Shared tail of one level: class table -> canonicals -> emission order -> mapping.
@@ -459,7 +414,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
         classInsertKernel<1><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
     else
         classInsertKernel<8><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     slots.release();
 
     DevBuf<uint32_t> canonOf(n, s), isCanon(n, s);
@@ -476,7 +431,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     DevBuf<uint64_t> sk(u, s);
     emitOrder = DevBuf<uint32_t>(u, s);
     gatherSortInputKernel<<<gridFor(u, 256), 256, 0, s>>>(canonList.get(), u, key, sk.get(), emitOrder.get());
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     canonList.release();
     radixSortPairs(sk.get(), emitOrder.get(), u, 0, 64, s);
     sk.release();
@@ -484,7 +439,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     DevBuf<uint32_t> handleOf(n, s);
     invOut = DevBuf<uint64_t>(u, s);
     handleKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, invOf.get(), handleOf.get(), invOut.get());
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     mapOut = DevBuf<uint64_t>(n, s);
     uint32_t* mid = nullptr;
     if (midInv) {
@@ -493,7 +448,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
         mid = midInv->get();
     }
     mappingKernel<<<gridFor(n, 256), 256, 0, s>>>(n, canonOf.get(), tOf.get(), handleOf.get(), ctx.tables, mapOut.get(), mid);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     return u;
 }
 
@@ -522,19 +477,19 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         DevBuf<uint64_t> sig(n, s), key(n, s);
         if (n) {
             leafSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(in.leaves, n, ctx.tables, dCanonByte.get(), allowed, sig.get(), key.get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
         const uint64_t* leaves = in.leaves;
         auto resolve = [&](const uint32_t* slotOf, const uint32_t* minIdx, uint32_t* canonOf, uint8_t* tOf, uint64_t* invOf, uint32_t* isCanon) {
             leafResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(leaves, n, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, ctx.status);
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         };
         DevBuf<uint32_t> emitOrder;
         const uint32_t u = n ? canonicaliseLevel(ctx, 2, n, sig.get(), 1, key.get(), resolve, prevMap, prevInv, emitOrder, midLevel == 2 ? &out.midInv : nullptr) : 0;
         out.leaves = DevBuf<uint64_t>(u, s);
         if (u) {
             emitLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, in.leaves, out.leaves.get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
         if (stats) {
             stats->hierarchical[2].items = n;
@@ -547,13 +502,13 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         DevBuf<uint64_t> sig((size_t)n * 8, s), key(n, s);
         if (n) {
             nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevInv.get(), ctx.tables, allowed, sig.get(), key.get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
         const uint64_t* pm = prevMap.get();
         const uint64_t* pi = prevInv.get();
         auto resolve = [&](const uint32_t* slotOf, const uint32_t* minIdx, uint32_t* canonOf, uint8_t* tOf, uint64_t* invOf, uint32_t* isCanon) {
             nodeResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, pm, pi, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, level, ctx.status);
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         };
         DevBuf<uint64_t> map, inv;
         DevBuf<uint32_t> emitOrder;
@@ -564,7 +519,7 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         lvl = DevBuf<uint64_t>((size_t)u * 8, s);
         if (u) {
             emitNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(emitOrder.get(), u, nodes, prevMap.get(), lvl.get());
-            TDAG_CUDA(cudaGetLastError());
+            TDAG_LAUNCHED();
         }
         prevMap = std::move(map);
         prevInv = std::move(inv);

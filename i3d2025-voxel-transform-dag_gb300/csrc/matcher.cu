@@ -471,10 +471,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     {
         DevBuf<uint64_t> key(n, s);
         popcountKeyKernel<W><<<gridFor(n, 256), 256, 0, s>>>(grids, n, R * R * R, key.get(), order.get());
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
         radixSortPairs(key.get(), order.get(), n, 0, 16, s);
         invertOrderKernel<<<gridFor(n, 256), 256, 0, s>>>(order.get(), n, posOf.get());
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
     }
 
     // corner hashes + table
@@ -482,7 +482,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint64_t> ekeys(m, s);
     DevBuf<uint32_t> epay(m, s);
     cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, ekeys.get(), epay.get());
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     const uint32_t loadPct = ctx.tuning.table_load_percent ? std::min(85u, std::max(25u, ctx.tuning.table_load_percent)) : 50u;
     const uint64_t cap = pow2AtLeast(m * 100 / loadPct + 16);
     DevBuf<uint64_t> tkeys(cap, s), tranges(cap, s);
@@ -491,7 +491,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CUDA(cudaMemsetAsync(tcount.get(), 0, cap * 4, s));
     TDAG_CUDA(cudaMemsetAsync(numDistinct.get(), 0, 4, s));
     tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), m, tkeys.get(), tcount.get(), slotOfEntry.get(), cap - 1, numDistinct.get(), ctx.status);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     const uint64_t numEntries = exclusiveScanU32Total(tcount.get(), tstart.get(), cap, s);
     uint32_t distinct = 0;
     TDAG_CUDA(cudaMemcpyAsync(&distinct, numDistinct.get(), 4, cudaMemcpyDeviceToHost, s));
@@ -501,14 +501,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         DevBuf<uint32_t> tfill(cap, s);
         TDAG_CUDA(cudaMemsetAsync(tfill.get(), 0, cap * 4, s));
         tableScatterKernel<<<gridFor(m, 256), 256, 0, s>>>(epay.get(), slotOfEntry.get(), m, tstart.get(), tfill.get(), entries.get());
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
     }
     const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
     const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, (uint64_t)distinct * bitsPerKey));
     DevBuf<uint32_t> filter(filterBits / 32, s);
     TDAG_CUDA(cudaMemsetAsync(filter.get(), 0, filterBits / 8, s));
     tableRangesKernel<<<gridFor(cap, 256), 256, 0, s>>>(tkeys.get(), tstart.get(), tcount.get(), cap, tranges.get(), filter.get(), filterBits - 1);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     ekeys.release();
     epay.release();
     slotOfEntry.release();
@@ -550,7 +550,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx.numSMs * perSM, groups));
     TDAG_CUDA(cudaEventRecord(ctx.ev[0], s));
     searchKernel<R, L><<<blocks, kThreads, smem, s>>>(sp);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     TDAG_CUDA(cudaEventRecord(ctx.ev[1], s));
 
     // resolve
@@ -558,13 +558,13 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint32_t> isUnique(n, s), newIdx(n, s);
     TDAG_CUDA(cudaMemsetAsync(isUnique.get(), 0, (size_t)n * 4, s));
     decodeParentsKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, order.get(), sentinelKey, L, parentTP.get(), isUnique.get());
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     out.uniques = DevBuf<uint32_t>(n, s);
     out.numUnique = compactFlags(isUnique.get(), out.uniques.get(), n, s);
     exclusiveScanU32(isUnique.get(), newIdx.get(), n, s);
     out.mapping = DevBuf<uint64_t>(n, s);
     finalMappingKernel<<<gridFor(n, 256), 256, 0, s>>>(parentTP.get(), isUnique.get(), newIdx.get(), n, out.mapping.get());
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
 
     if (stats) {
         unsigned long long c[8];

@@ -98,15 +98,15 @@ void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t 
     const size_t blocks = (n + kScanTile - 1) / kScanTile;
     if (blocks == 1) {
         scanDownKernel<<<1, kScanThreads, 0, s>>>(in, out, nullptr, n);
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
         return;
     }
     DevBuf<uint32_t> sums(blocks, s), offs(blocks, s);
     scanReduceKernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(in, sums.get(), n);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     exclusiveScanU32(sums.get(), offs.get(), blocks, s);
     scanDownKernel<<<(unsigned)blocks, kScanThreads, 0, s>>>(in, out, offs.get(), n);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
 }
 
 uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s)
@@ -137,7 +137,7 @@ uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream
     DevBuf<uint32_t> offs(n, s);
     const uint64_t total = exclusiveScanU32Total(flags, offs.get(), n, s);
     scatterFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(flags, offs.get(), out, n);
-    TDAG_CUDA(cudaGetLastError());
+    TDAG_LAUNCHED();
     return (uint32_t)total;
 }
 
@@ -243,10 +243,10 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
     uint32_t passes = 0;
     for (uint32_t shift = beginBit; shift < endBit; shift += 8, ++passes) {
         radixHistKernel<<<numTiles, kSortThreads, 0, s>>>(kin, n, shift, counts.get(), numTiles);
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
         exclusiveScanU32(counts.get(), offs.get(), (size_t)256 * numTiles, s);
         radixScatterKernel<<<numTiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
-        TDAG_CUDA(cudaGetLastError());
+        TDAG_LAUNCHED();
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

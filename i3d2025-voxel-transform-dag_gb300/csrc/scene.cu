@@ -1,0 +1,693 @@
+// scene.cu — device-side input pipeline: procedural scenes, SVO construction, toDAG.
+//
+//  * Scenes (no reference counterpart; the reference voxelises meshes, which are not available here):
+//    an integer-only fBm value-noise terrain (solid where fbm - z/res > 0) and a seeded union of boxes,
+//    spheres and terrain blocks, 30% of them transformed copies of earlier ones, reduced to its
+//    1-voxel surface shell. Evaluated per 32^3 brick with a 1-voxel halo; rows of 34 voxels are
+//    built analytically for boxes and spheres and per voxel for terrain blocks.
+//  * SVO build: restates EditStructure(VoxelGrid) (tools/lib/include/voxcom/voxel/structure.h:423-429,
+//    658-701). Its depth-first recursion over Morton child order emits, per level, the non-empty cells
+//    in increasing Morton order, so the device build sorts nothing: non-empty leaves are compacted
+//    from a Morton-indexed array, and each level is the run-length compaction of the level below.
+//  * toDAG: restates EditStructure::toDAG (structure.h:703-763): per level, bottom-up, every item maps
+//    to the first occurrence of its content; first occurrences keep their order.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "class_table.cuh"
+#include "common.cuh"
+#include "internal.cuh"
+
+namespace tdag {
+
+struct SvdagOwned {
+    uint32_t resolution = 0, rootLevel = 0, structureType = 0;
+    std::vector<DevBuf<uint32_t>> nodes;
+    DevBuf<uint64_t> leaves;
+    uint64_t voxelCount = 0;
+};
+
+namespace {
+
+// ------------------------------------------------------------------------------------------------
+// fBm value noise, integer only (identical to the CPU statement used by the tests).
+// ------------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h)
+{
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h;
+}
+__host__ __device__ __forceinline__ uint32_t latticeValue(int64_t ix, int64_t iy, int64_t iz, uint32_t octave, uint32_t seed)
+{
+    uint32_t h = seed * 0x9E3779B1u + octave * 0x85EBCA77u;
+    h = mix32(h ^ ((uint32_t)ix * 0x27D4EB2Fu));
+    h = mix32(h ^ ((uint32_t)iy * 0x165667B1u));
+    h = mix32(h ^ ((uint32_t)iz * 0xD3A2646Du));
+    return h >> 16;
+}
+__host__ __device__ __forceinline__ int64_t smoothWeight(int64_t a, int64_t cell)
+{
+    const int64_t num = 2 * a + 1, den = 2 * cell;
+    return (num * num * (3 * den - 2 * num) * 65536) / (den * den * den);
+}
+__host__ __device__ __forceinline__ int64_t lerpQ16(int64_t a, int64_t b, int64_t w) { return (a * (65536 - w) + b * w) >> 16; }
+
+__host__ __device__ inline int64_t fbmValue(int64_t x, int64_t y, int64_t z, uint32_t seed)
+{
+    int64_t total = 0;
+    for (uint32_t o = 0; o < 5; ++o) {
+        const int64_t cell = 64 >> o;
+        const int64_t ix = x / cell, iy = y / cell, iz = z / cell;
+        const int64_t wx = smoothWeight(x % cell, cell), wy = smoothWeight(y % cell, cell), wz = smoothWeight(z % cell, cell);
+        const int64_t x00 = lerpQ16(latticeValue(ix, iy, iz, o, seed), latticeValue(ix + 1, iy, iz, o, seed), wx);
+        const int64_t x10 = lerpQ16(latticeValue(ix, iy + 1, iz, o, seed), latticeValue(ix + 1, iy + 1, iz, o, seed), wx);
+        const int64_t x01 = lerpQ16(latticeValue(ix, iy, iz + 1, o, seed), latticeValue(ix + 1, iy, iz + 1, o, seed), wx);
+        const int64_t x11 = lerpQ16(latticeValue(ix, iy + 1, iz + 1, o, seed), latticeValue(ix + 1, iy + 1, iz + 1, o, seed), wx);
+        total += lerpQ16(lerpQ16(x00, x10, wy), lerpQ16(x01, x11, wy), wz) * (16 >> o);
+    }
+    return total;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Primitive evaluation
+// ------------------------------------------------------------------------------------------------
+struct DevPrim {
+    int32_t type, perm, mirror, radius;
+    int32_t size[3]; // local extent
+    int32_t ext[3]; // world extent along each world axis = size[perm[k]]
+    int32_t lo[3]; // world offset (minimum corner)
+    uint32_t seed, pbits, pad;
+};
+
+__device__ __forceinline__ bool terrainInside(const DevPrim& p, int vx, int vy, int vz)
+{
+    int w[3] = { vx - p.lo[0], vy - p.lo[1], vz - p.lo[2] };
+    int u[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if ((p.mirror >> k) & 1)
+            w[k] = p.ext[k] - 1 - w[k];
+        u[(p.pbits >> (2 * k)) & 3] = w[k];
+    }
+    return fbmValue(u[0], u[1], u[2], p.seed) * p.size[0] > (int64_t)u[2] * 31 * 65535;
+}
+
+// integer square root: largest r with r*r <= v (v >= 0)
+__device__ __forceinline__ int isqrt64(int64_t v)
+{
+    int r = (int)sqrt((double)v);
+    while ((int64_t)r * r > v)
+        --r;
+    while ((int64_t)(r + 1) * (r + 1) <= v)
+        ++r;
+    return r;
+}
+
+constexpr int kBrick = 32;
+constexpr int kHalo = kBrick + 2;
+constexpr int kMaxList = 1024;
+
+// CTA per 32^3 brick. Writes the brick's 8^3 leaf masks into the Morton-indexed leaf array.
+__global__ void __launch_bounds__(256) sceneBrickKernel(const DevPrim* __restrict__ prims, uint32_t numPrims, uint32_t kind, uint32_t res, uint32_t seed,
+    uint32_t shell, uint32_t bricksPerAxis, uint64_t* __restrict__ leafArray, uint32_t* status)
+{
+    __shared__ uint64_t rows[kHalo * kHalo]; // bit hx (0..33) of row (hy, hz) = voxel (bx0 - 1 + hx, ...)
+    __shared__ uint32_t list[kMaxList];
+    __shared__ uint32_t listCount;
+    const uint32_t b = blockIdx.x;
+    const int bx = (int)(b % bricksPerAxis), by = (int)((b / bricksPerAxis) % bricksPerAxis), bz = (int)(b / (bricksPerAxis * bricksPerAxis));
+    const int x0 = bx * kBrick - 1, y0 = by * kBrick - 1, z0 = bz * kBrick - 1; // halo origin
+    if (threadIdx.x == 0)
+        listCount = 0;
+    __syncthreads();
+    if (kind == TDAG_SCENE_PRIMITIVES) {
+        for (uint32_t i = threadIdx.x; i < numPrims; i += blockDim.x) {
+            const DevPrim& p = prims[i];
+            bool hit = true;
+            const int lo[3] = { x0, y0, z0 };
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                hit &= (p.lo[k] < lo[k] + kHalo) && (p.lo[k] + p.ext[k] > lo[k]);
+            if (hit) {
+                const uint32_t slot = atomicAdd(&listCount, 1u);
+                if (slot < kMaxList)
+                    list[slot] = i;
+            }
+        }
+        __syncthreads();
+        if (listCount > kMaxList) {
+            if (threadIdx.x == 0)
+                setDeviceError(status, TDAG_ERR_ALLOC, 400);
+            return;
+        }
+    }
+    const uint32_t nList = listCount;
+    // ---- inside rows with halo
+    for (int r = threadIdx.x; r < kHalo * kHalo; r += blockDim.x) {
+        const int hy = r % kHalo, hz = r / kHalo;
+        const int y = y0 + hy, z = z0 + hz;
+        uint64_t bits = 0;
+        if (y >= 0 && z >= 0 && y < (int)res && z < (int)res) {
+            if (kind == TDAG_SCENE_TERRAIN) {
+                for (int hx = 0; hx < kHalo; ++hx) {
+                    const int x = x0 + hx;
+                    if (x < 0 || x >= (int)res)
+                        continue;
+                    if (fbmValue(x, y, z, seed) * (int64_t)res > (int64_t)z * 31 * 65535)
+                        bits |= 1ull << hx;
+                }
+            } else {
+                for (uint32_t li = 0; li < nList; ++li) {
+                    const DevPrim& p = prims[list[li]];
+                    if (y < p.lo[1] || y >= p.lo[1] + p.ext[1] || z < p.lo[2] || z >= p.lo[2] + p.ext[2])
+                        continue;
+                    int xa = p.lo[0], xb = p.lo[0] + p.ext[0]; // [xa, xb)
+                    if (p.type == 0) {
+                        // box: the whole x range
+                    } else if (p.type == 1) {
+                        const int64_t dy = y - (p.lo[1] + p.radius), dz = z - (p.lo[2] + p.radius);
+                        const int64_t rem = (int64_t)p.radius * p.radius - dy * dy - dz * dz;
+                        if (rem < 0)
+                            continue;
+                        const int dx = isqrt64(rem);
+                        xa = p.lo[0] + p.radius - dx;
+                        xb = p.lo[0] + p.radius + dx + 1;
+                    } else {
+                        const int ha = max(xa, x0), hb = min(xb, x0 + kHalo);
+                        for (int x = ha; x < hb; ++x)
+                            if (x >= 0 && x < (int)res && !((bits >> (x - x0)) & 1) && terrainInside(p, x, y, z))
+                                bits |= 1ull << (x - x0);
+                        continue;
+                    }
+                    const int ha = max(max(xa, x0), 0), hb = min(min(xb, x0 + kHalo), (int)res);
+                    if (ha < hb) {
+                        const int s = ha - x0, e = hb - x0;
+                        bits |= ((e >= 64 ? ~0ull : ((1ull << e) - 1)) & ~((1ull << s) - 1));
+                    }
+                }
+            }
+        }
+        rows[r] = bits;
+    }
+    __syncthreads();
+    // ---- shell and leaf emission: thread per leaf (8^3 = 512 leaves, 2 per thread)
+    for (int l = threadIdx.x; l < 512; l += blockDim.x) {
+        const int lx = l & 7, ly = (l >> 3) & 7, lz = l >> 6;
+        uint64_t mask = 0;
+        for (int vz = 0; vz < 4; ++vz)
+            for (int vy = 0; vy < 4; ++vy) {
+                const int hy = ly * 4 + vy + 1, hz = lz * 4 + vz + 1;
+                const uint64_t c = rows[hy + kHalo * hz];
+                uint64_t v = c;
+                if (shell) {
+                    const uint64_t all = c & (c << 1) & (c >> 1) & rows[hy - 1 + kHalo * hz] & rows[hy + 1 + kHalo * hz] & rows[hy + kHalo * (hz - 1)] & rows[hy + kHalo * (hz + 1)];
+                    v = c & ~all;
+                }
+                const uint32_t four = (uint32_t)(v >> (lx * 4 + 1)) & 0xF;
+                for (int vx = 0; vx < 4; ++vx)
+                    if ((four >> vx) & 1)
+                        mask |= 1ull << morton3(vx, vy, vz);
+            }
+        const uint32_t gx = bx * 8 + lx, gy = by * 8 + ly, gz = bz * 8 + lz;
+        const uint64_t code = (uint64_t)part1by2(gx) | ((uint64_t)part1by2(gy) << 1) | ((uint64_t)part1by2(gz) << 2);
+        leafArray[code] = mask;
+    }
+}
+
+// Dense host grid (uploaded) -> Morton-indexed leaf array.
+__global__ void denseLeafKernel(const uint8_t* __restrict__ dense, uint32_t res, uint64_t* __restrict__ leafArray, uint64_t numLeaves)
+{
+    const uint64_t code = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (code >= numLeaves)
+        return;
+    const uint32_t lx = compact1by2((uint32_t)code), ly = compact1by2((uint32_t)(code >> 1)), lz = compact1by2((uint32_t)(code >> 2));
+    uint64_t mask = 0;
+    for (uint32_t i = 0; i < 64; ++i) {
+        const uint32_t x = lx * 4 + compact1by2(i), y = ly * 4 + compact1by2(i >> 1), z = lz * 4 + compact1by2(i >> 2);
+        if (dense[(size_t)x + (size_t)res * y + (size_t)res * res * z])
+            mask |= 1ull << i;
+    }
+    leafArray[code] = mask;
+}
+
+__global__ void nonZeroFlagKernel(const uint64_t* __restrict__ a, uint64_t n, uint32_t* __restrict__ flags, unsigned long long* __restrict__ voxels)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t pc = 0;
+    if (i < n) {
+        const uint64_t v = a[i];
+        flags[i] = v != 0;
+        pc = __popcll(v);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        pc += __shfl_down_sync(0xffffffffu, pc, o);
+    if ((threadIdx.x & 31) == 0 && pc)
+        atomicAdd(voxels, (unsigned long long)pc);
+}
+
+__global__ void gatherLeavesKernel(const uint32_t* __restrict__ codes, uint32_t n, const uint64_t* __restrict__ leafArray, uint64_t* __restrict__ masks,
+    uint64_t* __restrict__ codes64)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    masks[i] = leafArray[codes[i]];
+    codes64[i] = codes[i];
+}
+
+// Level build: parent code = child code >> 3; run heads start new parents.
+__global__ void runHeadKernel(const uint64_t* __restrict__ codes, uint32_t n, uint32_t* __restrict__ flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        flags[i] = (i == 0) || ((codes[i] >> 3) != (codes[i - 1] >> 3));
+}
+
+__global__ void linkParentsKernel(const uint64_t* __restrict__ codes, uint32_t n, const uint32_t* __restrict__ flags, const uint32_t* __restrict__ offs,
+    uint32_t* __restrict__ nodes, uint64_t* __restrict__ parentCodes)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t parent = offs[i] + flags[i] - 1;
+    nodes[(size_t)parent * 8 + (codes[i] & 7)] = i;
+    if (flags[i])
+        parentCodes[parent] = codes[i] >> 3;
+}
+
+// toDAG helpers
+__global__ void remapChildrenKernel(const uint32_t* __restrict__ in, uint64_t count8, const uint32_t* __restrict__ mapping, uint64_t* __restrict__ keys)
+{
+    // keys: 4 u64 words per node = the remapped children pairs
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count8 / 2)
+        return;
+    const uint32_t a = in[2 * i], b = in[2 * i + 1];
+    const uint32_t ma = (a == kEmpty32) ? kEmpty32 : mapping[a];
+    const uint32_t mb = (b == kEmpty32) ? kEmpty32 : mapping[b];
+    keys[i] = (uint64_t)ma | ((uint64_t)mb << 32);
+}
+
+__global__ void firstFlagsKernel(const uint32_t* __restrict__ slotOf, const uint32_t* __restrict__ minIdx, uint32_t n, uint32_t* __restrict__ flags,
+    uint32_t* __restrict__ canon)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t c = minIdx[slotOf[i]];
+    canon[i] = c;
+    flags[i] = (c == i);
+}
+
+__global__ void dedupMapKernel(const uint32_t* __restrict__ canon, const uint32_t* __restrict__ handleOf, uint32_t n, uint32_t* __restrict__ mapping)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        mapping[i] = handleOf[canon[i]];
+}
+
+__global__ void gatherU64Kernel(const uint64_t* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n, uint32_t words, uint64_t* __restrict__ dst)
+{
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint64_t)n * words)
+        return;
+    const uint32_t i = (uint32_t)(g / words), w = (uint32_t)(g % words);
+    dst[g] = src[(size_t)idx[i] * words + w];
+}
+
+uint64_t pow2AtLeast(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v)
+        p <<= 1;
+    return p;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host-side primitive list (deterministic, splitmix64-driven)
+// ------------------------------------------------------------------------------------------------
+struct Rng {
+    uint64_t s;
+    uint64_t next()
+    {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    uint32_t below(uint32_t n) { return n ? (uint32_t)(next() % n) : 0; }
+    int32_t range(int32_t lo, int32_t hi) { return lo + (int32_t)below((uint32_t)(hi - lo + 1)); } // inclusive
+};
+
+void placePrimitive(tdag_primitive& p, uint32_t res, Rng& rng)
+{
+    const uint32_t pbits = permBitsOf(p.xform & 7);
+    for (int k = 0; k < 3; ++k) {
+        const int32_t ext = p.size[(pbits >> (2 * k)) & 3];
+        p.offset[k] = ext >= (int32_t)res ? 0 : (int32_t)rng.below((uint32_t)(res - ext + 1));
+    }
+}
+
+std::vector<tdag_primitive> scenePrimitives(const tdag_scene& sc)
+{
+    std::vector<tdag_primitive> out;
+    if (sc.kind != TDAG_SCENE_PRIMITIVES)
+        return out;
+    Rng rng { 0x5EEDull * 1000003ull + sc.seed };
+    const int32_t res = (int32_t)sc.resolution;
+    auto scaled = [&](int32_t num) { return std::max<int32_t>(1, (int32_t)((int64_t)res * num / 2048)); };
+    out.reserve(sc.num_primitives);
+    for (uint32_t i = 0; i < sc.num_primitives; ++i) {
+        tdag_primitive p {};
+        if (i > 0 && rng.below(100) < sc.copy_percent) {
+            const uint32_t j = rng.below(i);
+            p = out[j];
+            p.source = j;
+            const uint32_t mode = rng.below(3);
+            uint32_t perm = p.xform & 7, mirror = p.xform >> 3;
+            if (mode == 0)
+                mirror = mirror ^ (1 + rng.below(7)); // a different mirror
+            else if (mode == 1)
+                perm = (perm + 1 + rng.below(5)) % 6; // a different axis order
+            p.xform = perm | (mirror << 3);
+            placePrimitive(p, sc.resolution, rng); // mode 2: translation only
+        } else {
+            const uint32_t r = rng.below(100);
+            p.source = i;
+            p.seed = (uint32_t)rng.next();
+            if (r < 45) {
+                p.type = 0;
+                for (int k = 0; k < 3; ++k)
+                    p.size[k] = rng.range(scaled(8), scaled(256));
+            } else if (r < 90) {
+                p.type = 1;
+                p.radius = rng.range(scaled(4), scaled(128));
+                p.size[0] = p.size[1] = p.size[2] = 2 * p.radius + 1;
+            } else {
+                p.type = 2;
+                const int32_t s = rng.range(scaled(64), scaled(512));
+                p.size[0] = p.size[1] = p.size[2] = s;
+            }
+            p.xform = 0;
+            placePrimitive(p, sc.resolution, rng);
+        }
+        out.push_back(p);
+    }
+    return out;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Pipeline pieces
+// ------------------------------------------------------------------------------------------------
+// Morton-indexed leaf array -> SVO tree (levels 2..root) in the reference's order.
+void buildTree(Context& ctx, DevBuf<uint64_t>& leafArray, uint64_t numLeafCells, uint32_t res, SvdagOwned& out)
+{
+    cudaStream_t s = ctx.stream;
+    const uint32_t rootLevel = (uint32_t)(31 - __builtin_clz(res));
+    out.resolution = res;
+    out.rootLevel = rootLevel;
+    out.structureType = 0;
+    out.nodes.clear();
+    out.nodes.resize(rootLevel + 1);
+    TDAG_CHECK(numLeafCells < (1ull << 32), TDAG_ERR_ARG, "resolution too large for a single leaf array");
+    DevBuf<uint32_t> flags(numLeafCells, s);
+    DevBuf<unsigned long long> vox(1, s);
+    TDAG_CUDA(cudaMemsetAsync(vox.get(), 0, 8, s));
+    nonZeroFlagKernel<<<gridFor(numLeafCells, 256), 256, 0, s>>>(leafArray.get(), numLeafCells, flags.get(), vox.get());
+    TDAG_LAUNCHED();
+    DevBuf<uint32_t> codes32(numLeafCells, s);
+    const uint32_t n = compactFlags(flags.get(), codes32.get(), numLeafCells, s);
+    flags.release();
+    unsigned long long voxels = 0;
+    TDAG_CUDA(cudaMemcpyAsync(&voxels, vox.get(), 8, cudaMemcpyDeviceToHost, s));
+    out.leaves = DevBuf<uint64_t>(n, s);
+    DevBuf<uint64_t> codes(n, s);
+    if (n) {
+        gatherLeavesKernel<<<gridFor(n, 256), 256, 0, s>>>(codes32.get(), n, leafArray.get(), out.leaves.get(), codes.get());
+        TDAG_LAUNCHED();
+    }
+    codes32.release();
+    leafArray.release();
+    uint32_t cur = n;
+    for (uint32_t level = 3; level <= rootLevel && cur; ++level) {
+        DevBuf<uint32_t> heads(cur, s), offs(cur, s);
+        runHeadKernel<<<gridFor(cur, 256), 256, 0, s>>>(codes.get(), cur, heads.get());
+        TDAG_LAUNCHED();
+        const uint32_t np = (uint32_t)exclusiveScanU32Total(heads.get(), offs.get(), cur, s);
+        out.nodes[level] = DevBuf<uint32_t>((size_t)np * 8, s);
+        fillU32(out.nodes[level].get(), kEmpty32, (size_t)np * 8, s);
+        DevBuf<uint64_t> pcodes(np, s);
+        linkParentsKernel<<<gridFor(cur, 256), 256, 0, s>>>(codes.get(), cur, heads.get(), offs.get(), out.nodes[level].get(), pcodes.get());
+        TDAG_LAUNCHED();
+        codes = std::move(pcodes);
+        cur = np;
+    }
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    out.voxelCount = voxels;
+}
+
+// First-occurrence dedup of n items with W-word keys; returns the number of unique items, the
+// mapping (item -> handle) and the list of first occurrences.
+uint32_t dedupLevel(Context& ctx, const uint64_t* keys, int words, uint32_t n, DevBuf<uint32_t>& mapping, DevBuf<uint32_t>& firsts)
+{
+    cudaStream_t s = ctx.stream;
+    const uint64_t cap = pow2AtLeast((uint64_t)n * 2 + 16);
+    DevBuf<uint64_t> slots(cap, s);
+    DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
+    fillU64(slots.get(), kEmptySlot, cap, s);
+    fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
+    if (words == 1)
+        classInsertKernel<1><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    else
+        classInsertKernel<4><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    TDAG_LAUNCHED();
+    slots.release();
+    DevBuf<uint32_t> flags(n, s), canon(n, s);
+    firstFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(slotOf.get(), minIdx.get(), n, flags.get(), canon.get());
+    TDAG_LAUNCHED();
+    slotOf.release();
+    minIdx.release();
+    ctx.checkStatus("toDAG");
+    firsts = DevBuf<uint32_t>(n, s);
+    DevBuf<uint32_t> handleOf(n, s);
+    const uint32_t u = compactFlags(flags.get(), firsts.get(), n, s);
+    exclusiveScanU32(flags.get(), handleOf.get(), n, s);
+    mapping = DevBuf<uint32_t>(n, s);
+    dedupMapKernel<<<gridFor(n, 256), 256, 0, s>>>(canon.get(), handleOf.get(), n, mapping.get());
+    TDAG_LAUNCHED();
+    return u;
+}
+
+void toDagDevice(Context& ctx, SvdagOwned& g)
+{
+    cudaStream_t s = ctx.stream;
+    DevBuf<uint32_t> mapping, firsts;
+    const uint32_t nl = (uint32_t)g.leaves.n;
+    if (nl) {
+        const uint32_t u = dedupLevel(ctx, g.leaves.get(), 1, nl, mapping, firsts);
+        DevBuf<uint64_t> uniq(u, s);
+        gatherU64Kernel<<<gridFor(u, 256), 256, 0, s>>>(g.leaves.get(), firsts.get(), u, 1, uniq.get());
+        TDAG_LAUNCHED();
+        g.leaves = std::move(uniq);
+    }
+    for (uint32_t level = 3; level <= g.rootLevel; ++level) {
+        const uint32_t n = (uint32_t)(g.nodes[level].n / 8);
+        if (!n)
+            continue;
+        DevBuf<uint64_t> keys((size_t)n * 4, s);
+        remapChildrenKernel<<<gridFor((size_t)n * 4, 256), 256, 0, s>>>(g.nodes[level].get(), (uint64_t)n * 8, mapping.get(), keys.get());
+        TDAG_LAUNCHED();
+        DevBuf<uint32_t> m2, f2;
+        const uint32_t u = dedupLevel(ctx, keys.get(), 4, n, m2, f2);
+        DevBuf<uint32_t> uniq((size_t)u * 8, s);
+        gatherU64Kernel<<<gridFor((size_t)u * 4, 256), 256, 0, s>>>(keys.get(), f2.get(), u, 4, reinterpret_cast<uint64_t*>(uniq.get()));
+        TDAG_LAUNCHED();
+        g.nodes[level] = std::move(uniq);
+        mapping = std::move(m2);
+    }
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    g.structureType = 1;
+}
+
+DevPrim toDevPrim(const tdag_primitive& p)
+{
+    DevPrim d {};
+    d.type = (int32_t)p.type;
+    d.perm = (int32_t)(p.xform & 7);
+    d.mirror = (int32_t)(p.xform >> 3);
+    d.radius = p.radius;
+    d.pbits = permBitsOf(p.xform & 7);
+    for (int k = 0; k < 3; ++k) {
+        d.size[k] = p.size[k];
+        d.ext[k] = p.size[(d.pbits >> (2 * k)) & 3];
+        d.lo[k] = p.offset[k];
+    }
+    d.seed = p.seed;
+    return d;
+}
+
+} // namespace
+
+std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool toDag)
+{
+    TDAG_CHECK(sc.kind == TDAG_SCENE_TERRAIN || sc.kind == TDAG_SCENE_PRIMITIVES, TDAG_ERR_ARG, "unknown scene kind");
+    TDAG_CHECK(sc.resolution >= 32 && sc.resolution <= 16384 && (sc.resolution & (sc.resolution - 1)) == 0, TDAG_ERR_ARG,
+        "scene resolution must be a power of two in [32, 16384]");
+    cudaStream_t s = ctx.stream;
+    const uint32_t res = sc.resolution;
+    const uint64_t cells = (uint64_t)(res / 4) * (res / 4) * (res / 4);
+    TDAG_CHECK(cells < (1ull << 32), TDAG_ERR_ARG, "scene too large for the single-pass generator");
+    auto prims = scenePrimitives(sc);
+    std::vector<DevPrim> dp(prims.size());
+    for (size_t i = 0; i < prims.size(); ++i)
+        dp[i] = toDevPrim(prims[i]);
+    DevBuf<DevPrim> dprims(std::max<size_t>(1, dp.size()), s);
+    if (!dp.empty())
+        TDAG_CUDA(cudaMemcpyAsync(dprims.get(), dp.data(), dp.size() * sizeof(DevPrim), cudaMemcpyHostToDevice, s));
+    DevBuf<uint64_t> leafArray(cells, s);
+    const uint32_t bpa = res / kBrick;
+    const uint64_t bricks = (uint64_t)bpa * bpa * bpa;
+    sceneBrickKernel<<<(unsigned)bricks, 256, 0, s>>>(dprims.get(), (uint32_t)dp.size(), sc.kind, res, sc.seed, sc.shell, bpa, leafArray.get(), ctx.status);
+    TDAG_LAUNCHED();
+    ctx.checkStatus("scene generation");
+    auto out = std::make_unique<SvdagOwned>();
+    buildTree(ctx, leafArray, cells, res, *out);
+    if (toDag)
+        toDagDevice(ctx, *out);
+    return out;
+}
+
+std::unique_ptr<SvdagOwned> denseSvdag(Context& ctx, const uint8_t* dense, uint32_t res, bool toDag)
+{
+    TDAG_CHECK(res >= 4 && (res & (res - 1)) == 0 && res <= 2048, TDAG_ERR_ARG, "dense resolution must be a power of two in [4, 2048]");
+    cudaStream_t s = ctx.stream;
+    const uint64_t nvox = (uint64_t)res * res * res;
+    DevBuf<uint8_t> d(nvox, s);
+    TDAG_CUDA(cudaMemcpyAsync(d.get(), dense, nvox, cudaMemcpyHostToDevice, s));
+    const uint64_t cells = nvox / 64;
+    DevBuf<uint64_t> leafArray(cells, s);
+    denseLeafKernel<<<gridFor(cells, 256), 256, 0, s>>>(d.get(), res, leafArray.get(), cells);
+    TDAG_LAUNCHED();
+    d.release();
+    auto out = std::make_unique<SvdagOwned>();
+    buildTree(ctx, leafArray, cells, res, *out);
+    if (toDag)
+        toDagDevice(ctx, *out);
+    return out;
+}
+
+std::vector<tdag_primitive> hostScenePrimitives(const tdag_scene& sc) { return scenePrimitives(sc); }
+
+} // namespace tdag
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+using namespace tdag;
+
+struct tdag_svdag {
+    std::unique_ptr<SvdagOwned> g;
+};
+
+Context& ctxOf(tdag_ctx* c); // build.cu
+int guardedCall(const std::function<void()>& f); // build.cu
+int failWith(int code, const char* msg); // build.cu
+
+extern "C" {
+
+int tdag_scene_primitives(const tdag_scene* scene, tdag_primitive* out, uint32_t capacity, uint32_t* count)
+{
+    if (!scene || !count)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        auto p = hostScenePrimitives(*scene);
+        *count = (uint32_t)p.size();
+        if (out)
+            std::memcpy(out, p.data(), std::min<size_t>(capacity, p.size()) * sizeof(tdag_primitive));
+    });
+}
+
+int tdag_scene_svdag(tdag_ctx* ctx, const tdag_scene* scene, int toDag, tdag_svdag** out)
+{
+    if (!ctx || !scene || !out)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guardedCall([&] {
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        auto h = std::make_unique<tdag_svdag>();
+        h->g = sceneSvdag(c, *scene, toDag != 0);
+        *out = h.release();
+    });
+}
+
+int tdag_svdag_from_dense(tdag_ctx* ctx, const uint8_t* dense, uint32_t res, int toDag, tdag_svdag** out)
+{
+    if (!ctx || !dense || !out)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guardedCall([&] {
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        auto h = std::make_unique<tdag_svdag>();
+        h->g = denseSvdag(c, dense, res, toDag != 0);
+        *out = h.release();
+    });
+}
+
+int tdag_svdag_get_view(const tdag_svdag* sv, tdag_svdag_view* v)
+{
+    if (!sv || !v)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    std::memset(v, 0, sizeof(*v));
+    const SvdagOwned& g = *sv->g;
+    v->resolution = g.resolution;
+    v->root_level = g.rootLevel;
+    v->structure_type = g.structureType;
+    for (uint32_t l = 3; l <= g.rootLevel; ++l) {
+        v->nodes[l] = g.nodes[l].get();
+        v->node_counts[l] = g.nodes[l].n / 8;
+    }
+    v->leaves = g.leaves.get();
+    v->leaf_count = g.leaves.n;
+    return TDAG_OK;
+}
+
+int tdag_svdag_voxel_count(const tdag_svdag* sv, uint64_t* out)
+{
+    if (!sv || !out)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    *out = sv->g->voxelCount;
+    return TDAG_OK;
+}
+
+int tdag_svdag_copy_level(tdag_ctx* ctx, const tdag_svdag* sv, uint32_t level, void* dst, uint64_t bytes)
+{
+    if (!ctx || !sv || (!dst && bytes))
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        const SvdagOwned& g = *sv->g;
+        Context& c = ctxOf(ctx);
+        TDAG_CHECK(level >= 2 && level <= g.rootLevel, TDAG_ERR_ARG, "level out of range");
+        const void* src = level == 2 ? (const void*)g.leaves.get() : (const void*)g.nodes[level].get();
+        const uint64_t need = level == 2 ? g.leaves.n * 8 : g.nodes[level].n * 4;
+        TDAG_CHECK(bytes >= need, TDAG_ERR_ARG, "destination buffer too small");
+        if (need)
+            TDAG_CUDA(cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToHost, c.stream));
+        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int tdag_svdag_free(tdag_svdag* sv)
+{
+    delete sv;
+    return TDAG_OK;
+}
+
+} // extern "C"

@@ -328,3 +328,138 @@ def find_duplicates_among_flattened_items(level: int, grids: np.ndarray, config:
                                                 ctypes.byref(st)))
     res = (uniq[: nu.value].copy(), mapping)
     return (res + (_abi.level_stats_to_dict(st),)) if return_stats else res
+
+
+# ------------------------------------------------------------------------------------------------
+# Device-side input pipeline: scenes, SVO build, toDAG (device-resident EditStructure<void, uint32_t>)
+# ------------------------------------------------------------------------------------------------
+SCENE_TERRAIN = 0
+SCENE_PRIMITIVES = 1
+
+
+@dataclasses.dataclass
+class SceneSpec:
+    """tdag_scene: a procedural grid generated on the device."""
+
+    kind: int = SCENE_PRIMITIVES
+    resolution: int = 2048
+    seed: int = 1
+    num_primitives: int = 4000
+    copy_percent: int = 30
+    shell: bool = True
+
+    def to_c(self) -> _abi.Scene:
+        c = _abi.Scene()
+        c.kind, c.resolution, c.seed = self.kind, self.resolution, self.seed
+        c.num_primitives, c.copy_percent, c.shell = self.num_primitives, self.copy_percent, int(self.shell)
+        return c
+
+
+def scene_primitives(spec: SceneSpec) -> list:
+    """The deterministic primitive list of a scene (tdag_scene_primitives)."""
+    c = spec.to_c()
+    n = ctypes.c_uint32()
+    _abi.check(lib().tdag_scene_primitives(ctypes.byref(c), None, 0, ctypes.byref(n)))
+    arr = (_abi.Primitive * max(1, n.value))()
+    _abi.check(lib().tdag_scene_primitives(ctypes.byref(c), arr, n.value, ctypes.byref(n)))
+    out = []
+    for i in range(n.value):
+        p = arr[i]
+        out.append({"type": p.type, "xform": p.xform, "size": tuple(p.size), "radius": p.radius,
+                    "offset": tuple(p.offset), "seed": p.seed, "source": p.source})
+    return out
+
+
+class DeviceSvdag:
+    """A library-owned device-resident EditStructure<void, uint32_t> (tdag_svdag)."""
+
+    def __init__(self, handle: ctypes.c_void_p, ctx: Context):
+        self._h = handle
+        self._ctx = ctx
+
+    @property
+    def handle(self):
+        return self._h
+
+    def view(self) -> _abi.SvdagView:
+        v = _abi.SvdagView()
+        _abi.check(lib().tdag_svdag_get_view(self._h, ctypes.byref(v)))
+        return v
+
+    @property
+    def voxel_count(self) -> int:
+        n = ctypes.c_uint64()
+        _abi.check(lib().tdag_svdag_voxel_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def to_host(self) -> EditStructure:
+        v = self.view()
+        levels = []
+        for lvl in range(v.root_level + 1):
+            cnt = v.node_counts[lvl] if lvl >= 3 else 0
+            a = np.zeros((cnt, 8), np.uint32)
+            if cnt:
+                _abi.check(lib().tdag_svdag_copy_level(self._ctx.handle, self._h, lvl, a.ctypes.data, a.nbytes))
+            levels.append(a)
+        leaves = np.zeros(v.leaf_count, np.uint64)
+        if v.leaf_count:
+            _abi.check(lib().tdag_svdag_copy_level(self._ctx.handle, self._h, 2, leaves.ctypes.data, leaves.nbytes))
+        return EditStructure(levels, leaves, v.resolution, v.root_level, v.structure_type, "u32")
+
+    def free(self):
+        if self._h:
+            lib().tdag_svdag_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def scene_svdag(spec: SceneSpec, to_dag: bool = True, ctx: Optional[Context] = None) -> DeviceSvdag:
+    ctx = ctx or default_context()
+    h = ctypes.c_void_p()
+    c = spec.to_c()
+    _abi.check(lib().tdag_scene_svdag(ctx.handle, ctypes.byref(c), int(to_dag), ctypes.byref(h)))
+    return DeviceSvdag(h, ctx)
+
+
+def svdag_from_dense(dense: np.ndarray, to_dag: bool = True, ctx: Optional[Context] = None) -> DeviceSvdag:
+    """EditStructure(VoxelGrid) (+ toDAG) on the device; dense[z, y, x] (x fastest)."""
+    ctx = ctx or default_context()
+    d = np.ascontiguousarray(dense, dtype=np.uint8)
+    h = ctypes.c_void_p()
+    _abi.check(lib().tdag_svdag_from_dense(ctx.handle, d.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), d.shape[0],
+                                           int(to_dag), ctypes.byref(h)))
+    return DeviceSvdag(h, ctx)
+
+
+class DeviceResult:
+    """A device-resident EditStructure<void, TransformPointer> (tdag_result with on_device = 1)."""
+
+    def __init__(self, rp):
+        self._rp = rp
+        self.stats = _abi.stats_to_dict(rp.contents.stats, rp.contents.root_level)
+
+    def free(self):
+        if self._rp:
+            lib().tdag_result_free(self._rp)
+            self._rp = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def construct_transform_dag_device(in_dag: DeviceSvdag, config: TransformDAGConfig = TransformDAGConfig(),
+                                   ctx: Optional[Context] = None) -> DeviceResult:
+    """constructTransformDAG with the input and the result resident in device memory (tdag_build_device)."""
+    ctx = ctx or default_context()
+    v = in_dag.view()
+    rp = ctypes.POINTER(_abi.Result)()
+    _abi.check(lib().tdag_build_device(ctx.handle, ctypes.byref(v), ctypes.byref(_config_struct(config)), ctypes.byref(rp)))
+    return DeviceResult(rp)

@@ -50,7 +50,7 @@ class LevelStats(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("hierarchical", LevelStats * MAX_LEVELS), ("translation", LevelStats * MAX_LEVELS),
                 ("total_ms", ctypes.c_float), ("hierarchical_ms", ctypes.c_float),
-                ("translation_ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+                ("translation_ms", ctypes.c_float), ("reserved", ctypes.c_float), ("kernel_launches", ctypes.c_uint64)]
 
 
 class Result(ctypes.Structure):
@@ -62,6 +62,18 @@ class Result(ctypes.Structure):
                 ("stats", Stats)]
 
 
+class Scene(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("resolution", ctypes.c_uint32), ("seed", ctypes.c_uint32),
+                ("num_primitives", ctypes.c_uint32), ("copy_percent", ctypes.c_uint32), ("shell", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 2)]
+
+
+class Primitive(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("xform", ctypes.c_uint32), ("size", ctypes.c_int32 * 3),
+                ("radius", ctypes.c_int32), ("offset", ctypes.c_int32 * 3), ("seed", ctypes.c_uint32),
+                ("source", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("filter_bits_per_key", ctypes.c_uint32), ("table_load_percent", ctypes.c_uint32),
                 ("search_ctas_per_sm", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
@@ -71,6 +83,8 @@ class Tuning(ctypes.Structure):
 EXPORTED = (
     "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
     "tdag_build", "tdag_build_device", "tdag_result_free", "tdag_find_duplicates_level", "tdag_build_hierarchical",
+    "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
+    "tdag_svdag_copy_level", "tdag_svdag_free",
 )
 
 _lib = None
@@ -102,6 +116,13 @@ def lib(path: str = None):
                                                  ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_uint64),
                                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                                  ctypes.POINTER(LevelStats)]
+        L.tdag_scene_primitives.argtypes = [ctypes.POINTER(Scene), ctypes.POINTER(Primitive), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+        L.tdag_scene_svdag.argtypes = [vp, ctypes.POINTER(Scene), ctypes.c_int, ctypes.POINTER(vp)]
+        L.tdag_svdag_from_dense.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(vp)]
+        L.tdag_svdag_get_view.argtypes = [vp, ctypes.POINTER(SvdagView)]
+        L.tdag_svdag_voxel_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+        L.tdag_svdag_copy_level.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64]
+        L.tdag_svdag_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -117,7 +138,7 @@ def level_stats_to_dict(s: LevelStats) -> dict:
 
 def stats_to_dict(s: Stats, root_level: int) -> dict:
     return {
-        "total_ms": s.total_ms, "hierarchical_ms": s.hierarchical_ms, "translation_ms": s.translation_ms,
+        "kernel_launches": s.kernel_launches, "total_ms": s.total_ms, "hierarchical_ms": s.hierarchical_ms, "translation_ms": s.translation_ms,
         "hierarchical": {l: level_stats_to_dict(s.hierarchical[l]) for l in range(2, root_level + 1)},
         "translation": {l: level_stats_to_dict(s.translation[l]) for l in range(2, 5)},
     }

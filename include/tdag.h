@@ -80,6 +80,7 @@ typedef struct tdag_stats {
     float hierarchical_ms;
     float translation_ms;
     float reserved;
+    uint64_t kernel_launches; /* kernels this library launched for the construction */
 } tdag_stats;
 
 /* EditStructure<void, TransformPointer> result. Arrays are owned by the library: host memory from
@@ -139,6 +140,55 @@ int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* gr
  * tools/lib/src/voxel/transform_dag_hierarchical.cpp:304-529): symmetry + permutation only.
  * Host in, host out. */
 int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in_host, const tdag_config* config, tdag_result** out);
+
+/* ------------------------------------------------------------------------------------------------
+ * Input side of the path: procedural scenes, SVO construction and toDAG on the device.
+ * (EditStructure(VoxelGrid), structure.h:423-429, 658-701; EditStructure::toDAG, structure.h:703-763.)
+ * These have no C-ABI counterpart in the reference (it builds SVOs on the host); they produce the
+ * same structures in device memory so the Transform-DAG build can start from HBM.
+ * ------------------------------------------------------------------------------------------------ */
+#define TDAG_SCENE_TERRAIN 0 /* solid fBm terrain: solid where fbm(v) - z/res > 0 */
+#define TDAG_SCENE_PRIMITIVES 1 /* union of boxes, spheres and terrain blocks with transformed copies */
+
+typedef struct tdag_scene {
+    uint32_t kind; /* TDAG_SCENE_* */
+    uint32_t resolution; /* power of two, 16 .. 16384 */
+    uint32_t seed;
+    uint32_t num_primitives; /* TDAG_SCENE_PRIMITIVES */
+    uint32_t copy_percent; /* percent of primitives placed as mirrored / permuted / translated copies */
+    uint32_t shell; /* 1: keep only the 1-voxel surface shell (6-neighbourhood) */
+    uint32_t reserved[2];
+} tdag_scene;
+
+/* One primitive of a TDAG_SCENE_PRIMITIVES scene. A world voxel v is inside when
+ * w = v - offset lies in [0, size[perm[k]]) per axis k, then mirrored axes map w_k -> E_k - 1 - w_k,
+ * and the local voxel u (u[perm[k]] = w_k) is inside the shape:
+ * box: always; sphere: |u - radius|^2 <= radius^2; terrain: fbm(u, seed) * size > u.z * 31 * 65535. */
+typedef struct tdag_primitive {
+    uint32_t type; /* 0 box, 1 sphere, 2 terrain block */
+    uint32_t xform; /* permutation id (0..5, order 012 021 102 120 201 210) | mirror bits << 3 */
+    int32_t size[3]; /* local extent per local axis */
+    int32_t radius; /* sphere radius */
+    int32_t offset[3]; /* world position of the transformed box's minimum corner */
+    uint32_t seed; /* terrain noise seed */
+    uint32_t source; /* primitive this one is a copy of (itself for originals) */
+    uint32_t reserved;
+} tdag_primitive;
+
+typedef struct tdag_svdag tdag_svdag; /* device-resident EditStructure<void, uint32_t>, library-owned */
+
+/* Primitive list of a scene (host computation, deterministic in scene->seed). */
+int tdag_scene_primitives(const tdag_scene* scene, tdag_primitive* out, uint32_t capacity, uint32_t* count);
+/* Generate the scene on the device, build its SVO and, if to_dag, deduplicate it (toDAG). */
+int tdag_scene_svdag(tdag_ctx* ctx, const tdag_scene* scene, int to_dag, tdag_svdag** out);
+/* Same from a host dense grid: dense[x + res*y + res*res*z] != 0 means solid. */
+int tdag_svdag_from_dense(tdag_ctx* ctx, const uint8_t* dense, uint32_t resolution, int to_dag, tdag_svdag** out);
+/* Device-pointer view (valid until tdag_svdag_free), the number of solid voxels of the grid, and
+ * host copies of one level (level 2 = leaves: leaf_count x 8 bytes; level >= 3: node_counts x 32 bytes). */
+int tdag_svdag_get_view(const tdag_svdag* svdag, tdag_svdag_view* out_device_view);
+int tdag_svdag_voxel_count(const tdag_svdag* svdag, uint64_t* out);
+int tdag_svdag_copy_level(tdag_ctx* ctx, const tdag_svdag* svdag, uint32_t level, void* host_dst, uint64_t dst_bytes);
+int tdag_svdag_free(tdag_svdag* svdag);
 
 #ifdef __cplusplus
 }

@@ -75,6 +75,48 @@ def fbm_value(x, y, z, seed: int):
     return total
 
 
+PERMS = ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0))
+
+
+def primitives_scene(res: int, prims: list, shell: bool = True) -> np.ndarray:
+    """Dense [z, y, x] grid of a primitive-union scene (tdag_primitive semantics, see include/tdag.h),
+    optionally reduced to its 1-voxel surface shell (a solid voxel with a 6-neighbour outside, where
+    voxels beyond the grid count as outside)."""
+    inside = np.zeros((res, res, res), dtype=bool)  # [z, y, x]
+    for p in prims:
+        perm = PERMS[p["xform"] & 7]
+        mirror = p["xform"] >> 3
+        ext = [p["size"][perm[k]] for k in range(3)]
+        lo = list(p["offset"])
+        hi = [min(lo[k] + ext[k], res) for k in range(3)]
+        if any(hi[k] <= lo[k] for k in range(3)):
+            continue
+        xs = np.arange(lo[0], hi[0]); ys = np.arange(lo[1], hi[1]); zs = np.arange(lo[2], hi[2])
+        Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+        w = [X - lo[0], Y - lo[1], Z - lo[2]]
+        for k in range(3):
+            if (mirror >> k) & 1:
+                w[k] = ext[k] - 1 - w[k]
+        u = [None, None, None]
+        for k in range(3):
+            u[perm[k]] = w[k]
+        if p["type"] == 0:
+            m = np.ones(X.shape, bool)
+        elif p["type"] == 1:
+            r = p["radius"]
+            m = (u[0] - r) ** 2 + (u[1] - r) ** 2 + (u[2] - r) ** 2 <= r * r
+        else:
+            s = p["size"][0]
+            m = fbm_value(u[0].astype(np.int64), u[1].astype(np.int64), u[2].astype(np.int64), p["seed"]) * s > u[2].astype(np.int64) * 31 * 65535
+        inside[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] |= m
+    if not shell:
+        return inside.astype(np.uint8)
+    pad = np.pad(inside, 1, constant_values=False)
+    allin = (pad[1:-1, 1:-1, :-2] & pad[1:-1, 1:-1, 2:] & pad[1:-1, :-2, 1:-1] & pad[1:-1, 2:, 1:-1]
+             & pad[:-2, 1:-1, 1:-1] & pad[2:, 1:-1, 1:-1])
+    return (inside & ~allin).astype(np.uint8)
+
+
 def terrain(res: int, seed: int = 1) -> np.ndarray:
     """Config-0 grid: dense[z, y, x] uint8, solid where fBm - z/res > 0.
 

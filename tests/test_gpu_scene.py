@@ -1,0 +1,68 @@
+"""GPU tests of the input side: SVO build (A1), toDAG (A2) and the procedural scenes (N1)."""
+import numpy as np
+import pytest
+
+from helpers import blocky_grid, random_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def _svo_struct(tdaglib, oracle, dense, dag):
+    svo = oracle.svo_from_dense(dense)
+    if dag:
+        svo = oracle.to_dag(svo)
+    return tdaglib.EditStructure.from_svo_bytes(svo)
+
+
+def _assert_same(a, b):
+    assert a.resolution == b.resolution and a.root_level == b.root_level
+    assert a.structure_type == b.structure_type
+    assert np.array_equal(a.sub_grids, b.sub_grids)
+    for la, lb in zip(a.nodes_per_level, b.nodes_per_level):
+        assert np.array_equal(la, lb)
+
+
+@pytest.mark.parametrize("dag", [False, True])
+@pytest.mark.parametrize("kind", ["random", "blocky", "terrain", "empty", "full"])
+def test_svo_and_todag_match_oracle(oracle, tdaglib, gpu_ctx, kind, dag):
+    from oracle import generator
+    dense = {"random": lambda: random_grid(32, 0.05, 1), "blocky": lambda: blocky_grid(64, 3),
+             "terrain": lambda: generator.terrain(64, 2), "empty": lambda: np.zeros((16, 16, 16), np.uint8),
+             "full": lambda: np.ones((32, 32, 32), np.uint8)}[kind]()
+    ref = _svo_struct(tdaglib, oracle, dense, dag)
+    g = tdaglib.svdag_from_dense(dense, to_dag=dag, ctx=gpu_ctx)
+    got = g.to_host()
+    _assert_same(got, ref)
+    assert g.voxel_count == int(dense.sum())
+
+
+@pytest.mark.parametrize("res,seed", [(64, 1), (128, 5)])
+def test_terrain_scene_matches_cpu_generator(oracle, tdaglib, gpu_ctx, res, seed):
+    from oracle import generator
+    dense = generator.terrain(res, seed)
+    spec = tdaglib.SceneSpec(kind=tdaglib.SCENE_TERRAIN, resolution=res, seed=seed, shell=False)
+    got = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx)
+    _assert_same(got.to_host(), _svo_struct(tdaglib, oracle, dense, True))
+    assert got.voxel_count == int(dense.sum())
+
+
+@pytest.mark.parametrize("res,n,seed,shell", [(64, 40, 3, True), (128, 120, 7, True), (128, 60, 9, False)])
+def test_primitive_scene_matches_cpu_generator(oracle, tdaglib, gpu_ctx, res, n, seed, shell):
+    from oracle import generator
+    spec = tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=res, seed=seed, num_primitives=n, copy_percent=30, shell=shell)
+    prims = tdaglib.scene_primitives(spec)
+    dense = generator.primitives_scene(res, prims, shell=shell)
+    got = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx)
+    _assert_same(got.to_host(), _svo_struct(tdaglib, oracle, dense, True))
+    assert got.voxel_count == int(dense.sum())
+
+
+def test_scene_build_end_to_end_matches_oracle(oracle, tdaglib, gpu_ctx):
+    """Device scene -> device SVDAG -> device TDAG equals the oracle's TDAG of the same SVDAG."""
+    spec = tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=128, seed=11, num_primitives=150)
+    g = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx)
+    host = g.to_host()
+    ref, _, _ = oracle.construct_tdag(host.to_svo_bytes())
+    cfg = tdaglib.TransformDAGConfig()
+    got = tdaglib.write_tdag(tdaglib.construct_transform_dag(host, cfg, ctx=gpu_ctx), cfg)
+    assert got == ref
