@@ -1,0 +1,446 @@
+"""Benchmark: Transform-DAG construction throughput (Mvoxels/s) on GB300.
+
+Workload (one step = one constructTransformDAG over one SVDAG): the 2048^3 single-grid build,
+exhaustive symmetry + axis permutation + translation matching at the reference's default window
+(maxTranslationLevel 4). The grid is a seeded union of 4,000 boxes / spheres / fBm terrain blocks,
+30% of them mirrored, axis-permuted or translated copies of earlier ones, reduced to its 1-voxel
+surface shell, generated on the device (synthetic data; the reference's mesh scenes are not
+available). SVO build and toDAG happen once before timing.
+
+value   : solid input voxels / device time of the build, input and output resident in HBM.
+e2e     : the same through tdag_build() with pinned host buffers: host->device copy of the SVDAG,
+          the build, and the device->host copy of the Transform DAG inside the timed region.
+roofline: the dominant kernel (the translation search of the level with the largest device time),
+          algorithmic bytes per launch / its CUDA-event duration, against MEASURED_PEAKS.json.
+cpu_baseline / --impl reference: the CPU oracle (a restatement of the reference's CPU path, all
+          host threads) on a bounded sub-volume sample of the same grid.
+
+Multi-GPU: the path does not shard; --gpus N runs N independent replicas (one per rank), and value
+is the sum of their throughputs (max-over-ranks timing).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "i3d2025-voxel-transform-dag_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "TDAG build Mvoxels/s"
+UNIT = "Mvoxels/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--resolution", type=int, default=2048)
+    ap.add_argument("--primitives", type=int, default=4000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(args, voxels=None):
+    cfg = {
+        "workload": f"single-grid exhaustive TDAG build, {args.resolution}^3 primitive-union shell "
+                    f"({args.primitives} primitives, 30% transformed copies, seed {args.seed}), "
+                    f"symmetry+axis permutation+translation, maxTranslationLevel 4",
+        "resolution": args.resolution,
+        "primitives": args.primitives,
+        "seed": args.seed,
+        "l2": "flushed between timed steps (256 MiB device write)",
+    }
+    if voxels is not None:
+        cfg["solid_voxels"] = int(voxels)
+    return cfg
+
+
+# ------------------------------------------------------------------------------------------------
+# distributed helpers (torchrun: one process per GPU, replicas)
+# ------------------------------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU sample: a sub-volume of the same grid, as its own SVDAG (.svo bytes)
+# ------------------------------------------------------------------------------------------------
+def sub_volume_svo(host, sample_res: int):
+    """Extract the SVDAG of the densest aligned sample_res^3 sub-volume reachable from the root."""
+    import tdag
+    target_level = sample_res.bit_length() - 1
+    levels = host.nodes_per_level
+    # voxel counts per node, bottom-up
+    pc = np.array([bin(int(v)).count("1") for v in host.sub_grids], dtype=np.int64)
+    counts = {2: pc}
+    for lvl in range(3, host.root_level + 1):
+        n = levels[lvl].astype(np.int64)
+        e = n == tdag.EMPTY_CHILD
+        counts[lvl] = np.where(e, 0, counts[lvl - 1][np.where(e, 0, n)]).sum(axis=1)
+    # walk down from the root along the densest child to the target level
+    node = 0
+    for lvl in range(host.root_level, target_level, -1):
+        ch = levels[lvl][node].astype(np.int64)
+        best, bestc = None, -1
+        for c in ch:
+            if c != tdag.EMPTY_CHILD and counts[lvl - 1][c] > bestc:
+                best, bestc = int(c), int(counts[lvl - 1][c])
+        node = best
+    # collect reachable items per level and re-index
+    new_levels = [np.zeros((0, 8), np.uint32) for _ in range(target_level + 1)]
+    frontier = np.array([node], dtype=np.int64)
+    remap_prev = None
+    order = {}
+    for lvl in range(target_level, 2, -1):
+        order[lvl] = frontier
+        ch = levels[lvl][frontier].astype(np.int64)
+        nxt = np.unique(ch[ch != tdag.EMPTY_CHILD])
+        frontier = nxt
+    order[2] = frontier
+    for lvl in range(3, target_level + 1):
+        ids = order[lvl]
+        below = order[lvl - 1]
+        ch = levels[lvl][ids].astype(np.int64)
+        e = ch == tdag.EMPTY_CHILD
+        pos = np.searchsorted(below, np.where(e, below[0] if len(below) else 0, ch))
+        new_levels[lvl] = np.where(e, tdag.EMPTY_CHILD, pos).astype(np.uint32)
+    sub = tdag.EditStructure(new_levels, host.sub_grids[order[2]].copy(), sample_res, target_level, 1, "u32")
+    return sub.to_svo_bytes(), int(counts[target_level][node])
+
+
+def cpu_sample_run(svo: bytes, threads: int = 0):
+    from oracle import oracle as orc
+    orc.build()
+    if threads:
+        orc.set_threads(threads)
+    t0 = time.perf_counter()
+    _, st, _ = orc.construct_tdag(svo, True, True, True, 4)
+    return time.perf_counter() - t0, st
+
+
+def choose_sample(host, requested: int, budget_s: float):
+    """Pick the largest sub-volume side (power of two) whose oracle run fits the time budget."""
+    sizes = [requested] if requested else [512, 256, 128]
+    last = None
+    for s in sizes:
+        if s >= host.resolution:
+            continue
+        svo, vox = sub_volume_svo(host, s)
+        last = (s, svo, vox)
+        if requested:
+            break
+        # estimate from a probe on the next smaller side
+        if s > 128:
+            psvo, pvox = sub_volume_svo(host, s // 2)
+            dt, _ = cpu_sample_run(psvo)
+            est = dt * (vox / max(pvox, 1))
+            if est <= budget_s:
+                return last
+            continue
+        return last
+    return last
+
+
+# ------------------------------------------------------------------------------------------------
+# roofline of the dominant kernel
+# ------------------------------------------------------------------------------------------------
+GRID_BYTES = {2: 8, 3: 64, 4: 512}
+
+
+def search_algorithmic_bytes(level: int, st: dict) -> float:
+    """Translation search of one level: every source grid read once (M*G), one 16-byte (hash, range)
+    table slot per non-empty probe (P*16), two grids per verification (V*2G)."""
+    G = GRID_BYTES[level]
+    return st["items"] * G + st["probes"] * 16 + st["verifications"] * 2 * G
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(level: int):
+    p = os.path.join(REPO, "profiles", "search_traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(str(level))
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------------------------------------
+def run_reference(args, world, rank, pg):
+    """Reference arm: the CPU restatement of the reference path (all host threads) on a bounded
+    sub-volume sample of the same grid; only rank 0 works."""
+    if rank != 0:
+        barrier(pg)
+        return
+    import tdag
+    ctx = tdag.default_context()
+    spec = tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+    g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
+    host = g.to_host()
+    g.free()
+    s = args.sample_resolution or 256
+    svo, vox = sub_volume_svo(host, s)
+    from oracle import oracle as orc
+    orc.build()
+    cores = orc.max_threads()
+    for _ in range(args.warmup):
+        cpu_sample_run(svo)
+    times = []
+    for _ in range(args.steps):
+        dt, _ = cpu_sample_run(svo)
+        times.append(dt)
+    total = sum(times)
+    value = vox * len(times) / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": workload_config(args, host.compute_voxel_count()),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{s}^3 densest sub-volume of the same grid ({vox} solid voxels) per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(pg)
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    import tdag
+    from tdag import _abi
+
+    dev = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(dev)
+    ctx = tdag.Context(dev)
+    spec = tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+    g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
+    voxels = g.voxel_count
+    cfg = tdag.TransformDAGConfig()
+    sp = ctypes.c_void_p()
+    _abi.check(tdag.lib().tdag_ctx_stream(ctx.handle, ctypes.byref(sp)))
+    lib_stream = torch.cuda.ExternalStream(sp.value, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def step():
+        r = tdag.construct_transform_dag_device(g, cfg, ctx=ctx)
+        st = r.stats
+        r.free()
+        return st
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    # ---- timed, device-resident
+    clocks = ClockSampler(dev)
+    barrier(pg)
+    torch.cuda.synchronize()
+    clocks.start()
+    dev_ms, stats_list = 0.0, []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lib_stream)
+        st = step()
+        e1.record(lib_stream)
+        e1.synchronize()
+        dev_ms += e0.elapsed_time(e1)
+        stats_list.append(st)
+    torch.cuda.synchronize()
+    barrier(pg)
+    clk = clocks.stop()
+    dev_ms = max_over_ranks(pg, dev_ms)
+    value = voxels * args.steps * world / (dev_ms / 1e3) / 1e6
+
+    # ---- e2e through tdag_build with pinned host buffers
+    host = g.to_host()
+    keep = []
+    view = _abi.SvdagView()
+    view.resolution, view.root_level, view.structure_type = host.resolution, host.root_level, host.structure_type
+    h2d = 0
+    for lvl in range(3, host.root_level + 1):
+        a = host.nodes_per_level[lvl]
+        pt = torch.empty(a.size, dtype=torch.int32, pin_memory=True)
+        pn = pt.numpy().view(np.uint32)
+        pn[:] = a.reshape(-1)
+        keep.append(pt)
+        view.nodes[lvl] = ctypes.cast(pn.ctypes.data, ctypes.POINTER(ctypes.c_uint32))
+        view.node_counts[lvl] = a.shape[0]
+        h2d += a.nbytes
+    lt = torch.empty(host.sub_grids.size, dtype=torch.int64, pin_memory=True)
+    ln = lt.numpy().view(np.uint64)
+    ln[:] = host.sub_grids
+    keep.append(lt)
+    view.leaves = ctypes.cast(ln.ctypes.data, ctypes.POINTER(ctypes.c_uint64))
+    view.leaf_count = host.sub_grids.size
+    h2d += host.sub_grids.nbytes
+    cfg_c = tdag._config_struct(cfg)
+    d2h = 0
+    e2e_s = 0.0
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        rp = ctypes.POINTER(_abi.Result)()
+        t0 = time.perf_counter()
+        _abi.check(tdag.lib().tdag_build(ctx.handle, ctypes.byref(view), ctypes.byref(cfg_c), ctypes.byref(rp)))
+        dt = time.perf_counter() - t0
+        r = rp.contents
+        d2h = sum(r.node_counts[l] * 64 for l in range(3, r.root_level + 1)) + r.leaf_count * 8
+        tdag.lib().tdag_result_free(rp)
+        if i >= args.warmup:
+            e2e_s += dt
+    e2e_s = max_over_ranks(pg, e2e_s)
+    e2e_value = voxels * args.steps * world / e2e_s / 1e6
+
+    # ---- roofline of the dominant kernel
+    last = stats_list[-1]
+    lvl_times = {L: sum(s["translation"][L]["search_ms"] for s in stats_list) / len(stats_list) for L in (2, 3, 4)}
+    dom = max(lvl_times, key=lambda L: lvl_times[L])
+    ms = lvl_times[dom]
+    alg = search_algorithmic_bytes(dom, last["translation"][dom])
+    achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else None
+    peak, peak_kind = load_peaks()
+    roof = {"bound": "hbm", "kernel": f"searchKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+            "traffic": load_traffic(dom), "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (device-generated primitive scene; no public dataset)",
+        "config": workload_config(args, voxels),
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "clocks": clk,
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats_list)),
+        "subgrids_matched_per_s": sum(last["translation"][L]["items"] for L in (2, 3, 4)) / (dev_ms / args.steps / 1e3),
+        "stage_ms": {"hierarchical": last["hierarchical_ms"], "translation": last["translation_ms"],
+                     "search_L4": lvl_times[4], "search_L3": lvl_times[3], "search_L2": lvl_times[2]},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.build()
+        s, svo, vox = choose_sample(host, args.sample_resolution, budget_s=20.0)
+        dt, _ = cpu_sample_run(svo)
+        out["cpu_baseline"] = {"value": vox / dt / 1e6, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
+                               "sample": f"{s}^3 densest sub-volume of the same grid ({vox} solid voxels), one oracle build, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -391,7 +391,7 @@ std::vector<tdag_primitive> scenePrimitives(const tdag_scene& sc)
                 p.size[0] = p.size[1] = p.size[2] = 2 * p.radius + 1;
             } else {
                 p.type = 2;
-                const int32_t s = rng.range(scaled(64), scaled(512));
+                const int32_t s = rng.range(scaled(32), scaled(256));
                 p.size[0] = p.size[1] = p.size[2] = s;
             }
             p.xform = 0;
