@@ -349,6 +349,7 @@ def run_ours(args, world, rank, local, pg):
         e1.synchronize()
         dev_ms += e0.elapsed_time(e1)
         stats_list.append(st)
+        print(f"[bench] step {len(stats_list)}: {e0.elapsed_time(e1):.2f} ms (library {st['total_ms']:.2f} ms)", file=sys.stderr, flush=True)
     torch.cuda.synchronize()
     barrier(pg)
     clk = clocks.stop()

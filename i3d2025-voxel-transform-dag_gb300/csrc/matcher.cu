@@ -11,11 +11,23 @@
 //   * candidates are filtered by the config (:840-845), skipped when they cannot lower the target's
 //     parent (:830-850), verified by an exact grid comparison (:857-862) and merged with a 64-bit
 //     atomic minimum (:864);
+//   * sources run in batches of increasing popcount order; after a batch the table drops every
+//     target whose parent no later source can lower (:887-915);
 //   * the isUnique pass keeps every item that is nobody's child or somebody's parent (:953-961) and
 //     numbers the kept items in their original order (:982-997).
 // The result is the minimum encoded pointer over all verified candidates, which does not depend on
-// thread order, so the GPU output equals the CPU output bit for bit.
+// thread order or batching, so the GPU output equals the CPU output bit for bit.
+//
+// Search kernel layout (one team of R*R threads per source grid, one thread per grid line):
+//   pass 1 (6 per source) folds the occupancy bits along axis a0 into G1, pass 2 (24 per source)
+//   folds G1 along a1 into G2, pass 3 (48 per source) folds G2 along a2 in place — the thread keeps
+//   its original line in registers so both a2 directions come from one G2. Passes 1 and 2 are shared
+//   by the permutations that start with the same axes (78 passes instead of 144). Every non-zero hash
+//   is tested against a one-bit membership filter (global, L2-resident), the survivors are queued in
+//   shared memory, looked up in the table (16-byte slots: key + range) and each hit's candidate range
+//   is spread across the warp.
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.cuh"
@@ -35,6 +47,23 @@ __device__ __forceinline__ uint64_t foldStep(uint64_t acc, uint64_t v)
     return started ? c : 0;
 }
 
+// Table slot and membership-filter indices (32-bit multiply-xorshift hashes of the 64-bit key).
+__host__ __device__ __forceinline__ uint32_t slotHash(uint64_t k)
+{
+    uint32_t h = (uint32_t)k * 0xCC9E2D51u ^ (uint32_t)(k >> 32) * 0x1B873593u;
+    h ^= h >> 15;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    return h;
+}
+__host__ __device__ __forceinline__ uint32_t filterHash(uint64_t k)
+{
+    uint32_t h = ((uint32_t)k ^ (uint32_t)(k >> 32)) * 0x9E3779B1u;
+    h ^= h >> 16;
+    h *= 0x7FEB352Du;
+    return h;
+}
+
 // ---------------------------------------------------------------------------- popcount order
 template <int W>
 __global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n, uint32_t maxCount, uint64_t* __restrict__ key, uint32_t* __restrict__ val)
@@ -48,13 +77,6 @@ __global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n
         c += __popcll(grids[(size_t)i * W + k]);
     key[i] = maxCount - c; // ascending key == descending popcount; stable sort keeps index order
     val[i] = i;
-}
-
-__global__ void invertOrderKernel(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ posOf)
-{
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < n)
-        posOf[order[r]] = r;
 }
 
 // ---------------------------------------------------------------------------- corner hashes
@@ -106,24 +128,23 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
 }
 
 // ---------------------------------------------------------------------------- corner-hash table
-__device__ __forceinline__ uint64_t slotHash(uint64_t key) { return mix64(key ^ 0x2545F4914F6CDD1Dull); }
-
-__global__ void tableInsertKernel(const uint64_t* __restrict__ ekeys, size_t m, uint64_t* __restrict__ tkeys, uint32_t* __restrict__ tcount,
-    uint32_t* __restrict__ slotOfEntry, uint64_t capMask, uint32_t* __restrict__ numDistinct, uint32_t* status)
+// slots: (key, start | count << 32) pairs; entries: payload (item * 8 + corner) grouped by key.
+__global__ void tableInsertKernel(const uint64_t* __restrict__ ekeys, size_t m, ulonglong2* __restrict__ slots, uint32_t* __restrict__ tcount,
+    uint32_t* __restrict__ slotOfEntry, uint32_t capMask, uint32_t* __restrict__ numDistinct, uint32_t* status)
 {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m)
         return;
     const uint64_t key = ekeys[e];
-    if (key == 0) {
+    if (key == 0) { // an empty grid has no corner view (find_translation.cpp:722)
         slotOfEntry[e] = 0xFFFFFFFFu;
         return;
     }
-    uint64_t slot = slotHash(key) & capMask;
-    for (uint64_t probe = 0; probe <= capMask; ++probe) {
-        uint64_t cur = tkeys[slot];
+    uint32_t slot = slotHash(key) & capMask;
+    for (uint32_t probe = 0; probe <= capMask; ++probe) {
+        unsigned long long cur = slots[slot].x;
         if (cur == 0) {
-            cur = atomicCAS((unsigned long long*)&tkeys[slot], 0ull, (unsigned long long)key);
+            cur = atomicCAS(&slots[slot].x, 0ull, (unsigned long long)key);
             if (cur == 0) {
                 atomicAdd(numDistinct, 1u);
                 cur = key;
@@ -131,7 +152,7 @@ __global__ void tableInsertKernel(const uint64_t* __restrict__ ekeys, size_t m, 
         }
         if (cur == key) {
             atomicAdd(&tcount[slot], 1u);
-            slotOfEntry[e] = (uint32_t)slot;
+            slotOfEntry[e] = slot;
             return;
         }
         slot = (slot + 1) & capMask;
@@ -153,31 +174,50 @@ __global__ void tableScatterKernel(const uint32_t* __restrict__ epayload, const 
     entries[p] = epayload[e];
 }
 
-__global__ void tableRangesKernel(const uint64_t* __restrict__ tkeys, const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ tcount, uint64_t cap,
-    uint64_t* __restrict__ ranges, uint32_t* __restrict__ filter, uint64_t filterMask)
+__global__ void tableRangesKernel(ulonglong2* __restrict__ slots, const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ tcount, uint32_t cap,
+    uint32_t* __restrict__ filter, uint32_t filterShift)
 {
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cap)
         return;
-    const uint64_t key = tkeys[s];
-    ranges[s] = (uint64_t)tstart[s] | ((uint64_t)tcount[s] << 32);
+    const uint64_t key = slots[s].x;
+    slots[s].y = (uint64_t)tstart[s] | ((uint64_t)tcount[s] << 32);
     if (key != 0) {
-        const uint64_t fb = (slotHash(key) >> 20) & filterMask;
+        const uint32_t fb = filterHash(key) >> filterShift;
         atomicOr(&filter[fb >> 5], 1u << (fb & 31));
     }
+}
+
+// Entries still able to receive a lower parent: parent[target] > minKey of the next source batch.
+__global__ void liveEntriesKernel(const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay, size_t m, const unsigned long long* __restrict__ parents,
+    unsigned long long minKeyNext, uint32_t* __restrict__ flags)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m)
+        return;
+    flags[e] = (ekeys[e] != 0) && (parents[epay[e] >> 3] > minKeyNext);
+}
+
+__global__ void gatherEntriesKernel(const uint32_t* __restrict__ idx, uint32_t n, const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay,
+    uint64_t* __restrict__ k2, uint32_t* __restrict__ p2)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    k2[i] = ekeys[idx[i]];
+    p2[i] = epay[idx[i]];
 }
 
 // ---------------------------------------------------------------------------- search
 struct SearchParams {
     const uint64_t* grids; // n x W, original order
     const uint32_t* order; // sorted position -> original position
-    uint32_t n;
-    const uint64_t* tkeys;
-    const uint64_t* tranges;
-    uint64_t capMask;
+    uint32_t begin, end; // sorted positions of this batch
+    const ulonglong2* slots;
+    uint32_t capMask;
     const uint32_t* entries;
     const uint32_t* filter;
-    uint64_t filterMask;
+    uint32_t filterShift;
     unsigned long long* parents; // encoded parent per original position
     uint32_t* workCounter;
     unsigned long long* counters; // probes, filterPass, hits, candidates, verifications, verified
@@ -187,28 +227,29 @@ struct SearchParams {
 template <int R>
 struct SearchShape {
     static constexpr int TEAM = R * R; // one thread per line
-    static constexpr int TEAMS = (kThreads / TEAM) > 0 ? (kThreads / TEAM) : 1;
+    static constexpr int TEAMS = kThreads / TEAM;
     static constexpr int W = R * R * R / 64;
     static constexpr int SY = R + 1;
     static constexpr int SZ = (R + 1) * R;
     static constexpr int GRID = (R + 1) * R * R; // padded u64 hash grid
-    // per team: G1, G2 (u64), srcW (u64), lines[3][R*R] (u16)
-    static constexpr size_t TEAM_BYTES = (size_t)(2 * GRID + W) * 8 + 3 * R * R * 2;
+    static constexpr int N = R * R * R;
+    // per team: G1, G2, G3 (u64), srcW (u64), lines[3][R*R] (u16), queue[N] (u16), queue count (u32)
+    static constexpr size_t TEAM_BYTES = (size_t)(3 * GRID + W) * 8 + 3 * R * R * 2 + N * 2 + 16;
     static constexpr size_t SMEM = TEAM_BYTES * TEAMS + 16;
 };
 
-template <int R>
-__device__ __forceinline__ int sidx(int x, int y, int z) { return x + SearchShape<R>::SY * y + SearchShape<R>::SZ * z; }
+__device__ __forceinline__ int smemStride(int a, int SY, int SZ) { return a == 0 ? 1 : (a == 1 ? SY : SZ); }
+__device__ __forceinline__ int otherLo(int a) { return a == 0 ? 1 : 0; }
+__device__ __forceinline__ int otherHi(int a) { return a == 2 ? 1 : 2; }
 
 // Exact verification: target == translate(mirror(permute(source, P), S), T) (find_translation.cpp:857-862),
 // row by row. lines[a][u_lo + R u_hi] holds the source's voxels along axis a (bit j = coordinate j).
 template <int R>
-__device__ bool verifyCandidate(const uint64_t* __restrict__ tgrid, const uint16_t* lines, int a0, int a1, int a2, uint32_t S, int T0, int T1, int T2)
+__device__ __noinline__ bool verifyCandidate(const uint64_t* __restrict__ tgrid, const uint16_t* lines, int a0, int a1, int a2, uint32_t S, int T0, int T1, int T2)
 {
     constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
     const uint16_t* L = lines + a0 * R * R;
-    const int lo = (a0 == 0) ? 1 : 0; // other axes of a0 in increasing order
-    const int hi = (a0 == 2) ? 1 : 2;
+    const int lo = otherLo(a0), hi = otherHi(a0);
     for (int w2 = 0; w2 < R; ++w2) {
         for (int w1 = 0; w1 < R; ++w1) {
             const uint32_t bitOff = (uint32_t)(R * (w1 + R * w2));
@@ -220,10 +261,10 @@ __device__ bool verifyCandidate(const uint64_t* __restrict__ tgrid, const uint16
                     y1 = R - 1 - y1;
                 if (S & 4)
                     y2 = R - 1 - y2;
-                int u[3];
-                u[a1] = y1;
-                u[a2] = y2;
-                uint32_t line = L[u[lo] + R * u[hi]];
+                // u[a1] = y1, u[a2] = y2; line index = u[lo] + R u[hi]
+                const int ulo = (lo == a1) ? y1 : y2;
+                const int uhi = (hi == a1) ? y1 : y2;
+                uint32_t line = L[ulo + R * uhi];
                 if (S & 1)
                     line = __brev(line) >> (32 - R);
                 zrow = (T0 >= 0) ? ((line << T0) & rowMask) : (line >> (-T0));
@@ -236,75 +277,79 @@ __device__ bool verifyCandidate(const uint64_t* __restrict__ tgrid, const uint16
 }
 
 template <int R, int L>
-__global__ void __launch_bounds__(kThreads) searchKernel(SearchParams p)
+__global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
 {
     using Sh = SearchShape<R>;
-    constexpr int TEAM = Sh::TEAM, TEAMS = Sh::TEAMS, W = Sh::W;
+    constexpr int TEAM = Sh::TEAM, TEAMS = Sh::TEAMS, W = Sh::W, SY = Sh::SY, SZ = Sh::SZ, N = Sh::N;
     constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
     extern __shared__ __align__(16) uint8_t smem[];
     const int team = threadIdx.x / TEAM;
     const int tl = threadIdx.x % TEAM;
-    const bool active = team < TEAMS;
-    uint8_t* tb = smem + (size_t)(active ? team : 0) * Sh::TEAM_BYTES;
+    const uint32_t lane = threadIdx.x & 31;
+    uint8_t* tb = smem + (size_t)team * Sh::TEAM_BYTES;
     uint64_t* G1 = reinterpret_cast<uint64_t*>(tb);
     uint64_t* G2 = G1 + Sh::GRID;
-    uint64_t* srcW = G2 + Sh::GRID;
+    uint64_t* G3 = G2 + Sh::GRID;
+    uint64_t* srcW = G3 + Sh::GRID;
     uint16_t* lines = reinterpret_cast<uint16_t*>(srcW + W);
+    uint16_t* queue = lines + 3 * R * R;
+    uint32_t* qcount = reinterpret_cast<uint32_t*>(queue + N);
     uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::TEAM_BYTES * TEAMS);
+    const int c1 = tl % R, c2 = tl / R;
 
     unsigned long long cProbe = 0, cFilter = 0, cHit = 0, cCand = 0, cVer = 0, cOk = 0;
 
     for (;;) {
         if (threadIdx.x == 0)
-            *shBase = atomicAdd(p.workCounter, (uint32_t)TEAMS);
+            *shBase = p.begin + atomicAdd(p.workCounter, (uint32_t)TEAMS);
         __syncthreads();
         const uint32_t base = *shBase;
         __syncthreads();
-        if (base >= p.n)
+        if (base >= p.end)
             break;
         const uint32_t r = base + team;
-        const bool valid = active && r < p.n;
+        const bool valid = r < p.end;
         // ---- load the source grid and its three line orientations
         if (valid) {
             const uint64_t* g = p.grids + (size_t)p.order[r] * W;
             for (int k = tl; k < W; k += TEAM)
                 srcW[k] = g[k];
         }
+        if (tl == 0)
+            *qcount = 0;
         __syncthreads();
         if (valid) {
-            const int c1 = tl % R, c2 = tl / R;
-            // x-lines: (y, z) = (c1, c2)
-            {
-                const uint32_t off = (uint32_t)R * (c1 + R * c2);
-                lines[0 * R * R + tl] = (uint16_t)((srcW[off >> 6] >> (off & 63)) & rowMask);
-            }
+            const uint32_t off = (uint32_t)R * (c1 + R * c2); // x-line at (y, z) = (c1, c2)
+            lines[tl] = (uint16_t)((srcW[off >> 6] >> (off & 63)) & rowMask);
             uint32_t ly = 0, lz = 0;
+#pragma unroll
             for (int j = 0; j < R; ++j) {
                 const uint32_t iy = c1 + R * j + R * R * c2; // (x=c1, y=j, z=c2)
                 const uint32_t iz = c1 + R * c2 + R * R * j; // (x=c1, y=c2, z=j)
                 ly |= (uint32_t)((srcW[iy >> 6] >> (iy & 63)) & 1) << j;
                 lz |= (uint32_t)((srcW[iz >> 6] >> (iz & 63)) & 1) << j;
             }
-            lines[1 * R * R + tl] = (uint16_t)ly; // index x + R z
+            lines[R * R + tl] = (uint16_t)ly; // index x + R z
             lines[2 * R * R + tl] = (uint16_t)lz; // index x + R y
         }
         __syncthreads();
 
-        const uint64_t srcPos = r;
         for (int a0 = 0; a0 < 3; ++a0) {
             for (int d0 = 1; d0 >= 0; --d0) {
                 // ---- pass 1 along a0 from the occupancy bits
                 if (valid) {
-                    const int b = (a0 == 0) ? 1 : 0, c = (a0 == 2) ? 1 : 2;
-                    int u[3];
-                    u[b] = tl % R;
-                    u[c] = tl / R;
+                    const int lo = otherLo(a0), hi = otherHi(a0);
+                    const int bs = a0 == 0 ? 1 : (a0 == 1 ? R : R * R);
+                    const int bbase = c1 * (lo == 0 ? 1 : (lo == 1 ? R : R * R)) + c2 * (hi == 1 ? R : R * R);
+                    const int ss = smemStride(a0, SY, SZ);
+                    const int sbase = c1 * smemStride(lo, SY, SZ) + c2 * smemStride(hi, SY, SZ);
                     uint64_t acc = 0;
+#pragma unroll 4
                     for (int k = 0; k < R; ++k) {
-                        u[a0] = d0 ? R - 1 - k : k;
-                        const uint32_t bi = u[0] + R * u[1] + R * R * u[2];
+                        const int c = d0 ? R - 1 - k : k;
+                        const int bi = bbase + c * bs;
                         acc = foldStep(acc, (srcW[bi >> 6] >> (bi & 63)) & 1);
-                        G1[sidx<R>(u[0], u[1], u[2])] = acc;
+                        G1[sbase + c * ss] = acc;
                     }
                 }
                 __syncthreads();
@@ -315,88 +360,152 @@ __global__ void __launch_bounds__(kThreads) searchKernel(SearchParams p)
                     for (int d1 = 1; d1 >= 0; --d1) {
                         // ---- pass 2 along a1
                         if (valid) {
-                            const int b = (a1 == 0) ? 1 : 0, c = (a1 == 2) ? 1 : 2;
-                            int u[3];
-                            u[b] = tl % R;
-                            u[c] = tl / R;
+                            const int lo = otherLo(a1), hi = otherHi(a1);
+                            const int ss = smemStride(a1, SY, SZ);
+                            const int sbase = c1 * smemStride(lo, SY, SZ) + c2 * smemStride(hi, SY, SZ);
                             uint64_t acc = 0;
+#pragma unroll 4
                             for (int k = 0; k < R; ++k) {
-                                u[a1] = d1 ? R - 1 - k : k;
-                                const int si = sidx<R>(u[0], u[1], u[2]);
-                                acc = foldStep(acc, G1[si]);
-                                G2[si] = acc;
+                                const int c = d1 ? R - 1 - k : k;
+                                acc = foldStep(acc, G1[sbase + c * ss]);
+                                G2[sbase + c * ss] = acc;
                             }
                         }
                         __syncthreads();
-                        // ---- pass 3 along a2, consumed in place
-                        if (valid) {
-                            const int b = (a2 == 0) ? 1 : 0, c = (a2 == 2) ? 1 : 2;
-                            int u[3];
-                            u[b] = tl % R;
-                            u[c] = tl / R;
-                            for (int d2 = 1; d2 >= 0; --d2) {
-                                const uint32_t dir = (uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2);
-                                const int anchor0 = d0 ? 0 : R - 1, anchor1 = d1 ? 0 : R - 1, anchor2 = d2 ? 0 : R - 1;
+                        // ---- pass 3 along a2 into G3, fused with the membership filter; survivors queued
+                        const int lo3 = otherLo(a2), hi3 = otherHi(a2);
+                        const int ss3 = smemStride(a2, SY, SZ);
+                        const int sbase3 = c1 * smemStride(lo3, SY, SZ) + c2 * smemStride(hi3, SY, SZ);
+                        const int ls3 = a2 == 0 ? 1 : (a2 == 1 ? R : R * R); // logical stride along a2
+                        const int lbase3 = c1 * (lo3 == 0 ? 1 : (lo3 == 1 ? R : R * R)) + c2 * (hi3 == 1 ? R : R * R);
+#pragma unroll
+                        for (int d2 = 1; d2 >= 0; --d2) {
+                            uint32_t pass = 0;
+                            if (valid) {
                                 uint64_t acc = 0;
+#pragma unroll 4
                                 for (int k = 0; k < R; ++k) {
-                                    u[a2] = d2 ? R - 1 - k : k;
-                                    acc = foldStep(acc, G2[sidx<R>(u[0], u[1], u[2])]);
-                                    if (acc == 0)
-                                        continue;
-                                    ++cProbe;
-                                    const uint64_t h = slotHash(acc);
-                                    const uint64_t fb = (h >> 20) & p.filterMask;
-                                    if (!((__ldg(&p.filter[fb >> 5]) >> (fb & 31)) & 1))
-                                        continue;
-                                    ++cFilter;
-                                    uint64_t slot = h & p.capMask;
-                                    uint64_t range = 0;
-                                    bool hit = false;
-                                    for (uint64_t probe = 0; probe <= p.capMask; ++probe) {
-                                        const uint64_t tk = __ldg(&p.tkeys[slot]);
-                                        if (tk == acc) {
-                                            range = __ldg(&p.tranges[slot]);
-                                            hit = true;
+                                    const int c = d2 ? R - 1 - k : k;
+                                    acc = foldStep(acc, G2[sbase3 + c * ss3]);
+                                    G3[sbase3 + c * ss3] = acc;
+                                    if (acc != 0) {
+                                        ++cProbe;
+                                        const uint32_t fb = filterHash(acc) >> p.filterShift;
+                                        if ((__ldg(&p.filter[fb >> 5]) >> (fb & 31)) & 1)
+                                            pass |= 1u << c;
+                                    }
+                                }
+                            }
+                            // warp-aggregated enqueue of the surviving voxels (logical index x + R y + R^2 z)
+                            {
+                                const uint32_t np = __popc(pass);
+                                cFilter += np;
+                                uint32_t incl = np;
+#pragma unroll
+                                for (int o = 1; o < 32; o <<= 1) {
+                                    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                                    if ((int)lane >= o)
+                                        incl += t;
+                                }
+                                // teams smaller than a warp keep separate counters: restrict the scan to the team
+                                uint32_t excl = incl - np;
+                                if (TEAM < 32) {
+                                    const uint32_t teamFirst = lane & ~(uint32_t)(TEAM - 1);
+                                    // every lane takes part in the shuffle; lane 0's exclusive prefix is 0
+                                    const uint32_t before = __shfl_sync(0xffffffffu, incl - np, teamFirst);
+                                    excl -= before;
+                                    const uint32_t teamTotal = __shfl_sync(0xffffffffu, incl, teamFirst + TEAM - 1) - before;
+                                    uint32_t off = 0;
+                                    if (tl == 0 && teamTotal)
+                                        off = atomicAdd(qcount, teamTotal);
+                                    off = __shfl_sync(0xffffffffu, off, teamFirst);
+                                    excl += off;
+                                } else {
+                                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                                    uint32_t off = 0;
+                                    if (lane == 0 && total)
+                                        off = atomicAdd(qcount, total);
+                                    excl += __shfl_sync(0xffffffffu, off, 0);
+                                }
+                                while (pass) {
+                                    const int c = __ffs(pass) - 1;
+                                    pass &= pass - 1;
+                                    queue[excl++] = (uint16_t)(lbase3 + c * ls3);
+                                }
+                            }
+                            __syncthreads();
+                            // ---- table lookups and candidates (warp-uniform trip count)
+                            const uint32_t qn = valid ? *qcount : 0u;
+                            const uint32_t qmax = __reduce_max_sync(0xffffffffu, qn);
+                            const uint32_t dir = (uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2);
+                            for (uint32_t qb = 0; qb < qmax; qb += TEAM) {
+                                const uint32_t q = qb + tl;
+                                uint32_t start = 0, cnt = 0, vidx = 0;
+                                if (q < qn) {
+                                    vidx = queue[q];
+                                    const int x = vidx % R, y = (vidx / R) % R, z = vidx / (R * R);
+                                    const uint64_t h = G3[x + SY * y + SZ * z];
+                                    uint32_t slot = slotHash(h) & p.capMask;
+                                    for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
+                                        const ulonglong2 sv = p.slots[slot];
+                                        if (sv.x == h) {
+                                            start = (uint32_t)sv.y;
+                                            cnt = (uint32_t)(sv.y >> 32);
                                             break;
                                         }
-                                        if (tk == 0)
+                                        if (sv.x == 0)
                                             break;
                                         slot = (slot + 1) & p.capMask;
                                     }
-                                    if (!hit)
-                                        continue;
-                                    ++cHit;
-                                    // permuted voxel = (u[a0], u[a1], u[a2])
-                                    const int v0 = u[a0], v1 = u[a1], v2 = u[a2];
-                                    const uint32_t start = (uint32_t)range, cnt = (uint32_t)(range >> 32);
-                                    for (uint32_t e = 0; e < cnt; ++e) {
-                                        const uint32_t pay = __ldg(&p.entries[start + e]);
+                                    cHit += cnt ? 1 : 0;
+                                }
+                                uint32_t hitMask = __ballot_sync(0xffffffffu, cnt != 0);
+                                while (hitMask) {
+                                    const int src = __ffs(hitMask) - 1;
+                                    hitMask &= hitMask - 1;
+                                    const uint32_t bs = __shfl_sync(0xffffffffu, start, src);
+                                    const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
+                                    const uint32_t bv = __shfl_sync(0xffffffffu, vidx, src);
+                                    const uint32_t srcTeam = ((threadIdx.x & ~31u) + src) / TEAM;
+                                    const uint32_t rSrc = base + srcTeam;
+                                    // permuted voxel (u[a0], u[a1], u[a2]) of the queued hash
+                                    const int ux = bv % R, uy = (bv / R) % R, uz = bv / (R * R);
+                                    const int v0 = a0 == 0 ? ux : (a0 == 1 ? uy : uz);
+                                    const int v1 = a1 == 0 ? ux : (a1 == 1 ? uy : uz);
+                                    const int v2 = a2 == 0 ? ux : (a2 == 1 ? uy : uz);
+                                    const int an0 = d0 ? 0 : R - 1, an1 = d1 ? 0 : R - 1, an2 = d2 ? 0 : R - 1;
+                                    for (uint32_t e = lane; e < bc; e += 32) {
+                                        const uint32_t pay = __ldg(&p.entries[bs + e]);
                                         const uint32_t tgt = pay >> 3;
                                         const uint32_t S = dir ^ (pay & 7);
                                         ++cCand;
-                                        const int T0 = (S & 1) ? v0 - anchor0 : anchor0 - v0;
-                                        const int T1 = (S & 2) ? v1 - anchor1 : anchor1 - v1;
-                                        const int T2 = (S & 4) ? v2 - anchor2 : anchor2 - v2;
+                                        const int T0 = (S & 1) ? v0 - an0 : an0 - v0;
+                                        const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
+                                        const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
                                         if (!p.allowPerm && pid != 0)
                                             continue;
                                         if (!p.allowSym && S != 0)
                                             continue;
                                         if (!p.allowTrans && (T0 | T1 | T2) != 0)
                                             continue;
-                                        const uint64_t key = encodeFixed64(srcPos, pid, S, T0, T1, T2, L);
+                                        const uint64_t key = encodeFixed64(rSrc, pid, S, T0, T1, T2, L);
                                         const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
                                         if (key >= cur)
                                             continue;
                                         ++cVer;
-                                        if (!verifyCandidate<R>(p.grids + (size_t)tgt * W, lines, a0, a1, a2, S, T0, T1, T2))
+                                        const uint16_t* srcLines = reinterpret_cast<const uint16_t*>(
+                                            reinterpret_cast<const uint64_t*>(smem + (size_t)srcTeam * Sh::TEAM_BYTES) + 3 * Sh::GRID + W);
+                                        if (!verifyCandidate<R>(p.grids + (size_t)tgt * W, srcLines, a0, a1, a2, S, T0, T1, T2))
                                             continue;
                                         ++cOk;
                                         atomicMin(&p.parents[tgt], (unsigned long long)key);
                                     }
                                 }
                             }
+                            if (tl == 0)
+                                *qcount = 0;
+                            __syncthreads();
                         }
-                        __syncthreads();
                     }
                 }
             }
@@ -409,7 +518,7 @@ __global__ void __launch_bounds__(kThreads) searchKernel(SearchParams p)
         unsigned long long v = vals[k];
         for (int o = 16; o > 0; o >>= 1)
             v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0 && v)
+        if (lane == 0 && v)
             atomicAdd(&p.counters[k], v);
     }
 }
@@ -455,6 +564,54 @@ uint64_t pow2AtLeast(uint64_t v)
     return p;
 }
 
+struct Table {
+    DevBuf<ulonglong2> slots;
+    DevBuf<uint32_t> entries;
+    DevBuf<uint32_t> filter;
+    uint32_t capMask = 0, filterShift = 31;
+    uint64_t numEntries = 0;
+};
+
+// Build the corner-hash table over m entries (non-zero keys).
+void buildTable(Context& ctx, const uint64_t* ekeys, const uint32_t* epay, size_t m, Table& t)
+{
+    cudaStream_t s = ctx.stream;
+    const uint32_t loadPct = ctx.tuning.table_load_percent ? std::min(85u, std::max(25u, ctx.tuning.table_load_percent)) : 50u;
+    const uint64_t cap = pow2AtLeast(std::max<uint64_t>(64, m * 100 / loadPct + 1));
+    TDAG_CHECK(cap <= (1ull << 31), TDAG_ERR_ARG, "corner-hash table too large");
+    t.slots = DevBuf<ulonglong2>(cap, s);
+    t.capMask = (uint32_t)(cap - 1);
+    DevBuf<uint32_t> tcount(cap, s), tstart(cap, s), slotOfEntry(std::max<size_t>(m, 1), s), numDistinct(1, s);
+    TDAG_CUDA(cudaMemsetAsync(t.slots.get(), 0, cap * sizeof(ulonglong2), s));
+    TDAG_CUDA(cudaMemsetAsync(tcount.get(), 0, cap * 4, s));
+    TDAG_CUDA(cudaMemsetAsync(numDistinct.get(), 0, 4, s));
+    if (m) {
+        tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys, m, t.slots.get(), tcount.get(), slotOfEntry.get(), t.capMask, numDistinct.get(), ctx.status);
+        TDAG_LAUNCHED();
+    }
+    t.numEntries = exclusiveScanU32Total(tcount.get(), tstart.get(), cap, s);
+    uint32_t distinct = 0;
+    TDAG_CUDA(cudaMemcpyAsync(&distinct, numDistinct.get(), 4, cudaMemcpyDeviceToHost, s));
+    ctx.checkStatus("corner-hash table");
+    t.entries = DevBuf<uint32_t>(std::max<uint64_t>(t.numEntries, 1), s);
+    if (m) {
+        DevBuf<uint32_t> tfill(cap, s);
+        TDAG_CUDA(cudaMemsetAsync(tfill.get(), 0, cap * 4, s));
+        tableScatterKernel<<<gridFor(m, 256), 256, 0, s>>>(epay, slotOfEntry.get(), m, tstart.get(), tfill.get(), t.entries.get());
+        TDAG_LAUNCHED();
+    }
+    const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
+    const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, (uint64_t)distinct * bitsPerKey));
+    uint32_t log2F = 0;
+    while ((1ull << log2F) < filterBits)
+        ++log2F;
+    t.filterShift = 32 - log2F;
+    t.filter = DevBuf<uint32_t>(filterBits / 32, s);
+    TDAG_CUDA(cudaMemsetAsync(t.filter.get(), 0, filterBits / 8, s));
+    tableRangesKernel<<<gridFor(cap, 256), 256, 0, s>>>(t.slots.get(), tstart.get(), tcount.get(), (uint32_t)cap, t.filter.get(), t.filterShift);
+    TDAG_LAUNCHED();
+}
+
 template <int L>
 MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats)
 {
@@ -467,78 +624,28 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CHECK(n < (1u << 29), TDAG_ERR_ARG, "too many items for one matcher level");
 
     // popcount order
-    DevBuf<uint32_t> order(n, s), posOf(n, s);
+    DevBuf<uint32_t> order(n, s);
     {
         DevBuf<uint64_t> key(n, s);
         popcountKeyKernel<W><<<gridFor(n, 256), 256, 0, s>>>(grids, n, R * R * R, key.get(), order.get());
         TDAG_LAUNCHED();
         radixSortPairs(key.get(), order.get(), n, 0, 16, s);
-        invertOrderKernel<<<gridFor(n, 256), 256, 0, s>>>(order.get(), n, posOf.get());
-        TDAG_LAUNCHED();
     }
 
-    // corner hashes + table
+    // corner hashes: 8 per item; zero hashes (empty grids) are never entries
     const size_t m = (size_t)n * 8;
     DevBuf<uint64_t> ekeys(m, s);
     DevBuf<uint32_t> epay(m, s);
     cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, ekeys.get(), epay.get());
     TDAG_LAUNCHED();
-    const uint32_t loadPct = ctx.tuning.table_load_percent ? std::min(85u, std::max(25u, ctx.tuning.table_load_percent)) : 50u;
-    const uint64_t cap = pow2AtLeast(m * 100 / loadPct + 16);
-    DevBuf<uint64_t> tkeys(cap, s), tranges(cap, s);
-    DevBuf<uint32_t> tcount(cap, s), tstart(cap, s), slotOfEntry(m, s), numDistinct(1, s);
-    TDAG_CUDA(cudaMemsetAsync(tkeys.get(), 0, cap * 8, s));
-    TDAG_CUDA(cudaMemsetAsync(tcount.get(), 0, cap * 4, s));
-    TDAG_CUDA(cudaMemsetAsync(numDistinct.get(), 0, 4, s));
-    tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), m, tkeys.get(), tcount.get(), slotOfEntry.get(), cap - 1, numDistinct.get(), ctx.status);
-    TDAG_LAUNCHED();
-    const uint64_t numEntries = exclusiveScanU32Total(tcount.get(), tstart.get(), cap, s);
-    uint32_t distinct = 0;
-    TDAG_CUDA(cudaMemcpyAsync(&distinct, numDistinct.get(), 4, cudaMemcpyDeviceToHost, s));
-    ctx.checkStatus("corner-hash table");
-    DevBuf<uint32_t> entries(numEntries ? numEntries : 1, s);
-    {
-        DevBuf<uint32_t> tfill(cap, s);
-        TDAG_CUDA(cudaMemsetAsync(tfill.get(), 0, cap * 4, s));
-        tableScatterKernel<<<gridFor(m, 256), 256, 0, s>>>(epay.get(), slotOfEntry.get(), m, tstart.get(), tfill.get(), entries.get());
-        TDAG_LAUNCHED();
-    }
-    const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
-    const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, (uint64_t)distinct * bitsPerKey));
-    DevBuf<uint32_t> filter(filterBits / 32, s);
-    TDAG_CUDA(cudaMemsetAsync(filter.get(), 0, filterBits / 8, s));
-    tableRangesKernel<<<gridFor(cap, 256), 256, 0, s>>>(tkeys.get(), tstart.get(), tcount.get(), cap, tranges.get(), filter.get(), filterBits - 1);
-    TDAG_LAUNCHED();
-    ekeys.release();
-    epay.release();
-    slotOfEntry.release();
-    tcount.release();
-    tstart.release();
 
-    // search
     const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, L);
     DevBuf<unsigned long long> parents(n, s);
     fillU64(reinterpret_cast<uint64_t*>(parents.get()), sentinelKey, n, s);
     DevBuf<uint32_t> work(1, s);
     DevBuf<unsigned long long> counters(8, s);
-    TDAG_CUDA(cudaMemsetAsync(work.get(), 0, 4, s));
     TDAG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, s));
-    SearchParams sp;
-    sp.grids = grids;
-    sp.order = order.get();
-    sp.n = n;
-    sp.tkeys = tkeys.get();
-    sp.tranges = tranges.get();
-    sp.capMask = cap - 1;
-    sp.entries = entries.get();
-    sp.filter = filter.get();
-    sp.filterMask = filterBits - 1;
-    sp.parents = parents.get();
-    sp.workCounter = work.get();
-    sp.counters = counters.get();
-    sp.allowSym = cfg.symmetry ? 1 : 0;
-    sp.allowPerm = cfg.axis_permutation ? 1 : 0;
-    sp.allowTrans = cfg.translation ? 1 : 0;
+
     const size_t smem = SearchShape<R>::SMEM;
     TDAG_CUDA(cudaFuncSetAttribute(searchKernel<R, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int perSM = 0;
@@ -546,12 +653,70 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     if (ctx.tuning.search_ctas_per_sm)
         perSM = std::min<int>(perSM, (int)ctx.tuning.search_ctas_per_sm);
     perSM = std::max(perSM, 1);
-    const uint64_t groups = (n + SearchShape<R>::TEAMS - 1) / SearchShape<R>::TEAMS;
-    const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx.numSMs * perSM, groups));
-    TDAG_CUDA(cudaEventRecord(ctx.ev[0], s));
-    searchKernel<R, L><<<blocks, kThreads, smem, s>>>(sp);
-    TDAG_LAUNCHED();
-    TDAG_CUDA(cudaEventRecord(ctx.ev[1], s));
+    const uint32_t maxBlocks = (uint32_t)ctx.numSMs * perSM;
+
+    // batch boundaries over sorted source positions: doubling, starting at a few waves of teams
+    std::vector<uint32_t> bounds { 0 };
+    const uint32_t minBatch = std::max<uint32_t>(maxBlocks * SearchShape<R>::TEAMS * 2, n / 256);
+    while (bounds.back() < n) {
+        const uint32_t b = bounds.back();
+        bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 2ull * b)));
+    }
+
+    Table table;
+    buildTable(ctx, ekeys.get(), epay.get(), m, table);
+    uint64_t entriesInitial = table.numEntries;
+    float searchMs = 0;
+    DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
+    DevBuf<uint64_t> k2(m, s);
+    DevBuf<uint32_t> p2(m, s);
+    for (size_t bi = 0; bi + 1 < bounds.size(); ++bi) {
+        const uint32_t b0 = bounds[bi], b1 = bounds[bi + 1];
+        if (bi > 0) {
+            // drop targets whose parent no source at or after b0 can lower
+            const unsigned long long minKeyNext = encodeFixed64(b0, 0, 0, 1 - R, 1 - R, 1 - R, L);
+            liveEntriesKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), epay.get(), m, parents.get(), minKeyNext, flags.get());
+            TDAG_LAUNCHED();
+            const uint32_t live = compactFlags(flags.get(), liveIdx.get(), m, s);
+            if (live == 0)
+                break;
+            gatherEntriesKernel<<<gridFor(live, 256), 256, 0, s>>>(liveIdx.get(), live, ekeys.get(), epay.get(), k2.get(), p2.get());
+            TDAG_LAUNCHED();
+            buildTable(ctx, k2.get(), p2.get(), live, table);
+        }
+        SearchParams sp;
+        sp.grids = grids;
+        sp.order = order.get();
+        sp.begin = b0;
+        sp.end = b1;
+        sp.slots = table.slots.get();
+        sp.capMask = table.capMask;
+        sp.entries = table.entries.get();
+        sp.filter = table.filter.get();
+        sp.filterShift = table.filterShift;
+        sp.parents = parents.get();
+        sp.workCounter = work.get();
+        sp.counters = counters.get();
+        sp.allowSym = cfg.symmetry ? 1 : 0;
+        sp.allowPerm = cfg.axis_permutation ? 1 : 0;
+        sp.allowTrans = cfg.translation ? 1 : 0;
+        TDAG_CUDA(cudaMemsetAsync(work.get(), 0, 4, s));
+        const uint64_t groups = ((uint64_t)(b1 - b0) + SearchShape<R>::TEAMS - 1) / SearchShape<R>::TEAMS;
+        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
+        TDAG_CUDA(cudaEventRecord(ctx.ev[0], s));
+        searchKernel<R, L><<<blocks, kThreads, smem, s>>>(sp);
+        TDAG_LAUNCHED();
+        TDAG_CUDA(cudaEventRecord(ctx.ev[1], s));
+        TDAG_CUDA(cudaEventSynchronize(ctx.ev[1]));
+        float ms = 0;
+        TDAG_CUDA(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]));
+        searchMs += ms;
+    }
+    table = Table();
+    flags.release();
+    liveIdx.release();
+    k2.release();
+    p2.release();
 
     // resolve
     DevBuf<uint64_t> parentTP(n, s);
@@ -570,8 +735,6 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         unsigned long long c[8];
         TDAG_CUDA(cudaMemcpyAsync(c, counters.get(), 64, cudaMemcpyDeviceToHost, s));
         TDAG_CUDA(cudaStreamSynchronize(s));
-        float ms = 0;
-        TDAG_CUDA(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]));
         stats->items = n;
         stats->unique = out.numUnique;
         stats->probes = c[0];
@@ -580,8 +743,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         stats->candidates = c[3];
         stats->verifications = c[4];
         stats->verified = c[5];
-        stats->table_entries = numEntries;
-        stats->search_ms = ms;
+        stats->table_entries = entriesInitial;
+        stats->search_ms = searchMs;
     }
     ctx.checkStatus("matcher level " + std::to_string(L));
     return out;
