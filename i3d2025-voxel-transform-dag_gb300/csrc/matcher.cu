@@ -27,6 +27,8 @@
 //   shared memory, looked up in the table (16-byte slots: key + range) and each hit's candidate range
 //   is spread across the warp.
 #include <algorithm>
+#include <functional>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -752,6 +754,239 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
 
 } // namespace
 
+// ================================================================================================
+// Matcher entry point that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: code that runs inside a host application which owns every
+// byte of device memory (a game engine's or renderer's fixed arena, a per-frame budget) or a
+// memory-capped service where an allocation could fail or stall at an arbitrary point. For them,
+// tdag_find_duplicates_level_noalloc runs one matcher level with all of its scratch (popcount
+// order, corner-hash table and entries, membership filter, parents, resolve arrays) in one
+// file-scope __device__ array of kNoAllocScratchBytes. The caller passes device pointers for the
+// grids and the outputs; the function calls no cudaMalloc, cudaFree or allocating routine.
+//
+// Limits: at most kNoAllocMaxItems items per call (levels 2..4). The array is part of the module:
+// every GPU that loads libtdag.so holds it until the process exits. All calls share it, so calls
+// that overlap on the GPU (two contexts, or two threads on one context) race and must be
+// serialised by the caller. The first call on a device looks up the array's device address with
+// cudaGetSymbolAddress (once per device, with that device current); make that first call before
+// any stream capture.
+// ================================================================================================
+namespace {
+
+constexpr uint32_t kNoAllocMaxItems = 4096;
+constexpr size_t kNoAllocScratchBytes = 4u << 20;
+static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocScratchBytes];
+
+// Stable rank by popcount (descending) for n <= kNoAllocMaxItems: O(n^2) comparisons, no sort temp.
+template <int W>
+__global__ void noAllocRankKernel(const uint64_t* __restrict__ grids, uint32_t n, uint32_t* __restrict__ pc, uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t cnt[kNoAllocMaxItems];
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        uint32_t c = 0;
+        for (int k = 0; k < W; ++k)
+            c += __popcll(grids[(size_t)i * W + k]);
+        cnt[i] = c;
+        pc[i] = c;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        uint32_t rank = 0;
+        const uint32_t ci = cnt[i];
+        for (uint32_t j = 0; j < n; ++j)
+            rank += (cnt[j] > ci) || (cnt[j] == ci && j < i);
+        order[rank] = i;
+    }
+}
+
+// Single-block exclusive scan (in < 2^32 total); writes the total to *total.
+__global__ void noAllocScanKernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n, uint32_t* __restrict__ total)
+{
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0)
+        carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t base = 0; base < n; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < n ? in[i] : 0;
+        uint32_t incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o)
+                incl += t;
+        }
+        if (lane == 31)
+            warpSums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < nw ? warpSums[lane] : 0;
+            uint32_t wi = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+                if ((int)lane >= o)
+                    wi += t;
+            }
+            if (lane < nw)
+                warpSums[lane] = wi - w;
+        }
+        __syncthreads();
+        const uint32_t c = carry;
+        if (i < n)
+            out[i] = c + warpSums[warp] + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1)
+            carry = c + warpSums[warp] + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        *total = carry;
+}
+
+// Kept items -> compacted positions (the scan gives their new indices).
+__global__ void noAllocUniquesKernel(const uint32_t* __restrict__ isUnique, const uint32_t* __restrict__ newIdx, uint32_t n, uint32_t* __restrict__ outUnique)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && isUnique[i])
+        outUnique[newIdx[i]] = i;
+}
+
+struct NoAllocLayout {
+    uint32_t *pc, *order, *epay, *slotOfEntry, *tcount, *tstart, *tfill, *entries, *filter, *isUnique, *newIdx, *misc;
+    uint64_t *ekeys, *parentTP;
+    unsigned long long *parents, *counters;
+    ulonglong2* slots;
+    uint32_t capMask, filterShift;
+    size_t bytes;
+};
+
+// Carve the scratch array; cap and filter sized for n items.
+NoAllocLayout noAllocCarve(unsigned char* base, uint32_t n)
+{
+    NoAllocLayout L {};
+    const uint64_t m = (uint64_t)n * 8;
+    const uint64_t cap = pow2AtLeast(std::max<uint64_t>(64, m * 2));
+    const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, m * 32));
+    uint32_t log2F = 0;
+    while ((1ull << log2F) < filterBits)
+        ++log2F;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char* p = base + off;
+        off += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    L.slots = reinterpret_cast<ulonglong2*>(take(cap * 16));
+    L.ekeys = reinterpret_cast<uint64_t*>(take(m * 8));
+    L.parents = reinterpret_cast<unsigned long long*>(take((size_t)n * 8));
+    L.parentTP = reinterpret_cast<uint64_t*>(take((size_t)n * 8));
+    L.counters = reinterpret_cast<unsigned long long*>(take(64));
+    L.pc = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+    L.order = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+    L.epay = reinterpret_cast<uint32_t*>(take(m * 4));
+    L.slotOfEntry = reinterpret_cast<uint32_t*>(take(m * 4));
+    L.tcount = reinterpret_cast<uint32_t*>(take(cap * 4));
+    L.tstart = reinterpret_cast<uint32_t*>(take(cap * 4));
+    L.tfill = reinterpret_cast<uint32_t*>(take(cap * 4));
+    L.entries = reinterpret_cast<uint32_t*>(take(m * 4));
+    L.filter = reinterpret_cast<uint32_t*>(take(filterBits / 8));
+    L.isUnique = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+    L.newIdx = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+    L.misc = reinterpret_cast<uint32_t*>(take(64)); // [0] work counter, [1] distinct keys, [2] entries, [3] kept
+    L.capMask = (uint32_t)(cap - 1);
+    L.filterShift = 32 - log2F;
+    L.bytes = off;
+    return L;
+}
+
+template <int LV>
+void runMatcherNoAlloc(Context& ctx, unsigned char* scratch, const uint64_t* grids, uint32_t n, const tdag_config& cfg, uint64_t* outMapping,
+    uint32_t* outUnique, uint32_t* outCount)
+{
+    constexpr int R = 1 << LV;
+    constexpr int W = R * R * R / 64;
+    cudaStream_t s = ctx.stream;
+    NoAllocLayout A = noAllocCarve(scratch, n);
+    TDAG_CHECK(A.bytes <= kNoAllocScratchBytes, TDAG_ERR_ARG, "no-alloc scratch too small for this level and item count");
+    const uint64_t m = (uint64_t)n * 8;
+    const uint64_t cap = (uint64_t)A.capMask + 1;
+    // everything that must start at zero (the array keeps the previous call's contents)
+    TDAG_CUDA(cudaMemsetAsync(A.slots, 0, cap * 16, s));
+    TDAG_CUDA(cudaMemsetAsync(A.tcount, 0, cap * 4, s));
+    TDAG_CUDA(cudaMemsetAsync(A.tfill, 0, cap * 4, s));
+    TDAG_CUDA(cudaMemsetAsync(A.filter, 0, (size_t)1 << (32 - A.filterShift) >> 3, s));
+    TDAG_CUDA(cudaMemsetAsync(A.isUnique, 0, (size_t)n * 4, s));
+    TDAG_CUDA(cudaMemsetAsync(A.counters, 0, 64, s));
+    TDAG_CUDA(cudaMemsetAsync(A.misc, 0, 64, s));
+
+    noAllocRankKernel<W><<<1, 1024, 0, s>>>(grids, n, A.pc, A.order);
+    TDAG_LAUNCHED();
+    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, A.ekeys, A.epay);
+    TDAG_LAUNCHED();
+    tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(A.ekeys, m, A.slots, A.tcount, A.slotOfEntry, A.capMask, A.misc + 1, ctx.status);
+    TDAG_LAUNCHED();
+    noAllocScanKernel<<<1, 1024, 0, s>>>(A.tcount, A.tstart, (uint32_t)cap, A.misc + 2);
+    TDAG_LAUNCHED();
+    tableScatterKernel<<<gridFor(m, 256), 256, 0, s>>>(A.epay, A.slotOfEntry, m, A.tstart, A.tfill, A.entries);
+    TDAG_LAUNCHED();
+    tableRangesKernel<<<gridFor(cap, 256), 256, 0, s>>>(A.slots, A.tstart, A.tcount, (uint32_t)cap, A.filter, A.filterShift);
+    TDAG_LAUNCHED();
+    const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, LV);
+    fillU64(reinterpret_cast<uint64_t*>(A.parents), sentinelKey, n, s);
+
+    SearchParams sp;
+    sp.grids = grids;
+    sp.order = A.order;
+    sp.begin = 0;
+    sp.end = n;
+    sp.slots = A.slots;
+    sp.capMask = A.capMask;
+    sp.entries = A.entries;
+    sp.filter = A.filter;
+    sp.filterShift = A.filterShift;
+    sp.parents = A.parents;
+    sp.workCounter = A.misc;
+    sp.counters = A.counters;
+    sp.allowSym = cfg.symmetry ? 1 : 0;
+    sp.allowPerm = cfg.axis_permutation ? 1 : 0;
+    sp.allowTrans = cfg.translation ? 1 : 0;
+    const size_t smem = SearchShape<R>::SMEM;
+    TDAG_CUDA(cudaFuncSetAttribute(searchKernel<R, LV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)ctx.numSMs * 2, (n + SearchShape<R>::TEAMS - 1) / SearchShape<R>::TEAMS));
+    searchKernel<R, LV><<<blocks, kThreads, smem, s>>>(sp);
+    TDAG_LAUNCHED();
+
+    decodeParentsKernel<<<gridFor(n, 256), 256, 0, s>>>(A.parents, n, A.order, sentinelKey, LV, A.parentTP, A.isUnique);
+    TDAG_LAUNCHED();
+    noAllocScanKernel<<<1, 1024, 0, s>>>(A.isUnique, A.newIdx, n, outCount);
+    TDAG_LAUNCHED();
+    noAllocUniquesKernel<<<gridFor(n, 256), 256, 0, s>>>(A.isUnique, A.newIdx, n, outUnique);
+    TDAG_LAUNCHED();
+    finalMappingKernel<<<gridFor(n, 256), 256, 0, s>>>(A.parentTP, A.isUnique, A.newIdx, n, outMapping);
+    TDAG_LAUNCHED();
+    ctx.checkStatus("no-alloc matcher level " + std::to_string(LV));
+}
+
+std::mutex g_noAllocMutex;
+unsigned char* g_noAllocAddr[64] = {};
+
+// Device address of the scratch array for the current device (looked up once per device).
+unsigned char* noAllocScratchAddress(int device)
+{
+    TDAG_CHECK(device >= 0 && device < 64, TDAG_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noAllocMutex);
+    if (!g_noAllocAddr[device]) {
+        void* p = nullptr;
+        TDAG_CUDA(cudaGetSymbolAddress(&p, g_noAllocScratch));
+        g_noAllocAddr[device] = static_cast<unsigned char*>(p);
+    }
+    return g_noAllocAddr[device];
+}
+
+} // namespace
+
 MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats)
 {
     switch (level) {
@@ -767,3 +1002,37 @@ MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint
 }
 
 } // namespace tdag
+
+// ================================================================================================
+// C ABI of the no-allocation matcher entry point
+// ================================================================================================
+struct tdag_ctx;
+tdag::Context& ctxOf(tdag_ctx* c); // build.cu
+int guardedCall(const std::function<void()>& f); // build.cu
+int failWith(int code, const char* msg); // build.cu
+
+extern "C" int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n, const tdag_config* cfg,
+    uint64_t* d_out_mapping, uint32_t* d_out_unique, uint32_t* d_n_unique)
+{
+    using namespace tdag;
+    if (!ctx || !cfg || !d_n_unique || (n && (!d_grids || !d_out_mapping || !d_out_unique)))
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        TDAG_CHECK(level >= 2 && level <= 4, TDAG_ERR_ARG, "level must be 2..4");
+        TDAG_CHECK(n <= kNoAllocMaxItems, TDAG_ERR_ARG, "tdag_find_duplicates_level_noalloc accepts at most 4096 items per call");
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        if (n == 0) {
+            TDAG_CUDA(cudaMemsetAsync(d_n_unique, 0, 4, c.stream));
+            TDAG_CUDA(cudaStreamSynchronize(c.stream));
+            return;
+        }
+        unsigned char* scratch = noAllocScratchAddress(c.device);
+        if (level == 2)
+            runMatcherNoAlloc<2>(c, scratch, d_grids, n, *cfg, d_out_mapping, d_out_unique, d_n_unique);
+        else if (level == 3)
+            runMatcherNoAlloc<3>(c, scratch, d_grids, n, *cfg, d_out_mapping, d_out_unique, d_n_unique);
+        else
+            runMatcherNoAlloc<4>(c, scratch, d_grids, n, *cfg, d_out_mapping, d_out_unique, d_n_unique);
+    });
+}

@@ -84,7 +84,7 @@ EXPORTED = (
     "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
     "tdag_build", "tdag_build_device", "tdag_result_free", "tdag_find_duplicates_level", "tdag_build_hierarchical",
     "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
-    "tdag_svdag_copy_level", "tdag_svdag_free",
+    "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
 )
 
 _lib = None
@@ -123,6 +123,8 @@ def lib(path: str = None):
         L.tdag_svdag_voxel_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
         L.tdag_svdag_copy_level.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64]
         L.tdag_svdag_free.argtypes = [vp]
+        L.tdag_find_duplicates_level_noalloc.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.POINTER(Config),
+                                                         vp, vp, vp]
         _lib = L
     return _lib
 

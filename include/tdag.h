@@ -136,6 +136,18 @@ int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* gr
     const tdag_config* config, uint64_t* out_mapping, uint32_t* out_unique, uint32_t* n_unique,
     tdag_level_stats* stats);
 
+/* No counterpart in the reference: tdag_find_duplicates_level for callers that cannot allocate
+ * device memory (code inside a host application that owns all device memory, such as an engine's
+ * fixed arena, or a memory-capped service where an allocation could fail or stall). Same result as
+ * tdag_find_duplicates_level, but grids and outputs are DEVICE pointers and every temporary lives in
+ * one 4 MiB array compiled into libtdag.so; the call makes no cudaMalloc/cudaFree. At most 4096
+ * items per call (levels 2..4; larger calls return TDAG_ERR_ARG). The array is shared by all calls
+ * on all contexts of a device: calls that overlap on the GPU race and must be serialised by the
+ * caller. The first call on a device looks up the array's address (once per device); make it before
+ * any stream capture. *d_n_unique is written on the device. */
+int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n,
+    const tdag_config* config, uint64_t* d_out_mapping, uint32_t* d_out_unique, uint32_t* d_n_unique);
+
 /* constructTransformDAGHierarchical(inDag, config) (transform_dag.h:168-169;
  * tools/lib/src/voxel/transform_dag_hierarchical.cpp:304-529): symmetry + permutation only.
  * Host in, host out. */
