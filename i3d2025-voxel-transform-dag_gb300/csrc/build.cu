@@ -195,10 +195,27 @@ __global__ void validateChildrenKernel(const uint32_t* __restrict__ nodes, uint6
         setDeviceError(status, TDAG_ERR_CORRUPT, level);
 }
 
+__global__ void gatherU32Kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n, uint32_t* __restrict__ dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        dst[i] = src[idx[i]];
+}
+
 struct DeviceResult {
     std::vector<DevBuf<uint64_t>> levels;
     DevBuf<uint64_t> leaves;
+    std::vector<std::vector<uint64_t>> off; // per level (2 = leaves): first output item of each grid
 };
+
+static DevBuf<uint32_t> uploadU32(const std::vector<uint64_t>& v, cudaStream_t s)
+{
+    std::vector<uint32_t> h(v.begin(), v.end());
+    DevBuf<uint32_t> d(h.size(), s);
+    TDAG_CUDA(cudaMemcpyAsync(d.get(), h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    return d;
+}
 
 template <int L>
 static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& out, const tdag_config& cfg, tdag_stats* stats)
@@ -229,9 +246,25 @@ static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& 
         flattenKernel<L><<<gridFor((size_t)m * W, 256), 256, 0, s>>>(lp, indices.get(), m, grids.get(), ctx.status);
         TDAG_LAUNCHED();
     }
+    // batch: grid of every matched item (items stay grid-contiguous: indices are ascending)
+    Segments sg;
+    DevBuf<uint32_t> gridOfM, offM;
+    if (in.numGrids > 1) {
+        sg.numGrids = in.numGrids;
+        gridOfM = DevBuf<uint32_t>(m, s);
+        if (m) {
+            gatherU32Kernel<<<gridFor(m, 256), 256, 0, s>>>(in.gridOf[L], indices.get(), m, gridOfM.get());
+            TDAG_LAUNCHED();
+        }
+        sg.off = countPerGrid(in.gridOf[L], indices.get(), m, in.numGrids, s);
+        offM = uploadU32(sg.off, s);
+        sg.gridOf = gridOfM.get();
+        sg.offDev = offM.get();
+    }
     tdag_level_stats* ls = stats ? &stats->translation[L] : nullptr;
-    MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls);
+    MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls, &sg);
     grids.release();
+    out.off[L] = mo.uniqueOff.empty() ? std::vector<uint64_t>(in.numGrids + 1, 0) : mo.uniqueOff;
     const uint32_t u = mo.numUnique;
     if (L == 2) {
         out.leaves = DevBuf<uint64_t>(u, s);
@@ -272,7 +305,7 @@ static void validateInput(Context& ctx, const DeviceSvdag& in)
 static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, tdag_stats* stats)
 {
     TDAG_CHECK(in.rootLevel >= 2 && in.rootLevel < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "root_level out of range");
-    TDAG_CHECK(in.resolution == (1u << in.rootLevel), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
+    TDAG_CHECK(in.numGrids > 1 || in.resolution == (1u << in.rootLevel), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
     if (cfg.translation) {
         TDAG_CHECK(cfg.max_translation_level >= 2 && cfg.max_translation_level <= 4, TDAG_ERR_ARG, "max_translation_level must be 2..4 when translation is on");
         TDAG_CHECK(in.rootLevel >= cfg.max_translation_level + 1, TDAG_ERR_ARG, "root_level must exceed max_translation_level");
@@ -289,6 +322,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
     TDAG_CUDA(cudaEventRecord(ctx.ev[3], s));
     DeviceResult out;
     out.levels.resize(in.rootLevel + 1);
+    out.off = h.handleOff;
     for (uint32_t l = 3; l <= in.rootLevel; ++l)
         out.levels[l] = std::move(h.levels[l]);
     out.leaves = std::move(h.leaves);
@@ -321,6 +355,77 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
         stats->kernel_launches = g_kernelLaunches.load() - launches0;
     }
     return out;
+}
+
+// Child indices of a concatenated level: add the grid's first index at the level below.
+__global__ void offsetChildrenKernel(uint32_t* __restrict__ nodes, uint64_t count8, const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ childOff)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count8)
+        return;
+    const uint32_t c = nodes[i];
+    if (c != kEmpty32)
+        nodes[i] = c + childOff[gridOf[i >> 3]];
+}
+
+// Device storage of a batch of SVDAGs concatenated level by level.
+struct BatchInput {
+    std::vector<DevBuf<uint32_t>> nodes, gridOf, offDev;
+    DevBuf<uint64_t> leaves;
+    DeviceSvdag view;
+};
+
+static void concatBatch(Context& ctx, const tdag_svdag_view* v, uint32_t count, bool hostInput, BatchInput& b)
+{
+    cudaStream_t s = ctx.stream;
+    const cudaMemcpyKind kind = hostInput ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    uint32_t maxRoot = 0;
+    for (uint32_t g = 0; g < count; ++g)
+        maxRoot = std::max(maxRoot, v[g].root_level);
+    DeviceSvdag& d = b.view;
+    d.numGrids = count;
+    d.rootLevel = maxRoot;
+    d.resolution = 1u << maxRoot;
+    b.nodes.resize(maxRoot + 1);
+    b.gridOf.resize(maxRoot + 1);
+    b.offDev.resize(maxRoot + 1);
+    // offsets
+    for (uint32_t l = 2; l <= maxRoot; ++l) {
+        auto& off = d.segOff[l];
+        off.assign(count + 1, 0);
+        for (uint32_t g = 0; g < count; ++g) {
+            const uint64_t c = (l == 2) ? v[g].leaf_count : (l <= v[g].root_level ? v[g].node_counts[l] : 0);
+            off[g + 1] = off[g] + c;
+        }
+        TDAG_CHECK(off[count] < (1ull << 31), TDAG_ERR_ARG, "batch level too large");
+        b.offDev[l] = uploadU32(off, s);
+        b.gridOf[l] = DevBuf<uint32_t>(off[count], s);
+        segmentIds(b.offDev[l].get(), count, off[count], b.gridOf[l].get(), s);
+        d.gridOf[l] = b.gridOf[l].get();
+    }
+    // leaves
+    b.leaves = DevBuf<uint64_t>(d.segOff[2][count], s);
+    for (uint32_t g = 0; g < count; ++g)
+        if (v[g].leaf_count)
+            TDAG_CUDA(cudaMemcpyAsync(b.leaves.get() + d.segOff[2][g], v[g].leaves, v[g].leaf_count * 8, kind, s));
+    d.leaves = b.leaves.get();
+    d.leafCount = d.segOff[2][count];
+    // nodes, children rebased onto the concatenated level below
+    for (uint32_t l = 3; l <= maxRoot; ++l) {
+        const uint64_t total = d.segOff[l][count];
+        b.nodes[l] = DevBuf<uint32_t>(total * 8, s);
+        for (uint32_t g = 0; g < count; ++g) {
+            const uint64_t c = d.segOff[l][g + 1] - d.segOff[l][g];
+            if (c)
+                TDAG_CUDA(cudaMemcpyAsync(b.nodes[l].get() + d.segOff[l][g] * 8, v[g].nodes[l], c * 32, kind, s));
+        }
+        if (total) {
+            offsetChildrenKernel<<<gridFor(total * 8, 256), 256, 0, s>>>(b.nodes[l].get(), total * 8, b.gridOf[l].get(), b.offDev[l - 1].get());
+            TDAG_LAUNCHED();
+        }
+        d.nodes[l] = b.nodes[l].get();
+        d.nodeCounts[l] = total;
+    }
 }
 
 } // namespace
@@ -556,6 +661,75 @@ int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg,
         TDAG_CUDA(cudaStreamSynchronize(s));
         *out = r.release();
     });
+}
+
+static int buildBatched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count, const tdag_config* cfg, tdag_result** out, tdag_stats* batchStats, bool host)
+{
+    if (!ctx || !cfg || !out || (count && !in))
+        return fail(TDAG_ERR_ARG, "null argument");
+    for (uint32_t g = 0; g < count; ++g)
+        out[g] = nullptr;
+    return guarded([&] {
+        for (uint32_t g = 0; g < count; ++g) {
+            checkView(&in[g]);
+            TDAG_CHECK(in[g].resolution == (1u << in[g].root_level), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
+            if (cfg->translation)
+                TDAG_CHECK(in[g].root_level >= cfg->max_translation_level + 1, TDAG_ERR_ARG, "root_level must exceed max_translation_level");
+        }
+        if (count == 0)
+            return;
+        Context& c = ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        BatchInput b;
+        concatBatch(c, in, count, host, b);
+        tdag_stats st;
+        std::memset(&st, 0, sizeof(st));
+        DeviceResult dr = buildDevice(c, b.view, *cfg, &st);
+        std::vector<std::unique_ptr<tdag_result>> res(count);
+        for (uint32_t g = 0; g < count; ++g) {
+            res[g].reset(newResult(in[g].resolution, in[g].root_level, !host));
+            res[g]->stats = st;
+            for (uint32_t l = 2; l <= in[g].root_level; ++l) {
+                const auto& off = dr.off[l];
+                const uint64_t first = off.empty() ? 0 : off[g], cnt = off.empty() ? 0 : off[g + 1] - off[g];
+                const uint64_t words = (l == 2) ? 1 : 8;
+                const uint64_t* src = (l == 2) ? dr.leaves.get() : dr.levels[l].get();
+                uint64_t* dst = nullptr;
+                const size_t bytes = cnt * words * 8;
+                if (host) {
+                    dst = (uint64_t*)std::malloc(bytes ? bytes : 1);
+                    TDAG_CHECK(dst != nullptr, TDAG_ERR_OOM, "host allocation failed");
+                } else {
+                    TDAG_CUDA(cudaMalloc(&dst, bytes ? bytes : 8));
+                }
+                if (l == 2) {
+                    res[g]->leaves = dst;
+                    res[g]->leaf_count = cnt;
+                } else {
+                    res[g]->nodes[l] = dst;
+                    res[g]->node_counts[l] = cnt;
+                }
+                if (bytes)
+                    TDAG_CUDA(cudaMemcpyAsync(dst, src + first * words, bytes, host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+            }
+        }
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        for (uint32_t g = 0; g < count; ++g)
+            out[g] = res[g].release();
+        if (batchStats)
+            *batchStats = st;
+    });
+}
+
+int tdag_build_batched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count, const tdag_config* cfg, tdag_result** out, tdag_stats* batchStats)
+{
+    return buildBatched(ctx, in, count, cfg, out, batchStats, true);
+}
+
+int tdag_build_batched_device(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count, const tdag_config* cfg, tdag_result** out, tdag_stats* batchStats)
+{
+    return buildBatched(ctx, in, count, cfg, out, batchStats, false);
 }
 
 int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)

@@ -79,7 +79,7 @@ __device__ __forceinline__ uint64_t sortedPtrHash(uint64_t p[8])
 
 // ---------------------------------------------------------------------------- leaves (level 2)
 __global__ void __launch_bounds__(kThreads) leafSigKernel(const uint64_t* __restrict__ leaves, uint32_t n, const TransformTables* __restrict__ tables,
-    const uint8_t* __restrict__ canonByte, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key)
+    const uint8_t* __restrict__ canonByte, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key, const uint32_t* __restrict__ gridOf)
 {
     __shared__ uint8_t byteMap[48][256];
     __shared__ uint8_t pos[48][8];
@@ -102,7 +102,12 @@ __global__ void __launch_bounds__(kThreads) leafSigKernel(const uint64_t* __rest
         const uint64_t v = transformLeaf(m, t, byteMap, pos);
         best = v < best ? v : best;
     }
-    sig[i] = best;
+    if (gridOf) { // batched build: the grid id is part of the class key
+        sig[2 * (size_t)i] = best;
+        sig[2 * (size_t)i + 1] = gridOf[i];
+    } else {
+        sig[i] = best;
+    }
     uint64_t p[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k)
@@ -210,7 +215,8 @@ __device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8]
 }
 
 __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
-    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key)
+    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key,
+    const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff)
 {
     __shared__ SmemTables st;
     loadTables(st, tables);
@@ -221,10 +227,12 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
     const uint32_t* node = nodes + (size_t)i * 8;
     Child ch[8];
     uint64_t p[8];
+    // the grouping key hashes the grid's own handles (a batch numbers handles across grids)
+    const uint32_t hbase = gridOf ? prevHandleOff[gridOf[i]] : 0u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         ch[k] = loadChild(node, k, prevMap, prevInv);
-        p[k] = ch[k].h;
+        p[k] = ch[k].h == kEmpty32 ? (uint64_t)kEmpty32 : (uint64_t)(ch[k].h - hbase);
     }
     key[i] = sortedPtrHash(p);
     uint64_t best[8], cur[8];
@@ -239,10 +247,12 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
                 best[k] = cur[k];
         }
     }
-    uint64_t* out = sig + (size_t)i * 8;
+    uint64_t* out = sig + (size_t)i * (gridOf ? 9 : 8);
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         out[k] = best[k];
+    if (gridOf) // batched build: the grid id is part of the class key
+        out[8] = gridOf[i];
 }
 
 __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
@@ -349,15 +359,32 @@ __global__ void emitLeavesKernel(const uint32_t* __restrict__ emitOrder, uint32_
         out[h] = leaves[emitOrder[h]];
 }
 
+// Children are mapping pointers of the level below; in a batch their handles are made local to the
+// node's grid (prevHandleOff = first handle of each grid at the level below).
 __global__ void emitNodesKernel(const uint32_t* __restrict__ emitOrder, uint32_t u, const uint32_t* __restrict__ nodes, const uint64_t* __restrict__ prevMap,
-    uint64_t* __restrict__ out)
+    uint64_t* __restrict__ out, const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff)
 {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (uint64_t)u * 8)
         return;
     const uint32_t h = (uint32_t)(gid >> 3), k = (uint32_t)(gid & 7);
-    const uint32_t c = nodes[(size_t)emitOrder[h] * 8 + k];
-    out[gid] = (c == kEmpty32) ? tpSentinel() : prevMap[c];
+    const uint32_t node = emitOrder[h];
+    const uint32_t c = nodes[(size_t)node * 8 + k];
+    if (c == kEmpty32) {
+        out[gid] = tpSentinel();
+        return;
+    }
+    uint64_t tp = prevMap[c];
+    if (gridOf)
+        tp = tpWithPtr(tp, tpPtr(tp) - prevHandleOff[gridOf[node]]);
+    out[gid] = tp;
+}
+
+__global__ void gatherGridKeysKernel(const uint32_t* __restrict__ emitOrder, uint32_t u, const uint32_t* __restrict__ gridOf, uint64_t* __restrict__ gk)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < u)
+        gk[h] = gridOf[emitOrder[h]];
 }
 
 __global__ void fillU64Kernel(uint64_t* p, uint64_t v, size_t n)
@@ -402,7 +429,8 @@ void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s)
 // sigWords = 1 (leaves) or 8 (nodes). Produces mapping (n), inv per handle (u) and the emit order.
 static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, const uint64_t* sig, int sigWords, const uint64_t* key,
     const std::function<void(const uint32_t*, const uint32_t*, uint32_t*, uint8_t*, uint64_t*, uint32_t*)>& resolve, DevBuf<uint64_t>& mapOut,
-    DevBuf<uint64_t>& invOut, DevBuf<uint32_t>& emitOrder, DevBuf<uint32_t>* midInv)
+    DevBuf<uint64_t>& invOut, DevBuf<uint32_t>& emitOrder, DevBuf<uint32_t>* midInv, const uint32_t* gridOf, uint32_t numGrids,
+    std::vector<uint64_t>& handleOff)
 {
     cudaStream_t s = ctx.stream;
     const uint64_t cap = pow2AtLeast((uint64_t)n * 2 + 16);
@@ -412,8 +440,12 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
     if (sigWords == 1)
         classInsertKernel<1><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    else
+    else if (sigWords == 2)
+        classInsertKernel<2><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    else if (sigWords == 8)
         classInsertKernel<8><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+    else
+        classInsertKernel<9><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
     TDAG_LAUNCHED();
     slots.release();
 
@@ -434,6 +466,18 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     TDAG_LAUNCHED();
     canonList.release();
     radixSortPairs(sk.get(), emitOrder.get(), u, 0, 64, s);
+    if (gridOf && numGrids > 1) {
+        // batched build: grid-major emission order, (grid, key, index), by a stable pass on the grid id
+        gatherGridKeysKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, gridOf, sk.get());
+        TDAG_LAUNCHED();
+        uint32_t bits = 8;
+        while ((1ull << bits) < numGrids)
+            bits += 8;
+        radixSortPairs(sk.get(), emitOrder.get(), u, 0, bits, s);
+        handleOff = countPerGrid(gridOf, emitOrder.get(), u, numGrids, s);
+    } else {
+        handleOff = { 0, u };
+    }
     sk.release();
 
     DevBuf<uint32_t> handleOf(n, s);
@@ -471,12 +515,21 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
 
     HierOutput out;
     out.levels.resize(in.rootLevel + 1);
+    out.handleOff.resize(in.rootLevel + 1);
     DevBuf<uint64_t> prevMap, prevInv;
+    DevBuf<uint32_t> prevHandleOffDev;
+    auto uploadOffsets = [&](const std::vector<uint64_t>& off) {
+        DevBuf<uint32_t> d(off.size(), s);
+        std::vector<uint32_t> o32(off.begin(), off.end());
+        TDAG_CUDA(cudaMemcpyAsync(d.get(), o32.data(), o32.size() * 4, cudaMemcpyHostToDevice, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        return d;
+    };
     {
         const uint32_t n = (uint32_t)in.leafCount;
-        DevBuf<uint64_t> sig(n, s), key(n, s);
+        DevBuf<uint64_t> sig((size_t)n * (in.gridOf[2] ? 2 : 1), s), key(n, s);
         if (n) {
-            leafSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(in.leaves, n, ctx.tables, dCanonByte.get(), allowed, sig.get(), key.get());
+            leafSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(in.leaves, n, ctx.tables, dCanonByte.get(), allowed, sig.get(), key.get(), in.gridOf[2]);
             TDAG_LAUNCHED();
         }
         const uint64_t* leaves = in.leaves;
@@ -485,7 +538,11 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
             TDAG_LAUNCHED();
         };
         DevBuf<uint32_t> emitOrder;
-        const uint32_t u = n ? canonicaliseLevel(ctx, 2, n, sig.get(), 1, key.get(), resolve, prevMap, prevInv, emitOrder, midLevel == 2 ? &out.midInv : nullptr) : 0;
+        std::vector<uint64_t> hoff { 0, 0 };
+        const uint32_t u = n ? canonicaliseLevel(ctx, 2, n, sig.get(), in.gridOf[2] ? 2 : 1, key.get(), resolve, prevMap, prevInv, emitOrder,
+                                   midLevel == 2 ? &out.midInv : nullptr, in.gridOf[2], in.numGrids, hoff)
+                             : 0;
+        out.handleOff[2] = n ? hoff : std::vector<uint64_t>(in.numGrids + 1, 0);
         out.leaves = DevBuf<uint64_t>(u, s);
         if (u) {
             emitLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, in.leaves, out.leaves.get());
@@ -499,9 +556,14 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
     for (uint32_t level = 3; level <= in.rootLevel; ++level) {
         const uint32_t n = (uint32_t)in.nodeCounts[level];
         const uint32_t* nodes = in.nodes[level];
-        DevBuf<uint64_t> sig((size_t)n * 8, s), key(n, s);
+        const uint32_t* gridOf = in.gridOf[level];
+        const int sw = gridOf ? 9 : 8;
+        if (gridOf)
+            prevHandleOffDev = uploadOffsets(out.handleOff[level - 1]);
+        DevBuf<uint64_t> sig((size_t)n * sw, s), key(n, s);
         if (n) {
-            nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevInv.get(), ctx.tables, allowed, sig.get(), key.get());
+            nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevInv.get(), ctx.tables, allowed, sig.get(), key.get(), gridOf,
+                gridOf ? prevHandleOffDev.get() : nullptr);
             TDAG_LAUNCHED();
         }
         const uint64_t* pm = prevMap.get();
@@ -512,13 +574,18 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         };
         DevBuf<uint64_t> map, inv;
         DevBuf<uint32_t> emitOrder;
-        const uint32_t u = n ? canonicaliseLevel(ctx, level, n, sig.get(), 8, key.get(), resolve, map, inv, emitOrder, level == midLevel ? &out.midInv : nullptr) : 0;
+        std::vector<uint64_t> hoff { 0, 0 };
+        const uint32_t u = n ? canonicaliseLevel(ctx, level, n, sig.get(), sw, key.get(), resolve, map, inv, emitOrder, level == midLevel ? &out.midInv : nullptr,
+                                   gridOf, in.numGrids, hoff)
+                             : 0;
+        out.handleOff[level] = n ? hoff : std::vector<uint64_t>(in.numGrids + 1, 0);
         sig.release();
         key.release();
         auto& lvl = out.levels[level];
         lvl = DevBuf<uint64_t>((size_t)u * 8, s);
         if (u) {
-            emitNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(emitOrder.get(), u, nodes, prevMap.get(), lvl.get());
+            emitNodesKernel<<<gridFor((size_t)u * 8, 256), 256, 0, s>>>(emitOrder.get(), u, nodes, prevMap.get(), lvl.get(), gridOf,
+                gridOf ? prevHandleOffDev.get() : nullptr);
             TDAG_LAUNCHED();
         }
         prevMap = std::move(map);

@@ -22,26 +22,48 @@ struct Context {
     void checkStatus(const std::string& where);
 };
 
-// Device-resident view of an EditStructure<void, uint32_t>.
+// Device-resident view of an EditStructure<void, uint32_t>, or of a batch of them concatenated level
+// by level in grid order (child indices then address the concatenated level below). For a batch,
+// segOff[l] holds each grid's first item at level l (size numGrids + 1; level 2 = leaves) and
+// gridOf[l] the grid of every item. A single structure is the batch of one (numGrids == 1, no
+// segment arrays).
 struct DeviceSvdag {
     uint32_t resolution = 0, rootLevel = 0;
     const uint32_t* nodes[TDAG_MAX_LEVELS] {};
     uint64_t nodeCounts[TDAG_MAX_LEVELS] {};
     const uint64_t* leaves = nullptr;
     uint64_t leafCount = 0;
+    uint32_t numGrids = 1;
+    std::vector<uint64_t> segOff[TDAG_MAX_LEVELS];
+    const uint32_t* gridOf[TDAG_MAX_LEVELS] {};
+};
+
+// Grid segmentation of a list of items (host offsets + device per-item grid ids and offsets).
+struct Segments {
+    uint32_t numGrids = 1;
+    std::vector<uint64_t> off; // size numGrids + 1
+    const uint32_t* gridOf = nullptr; // device, per item; null for a single grid
+    const uint32_t* offDev = nullptr; // device copy of off (u32); null for a single grid
+    bool batched() const { return numGrids > 1; }
 };
 
 struct HierOutput {
-    std::vector<DevBuf<uint64_t>> levels; // per level: unique nodes x 8 TransformPointers
+    std::vector<DevBuf<uint64_t>> levels; // per level: unique nodes x 8 TransformPointers (grid-local child handles)
     DevBuf<uint64_t> leaves; // unique leaves
     DevBuf<uint32_t> midInv; // new -> old index at the mid level
+    std::vector<std::vector<uint64_t>> handleOff; // per level: first output item of each grid (numGrids + 1)
 };
 
 struct MatchOutput {
-    DevBuf<uint64_t> mapping; // per item: TransformPointer into the unique list
+    DevBuf<uint64_t> mapping; // per item: TransformPointer into its grid's unique list
     DevBuf<uint32_t> uniques; // item positions kept (ascending)
     uint32_t numUnique = 0;
+    std::vector<uint64_t> uniqueOff; // first kept item of each grid in `uniques` (numGrids + 1)
 };
+
+// Per-grid salt folded into corner-hash keys of batched builds (grid 0: no salt, so a single grid's
+// table is exactly the unsalted one).
+__host__ __device__ __forceinline__ uint64_t gridSalt(uint32_t g) { return g ? mix64(0x632BE59BD9B4E019ull + g) : 0ull; }
 
 inline uint64_t allowedMask(const tdag_config& c)
 {
@@ -62,6 +84,12 @@ void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s);
 HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, uint32_t midLevel, tdag_stats* stats);
 
 // findDuplicatesAmongFlattenedItems on n dense grids of level `level` (device pointer, n x W words).
-MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats);
+// seg (optional) splits the items into independent grids of a batch.
+MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats,
+    const Segments* seg = nullptr);
+
+// Segment helpers: per-item grid ids from offsets, per-grid counts of a grid-id list.
+void segmentIds(const uint32_t* offDev, uint32_t numGrids, uint64_t n, uint32_t* out, cudaStream_t s);
+std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx, uint64_t n, uint32_t numGrids, cudaStream_t s);
 
 } // namespace tdag

@@ -66,9 +66,19 @@ __host__ __device__ __forceinline__ uint32_t filterHash(uint64_t k)
     return h;
 }
 
+// Key of a non-zero corner/view hash in the table of grid `salt`'s batch member (zero stays reserved
+// for empty slots; the salt is 0 for a single grid, leaving the key unchanged).
+__device__ __forceinline__ uint64_t saltedKey(uint64_t h, uint64_t salt)
+{
+    const uint64_t k = h ^ salt;
+    return k ? k : 0x9E3779B97F4A7C15ull;
+}
+
 // ---------------------------------------------------------------------------- popcount order
+// Sort key: grid id above (R^3 - popcount), so a batch sorts grid by grid, popcount descending.
 template <int W>
-__global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n, uint32_t maxCount, uint64_t* __restrict__ key, uint32_t* __restrict__ val)
+__global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n, uint32_t maxCount, uint64_t* __restrict__ key, uint32_t* __restrict__ val,
+    const uint32_t* __restrict__ gridOf)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -77,7 +87,7 @@ __global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n
 #pragma unroll 8
     for (int k = 0; k < W; ++k)
         c += __popcll(grids[(size_t)i * W + k]);
-    key[i] = maxCount - c; // ascending key == descending popcount; stable sort keeps index order
+    key[i] = (gridOf ? ((uint64_t)gridOf[i] << 13) : 0ull) | (maxCount - c); // ascending key == descending popcount; stable sort keeps index order
     val[i] = i;
 }
 
@@ -85,7 +95,8 @@ __global__ void popcountKeyKernel(const uint64_t* __restrict__ grids, uint32_t n
 // Warp per (item, direction). The value at the anchor corner is a nested fold: x-lines, then the
 // anchor x-plane along y, then the anchor column along z (computeGridHashInPlace<R, +x, +y, +z>).
 template <int R>
-__global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n, uint64_t* __restrict__ keys, uint32_t* __restrict__ payload)
+__global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n, uint64_t* __restrict__ keys, uint32_t* __restrict__ payload,
+    const uint32_t* __restrict__ gridOf)
 {
     constexpr int W = R * R * R / 64;
     constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
@@ -124,7 +135,7 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
         acc = foldStep(acc, v);
     }
     if (lane == 0) {
-        keys[gw] = acc;
+        keys[gw] = (acc && gridOf) ? saltedKey(acc, gridSalt(gridOf[item])) : acc;
         payload[gw] = item * 8 + d;
     }
 }
@@ -192,12 +203,14 @@ __global__ void tableRangesKernel(ulonglong2* __restrict__ slots, const uint32_t
 
 // Entries still able to receive a lower parent: parent[target] > minKey of the next source batch.
 __global__ void liveEntriesKernel(const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay, size_t m, const unsigned long long* __restrict__ parents,
-    unsigned long long minKeyNext, uint32_t* __restrict__ flags)
+    unsigned long long minKeyNext, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gridOf, const unsigned long long* __restrict__ minKeyOfGrid)
 {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m)
         return;
-    flags[e] = (ekeys[e] != 0) && (parents[epay[e] >> 3] > minKeyNext);
+    const uint32_t t = epay[e] >> 3;
+    const unsigned long long mk = gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext;
+    flags[e] = (ekeys[e] != 0) && (parents[t] > mk);
 }
 
 __global__ void gatherEntriesKernel(const uint32_t* __restrict__ idx, uint32_t n, const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay,
@@ -224,6 +237,11 @@ struct SearchParams {
     uint32_t* workCounter;
     unsigned long long* counters; // probes, filterPass, hits, candidates, verifications, verified
     uint32_t allowSym, allowPerm, allowTrans;
+    // batched builds (null for a single grid): grid of every item, first sorted position of every
+    // grid, and the batch's list of sorted source positions (indices begin..end of it)
+    const uint32_t* gridOf;
+    const uint32_t* segOff;
+    const uint32_t* workList;
 };
 
 template <int R>
@@ -235,8 +253,9 @@ struct SearchShape {
     static constexpr int SZ = (R + 1) * R;
     static constexpr int GRID = (R + 1) * R * R; // padded u64 hash grid
     static constexpr int N = R * R * R;
-    // per team: G1, G2, G3 (u64), srcW (u64), lines[3][R*R] (u16), queue[N] (u16), queue count (u32)
-    static constexpr size_t TEAM_BYTES = (size_t)(3 * GRID + W) * 8 + 3 * R * R * 2 + N * 2 + 16;
+    // per team: G1, G2, G3 (u64), srcW (u64), lines[3][R*R] (u16), queue[N] (u16), queue count (u32),
+    // source info (u32 x 5: local position, first and end target of its grid, salt low/high)
+    static constexpr size_t TEAM_BYTES = (size_t)(3 * GRID + W) * 8 + 3 * R * R * 2 + N * 2 + 32;
     static constexpr size_t SMEM = TEAM_BYTES * TEAMS + 16;
 };
 
@@ -296,6 +315,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
     uint16_t* lines = reinterpret_cast<uint16_t*>(srcW + W);
     uint16_t* queue = lines + 3 * R * R;
     uint32_t* qcount = reinterpret_cast<uint32_t*>(queue + N);
+    uint32_t* srcInfo = qcount + 1;
     uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::TEAM_BYTES * TEAMS);
     const int c1 = tl % R, c2 = tl / R;
 
@@ -309,13 +329,23 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
         __syncthreads();
         if (base >= p.end)
             break;
-        const uint32_t r = base + team;
-        const bool valid = r < p.end;
+        const uint32_t wi = base + team;
+        const bool valid = wi < p.end;
+        const uint32_t r = valid ? (p.workList ? p.workList[wi] : wi) : 0u;
+        uint64_t salt = 0;
         // ---- load the source grid and its three line orientations
         if (valid) {
-            const uint64_t* g = p.grids + (size_t)p.order[r] * W;
+            const uint32_t orig = p.order[r];
+            const uint64_t* g = p.grids + (size_t)orig * W;
             for (int k = tl; k < W; k += TEAM)
                 srcW[k] = g[k];
+            const uint32_t sg = p.gridOf ? p.gridOf[orig] : 0u;
+            salt = gridSalt(sg);
+            if (tl == 0) {
+                srcInfo[0] = p.segOff ? r - p.segOff[sg] : r;
+                srcInfo[1] = p.segOff ? p.segOff[sg] : 0u;
+                srcInfo[2] = p.segOff ? p.segOff[sg + 1] : 0xFFFFFFFFu;
+            }
         }
         if (tl == 0)
             *qcount = 0;
@@ -392,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                     G3[sbase3 + c * ss3] = acc;
                                     if (acc != 0) {
                                         ++cProbe;
-                                        const uint32_t fb = filterHash(acc) >> p.filterShift;
+                                        const uint32_t fb = filterHash(salt ? saltedKey(acc, salt) : acc) >> p.filterShift;
                                         if ((__ldg(&p.filter[fb >> 5]) >> (fb & 31)) & 1)
                                             pass |= 1u << c;
                                     }
@@ -446,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                 if (q < qn) {
                                     vidx = queue[q];
                                     const int x = vidx % R, y = (vidx / R) % R, z = vidx / (R * R);
-                                    const uint64_t h = G3[x + SY * y + SZ * z];
+                                    const uint64_t h = salt ? saltedKey(G3[x + SY * y + SZ * z], salt) : G3[x + SY * y + SZ * z];
                                     uint32_t slot = slotHash(h) & p.capMask;
                                     for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
                                         const ulonglong2 sv = p.slots[slot];
@@ -469,7 +499,9 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                     const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
                                     const uint32_t bv = __shfl_sync(0xffffffffu, vidx, src);
                                     const uint32_t srcTeam = ((threadIdx.x & ~31u) + src) / TEAM;
-                                    const uint32_t rSrc = base + srcTeam;
+                                    const uint32_t* info = reinterpret_cast<const uint32_t*>(smem + (size_t)srcTeam * Sh::TEAM_BYTES + (size_t)(3 * Sh::GRID + W) * 8
+                                        + 3 * R * R * 2 + N * 2) + 1;
+                                    const uint32_t rSrc = info[0], tLo = info[1], tHi = info[2];
                                     // permuted voxel (u[a0], u[a1], u[a2]) of the queued hash
                                     const int ux = bv % R, uy = (bv / R) % R, uz = bv / (R * R);
                                     const int v0 = a0 == 0 ? ux : (a0 == 1 ? uy : uz);
@@ -481,6 +513,8 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                         const uint32_t tgt = pay >> 3;
                                         const uint32_t S = dir ^ (pay & 7);
                                         ++cCand;
+                                        if (tgt < tLo || tgt >= tHi) // another grid of the batch
+                                            continue;
                                         const int T0 = (S & 1) ? v0 - an0 : an0 - v0;
                                         const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
                                         const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
@@ -527,7 +561,8 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
 
 // ---------------------------------------------------------------------------- resolve
 __global__ void decodeParentsKernel(const unsigned long long* __restrict__ parents, uint32_t n, const uint32_t* __restrict__ order, uint64_t sentinelKey,
-    uint32_t level, uint64_t* __restrict__ parentTP, uint32_t* __restrict__ isUnique)
+    uint32_t level, uint64_t* __restrict__ parentTP, uint32_t* __restrict__ isUnique, const uint32_t* __restrict__ gridOf = nullptr,
+    const uint32_t* __restrict__ segOff = nullptr)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -538,23 +573,24 @@ __global__ void decodeParentsKernel(const unsigned long long* __restrict__ paren
         isUnique[i] = 1;
     } else {
         uint64_t v = decodeFixed64(e, level);
-        const uint32_t src = order[tpPtr(v)];
+        const uint32_t src = order[tpPtr(v) + (gridOf ? segOff[gridOf[i]] : 0u)]; // parent's sorted position is local to the grid
         parentTP[i] = tpWithPtr(v, src);
         isUnique[src] = 1;
     }
 }
 
 __global__ void finalMappingKernel(const uint64_t* __restrict__ parentTP, const uint32_t* __restrict__ isUnique, const uint32_t* __restrict__ newIdx, uint32_t n,
-    uint64_t* __restrict__ mapping)
+    uint64_t* __restrict__ mapping, const uint32_t* __restrict__ gridOf = nullptr, const uint32_t* __restrict__ segOff = nullptr)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    const uint32_t base = gridOf ? newIdx[segOff[gridOf[i]]] : 0u; // kept items of earlier grids
     if (isUnique[i]) {
-        mapping[i] = tpCreate(newIdx[i], 0, 0);
+        mapping[i] = tpCreate(newIdx[i] - base, 0, 0);
     } else {
         const uint64_t pt = parentTP[i];
-        mapping[i] = tpWithPtr(pt, newIdx[tpPtr(pt)]);
+        mapping[i] = tpWithPtr(pt, newIdx[tpPtr(pt)] - base);
     }
 }
 
@@ -615,30 +651,39 @@ void buildTable(Context& ctx, const uint64_t* ekeys, const uint32_t* epay, size_
 }
 
 template <int L>
-MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats)
+MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg)
 {
     constexpr int R = 1 << L;
     constexpr int W = R * R * R / 64;
     cudaStream_t s = ctx.stream;
     MatchOutput out;
-    if (n == 0)
+    const bool batched = seg && seg->batched();
+    const uint32_t numGrids = batched ? seg->numGrids : 1u;
+    if (n == 0) {
+        out.uniqueOff.assign(numGrids + 1, 0);
         return out;
+    }
     TDAG_CHECK(n < (1u << 29), TDAG_ERR_ARG, "too many items for one matcher level");
+    const uint32_t* gridOf = batched ? seg->gridOf : nullptr;
+    const uint32_t* segOff = batched ? seg->offDev : nullptr;
 
-    // popcount order
+    // popcount order (grid by grid in a batch)
     DevBuf<uint32_t> order(n, s);
     {
         DevBuf<uint64_t> key(n, s);
-        popcountKeyKernel<W><<<gridFor(n, 256), 256, 0, s>>>(grids, n, R * R * R, key.get(), order.get());
+        popcountKeyKernel<W><<<gridFor(n, 256), 256, 0, s>>>(grids, n, R * R * R, key.get(), order.get(), gridOf);
         TDAG_LAUNCHED();
-        radixSortPairs(key.get(), order.get(), n, 0, 16, s);
+        uint32_t bits = 16;
+        while (batched && (1ull << (bits - 13)) < numGrids)
+            bits += 8;
+        radixSortPairs(key.get(), order.get(), n, 0, bits, s);
     }
 
     // corner hashes: 8 per item; zero hashes (empty grids) are never entries
     const size_t m = (size_t)n * 8;
     DevBuf<uint64_t> ekeys(m, s);
     DevBuf<uint32_t> epay(m, s);
-    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, ekeys.get(), epay.get());
+    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, ekeys.get(), epay.get(), gridOf);
     TDAG_LAUNCHED();
 
     const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, L);
@@ -657,13 +702,39 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     perSM = std::max(perSM, 1);
     const uint32_t maxBlocks = (uint32_t)ctx.numSMs * perSM;
 
-    // batch boundaries over sorted source positions: doubling, starting at a few waves of teams
+    // Source batches. Single grid: doubling ranges of sorted positions, starting at a few waves of
+    // teams. Batch: the same fractions of every grid (1/256, 1/128, ..., 1/2, 1), as a list of sorted
+    // positions per batch, with each grid's own next-batch start for the pruning keys.
     std::vector<uint32_t> bounds { 0 };
-    const uint32_t minBatch = std::max<uint32_t>(maxBlocks * SearchShape<R>::TEAMS * 2, n / 256);
-    while (bounds.back() < n) {
-        const uint32_t b = bounds.back();
-        bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 2ull * b)));
+    std::vector<uint32_t> workList;
+    std::vector<std::vector<unsigned long long>> minKeys; // per batch, per grid
+    if (!batched) {
+        const uint32_t minBatch = std::max<uint32_t>(maxBlocks * SearchShape<R>::TEAMS * 2, n / 256);
+        while (bounds.back() < n) {
+            const uint32_t b = bounds.back();
+            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 2ull * b)));
+        }
+    } else {
+        constexpr int kBatches = 9;
+        auto frac = [](uint64_t cnt, int k) { return k == 0 ? 0ull : (k >= kBatches ? cnt : (cnt >> (kBatches - k))); };
+        workList.reserve(n);
+        for (int k = 0; k < kBatches; ++k) {
+            std::vector<unsigned long long> mk(numGrids);
+            for (uint32_t g = 0; g < numGrids; ++g) {
+                const uint64_t cnt = seg->off[g + 1] - seg->off[g];
+                const uint64_t lo = frac(cnt, k), hi = frac(cnt, k + 1);
+                for (uint64_t q = lo; q < hi; ++q)
+                    workList.push_back((uint32_t)(seg->off[g] + q));
+                mk[g] = encodeFixed64(lo, 0, 0, 1 - R, 1 - R, 1 - R, L);
+            }
+            minKeys.push_back(std::move(mk));
+            bounds.push_back((uint32_t)workList.size());
+        }
     }
+    DevBuf<uint32_t> workListDev(workList.size(), s);
+    DevBuf<unsigned long long> minKeyDev(numGrids, s);
+    if (!workList.empty())
+        TDAG_CUDA(cudaMemcpyAsync(workListDev.get(), workList.data(), workList.size() * 4, cudaMemcpyHostToDevice, s));
 
     Table table;
     buildTable(ctx, ekeys.get(), epay.get(), m, table);
@@ -674,10 +745,17 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint32_t> p2(m, s);
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi) {
         const uint32_t b0 = bounds[bi], b1 = bounds[bi + 1];
+        if (b0 == b1)
+            continue;
         if (bi > 0) {
-            // drop targets whose parent no source at or after b0 can lower
+            // drop targets whose parent no source at or after this batch can lower
             const unsigned long long minKeyNext = encodeFixed64(b0, 0, 0, 1 - R, 1 - R, 1 - R, L);
-            liveEntriesKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), epay.get(), m, parents.get(), minKeyNext, flags.get());
+            if (batched) {
+                TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
+                TDAG_CUDA(cudaStreamSynchronize(s));
+            }
+            liveEntriesKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), epay.get(), m, parents.get(), minKeyNext, flags.get(), gridOf,
+                batched ? minKeyDev.get() : nullptr);
             TDAG_LAUNCHED();
             const uint32_t live = compactFlags(flags.get(), liveIdx.get(), m, s);
             if (live == 0)
@@ -686,7 +764,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             TDAG_LAUNCHED();
             buildTable(ctx, k2.get(), p2.get(), live, table);
         }
-        SearchParams sp;
+        SearchParams sp {};
         sp.grids = grids;
         sp.order = order.get();
         sp.begin = b0;
@@ -702,6 +780,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         sp.allowSym = cfg.symmetry ? 1 : 0;
         sp.allowPerm = cfg.axis_permutation ? 1 : 0;
         sp.allowTrans = cfg.translation ? 1 : 0;
+        sp.gridOf = gridOf;
+        sp.segOff = segOff;
+        sp.workList = batched ? workListDev.get() : nullptr;
         TDAG_CUDA(cudaMemsetAsync(work.get(), 0, 4, s));
         const uint64_t groups = ((uint64_t)(b1 - b0) + SearchShape<R>::TEAMS - 1) / SearchShape<R>::TEAMS;
         const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
@@ -724,29 +805,30 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint64_t> parentTP(n, s);
     DevBuf<uint32_t> isUnique(n, s), newIdx(n, s);
     TDAG_CUDA(cudaMemsetAsync(isUnique.get(), 0, (size_t)n * 4, s));
-    decodeParentsKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, order.get(), sentinelKey, L, parentTP.get(), isUnique.get());
+    decodeParentsKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, order.get(), sentinelKey, L, parentTP.get(), isUnique.get(), gridOf, segOff);
     TDAG_LAUNCHED();
     out.uniques = DevBuf<uint32_t>(n, s);
     out.numUnique = compactFlags(isUnique.get(), out.uniques.get(), n, s);
     exclusiveScanU32(isUnique.get(), newIdx.get(), n, s);
     out.mapping = DevBuf<uint64_t>(n, s);
-    finalMappingKernel<<<gridFor(n, 256), 256, 0, s>>>(parentTP.get(), isUnique.get(), newIdx.get(), n, out.mapping.get());
+    finalMappingKernel<<<gridFor(n, 256), 256, 0, s>>>(parentTP.get(), isUnique.get(), newIdx.get(), n, out.mapping.get(), gridOf, segOff);
     TDAG_LAUNCHED();
+    out.uniqueOff = batched ? countPerGrid(gridOf, out.uniques.get(), out.numUnique, numGrids, s) : std::vector<uint64_t> { 0, out.numUnique };
 
     if (stats) {
         unsigned long long c[8];
         TDAG_CUDA(cudaMemcpyAsync(c, counters.get(), 64, cudaMemcpyDeviceToHost, s));
         TDAG_CUDA(cudaStreamSynchronize(s));
-        stats->items = n;
-        stats->unique = out.numUnique;
-        stats->probes = c[0];
-        stats->filter_pass = c[1];
-        stats->hits = c[2];
-        stats->candidates = c[3];
-        stats->verifications = c[4];
-        stats->verified = c[5];
-        stats->table_entries = entriesInitial;
-        stats->search_ms = searchMs;
+        stats->items += n;
+        stats->unique += out.numUnique;
+        stats->probes += c[0];
+        stats->filter_pass += c[1];
+        stats->hits += c[2];
+        stats->candidates += c[3];
+        stats->verifications += c[4];
+        stats->verified += c[5];
+        stats->table_entries += entriesInitial;
+        stats->search_ms += searchMs;
     }
     ctx.checkStatus("matcher level " + std::to_string(L));
     return out;
@@ -923,7 +1005,7 @@ void runMatcherNoAlloc(Context& ctx, unsigned char* scratch, const uint64_t* gri
 
     noAllocRankKernel<W><<<1, 1024, 0, s>>>(grids, n, A.pc, A.order);
     TDAG_LAUNCHED();
-    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, A.ekeys, A.epay);
+    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, A.ekeys, A.epay, nullptr);
     TDAG_LAUNCHED();
     tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(A.ekeys, m, A.slots, A.tcount, A.slotOfEntry, A.capMask, A.misc + 1, ctx.status);
     TDAG_LAUNCHED();
@@ -936,7 +1018,7 @@ void runMatcherNoAlloc(Context& ctx, unsigned char* scratch, const uint64_t* gri
     const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, LV);
     fillU64(reinterpret_cast<uint64_t*>(A.parents), sentinelKey, n, s);
 
-    SearchParams sp;
+    SearchParams sp {};
     sp.grids = grids;
     sp.order = A.order;
     sp.begin = 0;
@@ -987,15 +1069,15 @@ unsigned char* noAllocScratchAddress(int device)
 
 } // namespace
 
-MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats)
+MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg)
 {
     switch (level) {
     case 2:
-        return runMatcherL<2>(ctx, grids, n, cfg, stats);
+        return runMatcherL<2>(ctx, grids, n, cfg, stats, seg);
     case 3:
-        return runMatcherL<3>(ctx, grids, n, cfg, stats);
+        return runMatcherL<3>(ctx, grids, n, cfg, stats, seg);
     case 4:
-        return runMatcherL<4>(ctx, grids, n, cfg, stats);
+        return runMatcherL<4>(ctx, grids, n, cfg, stats, seg);
     default:
         throw Error(TDAG_ERR_ARG, "translation matching supports levels 2..4");
     }

@@ -3,6 +3,8 @@
 // The reference sorts with std::sort / std::stable_sort (find_translation.cpp:639,727;
 // transform_dag_hierarchical.cpp:378). These kernels give the same orders: a stable sort on the key,
 // with values fed in ascending index order, yields (key, index) order.
+#include <vector>
+
 #include "common.cuh"
 
 namespace tdag {
@@ -129,6 +131,56 @@ __global__ void scatterFlagsKernel(const uint32_t* __restrict__ flags, const uin
         out[offs[i]] = (uint32_t)i;
 }
 } // namespace
+
+namespace {
+// grid of item i = the last g with off[g] <= i (binary search over numGrids + 1 offsets)
+__global__ void segmentIdsKernel(const uint32_t* __restrict__ off, uint32_t numGrids, uint64_t n, uint32_t* __restrict__ out)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t lo = 0, hi = numGrids; // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    out[i] = lo;
+}
+__global__ void countPerGridKernel(const uint32_t* __restrict__ gridIds, const uint32_t* __restrict__ idx, uint64_t n, uint32_t* __restrict__ counts)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        atomicAdd(&counts[gridIds[idx ? idx[i] : i]], 1u);
+}
+} // namespace
+
+void segmentIds(const uint32_t* offDev, uint32_t numGrids, uint64_t n, uint32_t* out, cudaStream_t s)
+{
+    if (!n)
+        return;
+    segmentIdsKernel<<<gridFor(n, 256), 256, 0, s>>>(offDev, numGrids, n, out);
+    TDAG_LAUNCHED();
+}
+
+std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx, uint64_t n, uint32_t numGrids, cudaStream_t s)
+{
+    std::vector<uint64_t> off(numGrids + 1, 0);
+    if (n) {
+        DevBuf<uint32_t> counts(numGrids, s);
+        TDAG_CUDA(cudaMemsetAsync(counts.get(), 0, numGrids * 4, s));
+        countPerGridKernel<<<gridFor(n, 256), 256, 0, s>>>(gridIds, idx, n, counts.get());
+        TDAG_LAUNCHED();
+        std::vector<uint32_t> c(numGrids);
+        TDAG_CUDA(cudaMemcpyAsync(c.data(), counts.get(), numGrids * 4, cudaMemcpyDeviceToHost, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        for (uint32_t g = 0; g < numGrids; ++g)
+            off[g + 1] = off[g] + c[g];
+    }
+    return off;
+}
 
 uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s)
 {

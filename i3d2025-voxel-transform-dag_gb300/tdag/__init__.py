@@ -463,3 +463,36 @@ def construct_transform_dag_device(in_dag: DeviceSvdag, config: TransformDAGConf
     rp = ctypes.POINTER(_abi.Result)()
     _abi.check(lib().tdag_build_device(ctx.handle, ctypes.byref(v), ctypes.byref(_config_struct(config)), ctypes.byref(rp)))
     return DeviceResult(rp)
+
+
+def construct_transform_dag_batched(dags: List[EditStructure], config: TransformDAGConfig = TransformDAGConfig(),
+                                    ctx: Optional[Context] = None, return_stats: bool = False):
+    """Batched constructTransformDAG (tdag_build_batched): one pass over all structures, result i equal
+    to construct_transform_dag(dags[i]) bit for bit."""
+    ctx = ctx or default_context()
+    keep = []
+    views = (_abi.SvdagView * max(1, len(dags)))()
+    for i, d in enumerate(dags):
+        views[i] = _view_of(d, keep)
+    outs = (ctypes.POINTER(_abi.Result) * max(1, len(dags)))()
+    st = _abi.Stats()
+    _abi.check(lib().tdag_build_batched(ctx.handle, views, len(dags), ctypes.byref(_config_struct(config)), outs, ctypes.byref(st)))
+    results = [_take_result(outs[i])[0] for i in range(len(dags))]
+    if return_stats:
+        return results, _abi.stats_to_dict(st, max((d.root_level for d in dags), default=2))
+    return results
+
+
+def construct_transform_dag_batched_device(dags: List["DeviceSvdag"], config: TransformDAGConfig = TransformDAGConfig(),
+                                           ctx: Optional[Context] = None):
+    """tdag_build_batched_device: device-resident inputs and results. Returns (results, batch stats)."""
+    ctx = ctx or default_context()
+    views = (_abi.SvdagView * max(1, len(dags)))()
+    root = 2
+    for i, d in enumerate(dags):
+        views[i] = d.view()
+        root = max(root, views[i].root_level)
+    outs = (ctypes.POINTER(_abi.Result) * max(1, len(dags)))()
+    st = _abi.Stats()
+    _abi.check(lib().tdag_build_batched_device(ctx.handle, views, len(dags), ctypes.byref(_config_struct(config)), outs, ctypes.byref(st)))
+    return [DeviceResult(outs[i]) for i in range(len(dags))], _abi.stats_to_dict(st, root)

@@ -126,6 +126,16 @@ int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, const tda
 
 int tdag_result_free(tdag_result* result);
 
+/* Batched constructTransformDAG (no reference counterpart: the reference builds one structure per
+ * call). Builds `count` independent SVDAGs of any sizes together — every stage runs one set of
+ * launches for the whole batch — and out[i] equals tdag_build of in[i] bit for bit. out must hold
+ * `count` pointers, each released with tdag_result_free. batch_stats (may be NULL) receives the
+ * statistics of the whole batch. Host in / host out, or device in / device out. */
+int tdag_build_batched(tdag_ctx* ctx, const tdag_svdag_view* in_host, uint32_t count, const tdag_config* config,
+    tdag_result** out, tdag_stats* batch_stats);
+int tdag_build_batched_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, uint32_t count, const tdag_config* config,
+    tdag_result** out, tdag_stats* batch_stats);
+
 /* findDuplicatesAmongFlattenedItems_cpp2<Level>(items, grids, outPrevLevelMapping, config)
  * (transform_dag.h:307-308; tools/lib/src/voxel/find_translation.cpp:616-1000), on dense grids:
  * grids = n x (R^3 / 64) uint64 words, R = 1 << level, bit index x + R*y + R*R*z
