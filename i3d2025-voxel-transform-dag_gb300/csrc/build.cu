@@ -741,6 +741,36 @@ int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag
     return tdag_build(ctx, in, &c, out);
 }
 
+int tdag_result_to_host(tdag_ctx* ctx, const tdag_result* d, tdag_result** out)
+{
+    if (!ctx || !d || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        TDAG_CHECK(d->on_device, TDAG_ERR_ARG, "result is not device-resident");
+        Context& c = ctx->c;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        std::unique_ptr<tdag_result> r(newResult(d->resolution, d->root_level, false));
+        r->structure_type = d->structure_type;
+        r->stats = d->stats;
+        for (uint32_t l = 3; l <= d->root_level; ++l) {
+            const size_t bytes = d->node_counts[l] * 64;
+            r->node_counts[l] = d->node_counts[l];
+            r->nodes[l] = (uint64_t*)std::malloc(bytes ? bytes : 1);
+            TDAG_CHECK(r->nodes[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
+            if (bytes)
+                TDAG_CUDA(cudaMemcpyAsync(r->nodes[l], d->nodes[l], bytes, cudaMemcpyDeviceToHost, c.stream));
+        }
+        r->leaf_count = d->leaf_count;
+        r->leaves = (uint64_t*)std::malloc(d->leaf_count ? d->leaf_count * 8 : 1);
+        TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
+        if (d->leaf_count)
+            TDAG_CUDA(cudaMemcpyAsync(r->leaves, d->leaves, d->leaf_count * 8, cudaMemcpyDeviceToHost, c.stream));
+        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+        *out = r.release();
+    });
+}
+
 int tdag_result_free(tdag_result* r)
 {
     if (!r)

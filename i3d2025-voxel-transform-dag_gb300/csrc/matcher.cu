@@ -27,6 +27,7 @@
 //   shared memory, looked up in the table (16-byte slots: key + range) and each hit's candidate range
 //   is spread across the warp.
 #include <algorithm>
+#include <cstdlib>
 #include <functional>
 #include <mutex>
 #include <vector>
@@ -794,6 +795,12 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         float ms = 0;
         TDAG_CUDA(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]));
         searchMs += ms;
+        if (std::getenv("TDAG_TRACE")) { // per-batch diagnostics on stderr
+            unsigned long long c[8];
+            TDAG_CUDA(cudaMemcpy(c, counters.get(), 64, cudaMemcpyDeviceToHost));
+            std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu\n", L, bi,
+                b1 - b0, (unsigned long long)table.numEntries, ms, c[0], c[1], c[2], c[3], c[4]);
+        }
     }
     table = Table();
     flags.release();

@@ -443,6 +443,13 @@ class DeviceResult:
         self._rp = rp
         self.stats = _abi.stats_to_dict(rp.contents.stats, rp.contents.root_level)
 
+    def to_host(self, ctx: Optional[Context] = None) -> EditStructure:
+        """Host copy of the device-resident result (tdag_result_to_host)."""
+        ctx = ctx or default_context()
+        hp = ctypes.POINTER(_abi.Result)()
+        _abi.check(lib().tdag_result_to_host(ctx.handle, self._rp, ctypes.byref(hp)))
+        return _take_result(hp)[0]
+
     def free(self):
         if self._rp:
             lib().tdag_result_free(self._rp)

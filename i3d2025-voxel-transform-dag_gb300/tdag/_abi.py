@@ -85,7 +85,7 @@ EXPORTED = (
     "tdag_build", "tdag_build_device", "tdag_result_free", "tdag_find_duplicates_level", "tdag_build_hierarchical",
     "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
     "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
-    "tdag_build_batched", "tdag_build_batched_device",
+    "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
 )
 
 _lib = None
@@ -126,6 +126,7 @@ def lib(path: str = None):
         L.tdag_svdag_free.argtypes = [vp]
         L.tdag_find_duplicates_level_noalloc.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.POINTER(Config),
                                                          vp, vp, vp]
+        L.tdag_result_to_host.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(ctypes.POINTER(Result))]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

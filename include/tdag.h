@@ -126,6 +126,9 @@ int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, const tda
 
 int tdag_result_free(tdag_result* result);
 
+/* Host copy of a device-resident result (release both with tdag_result_free). */
+int tdag_result_to_host(tdag_ctx* ctx, const tdag_result* device_result, tdag_result** host_out);
+
 /* Batched constructTransformDAG (no reference counterpart: the reference builds one structure per
  * call). Builds `count` independent SVDAGs of any sizes together — every stage runs one set of
  * launches for the whole batch — and out[i] equals tdag_build of in[i] bit for bit. out must hold
