@@ -41,13 +41,20 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// One step of the directional box hash (find_translation.cpp:210-218).
-__device__ __forceinline__ uint64_t foldStep(uint64_t acc, uint64_t v)
+// One step of the directional box hash, pass P (0: along the first fold axis, 1: second, 2: third).
+// The reference folds with hash_combine and clamps to 1 once started (find_translation.cpp:210-218).
+// Which hash is used does not change the result: a probe only proposes (source, target, transform)
+// candidates and every candidate is verified exactly, and verification passes precisely when the two
+// boxes agree after leading empty elements are stripped on every axis -- which makes any such hash
+// equal. The only requirements are (a) leading empty elements leave the state at zero and (b) a
+// non-empty box never hashes to zero (it would not be probed). This fold is a polynomial hash mod
+// 2^64 with an odd base per pass, and bit 0 carries "started": 0 stays 0, a non-empty box is odd.
+// It costs three integer multiply-adds and a logic op instead of the shift/add chain of hash_combine.
+template <int P>
+__device__ __forceinline__ uint64_t boxFold(uint64_t acc, uint64_t v)
 {
-    const bool started = (v | acc) != 0;
-    uint64_t c = hashCombine(acc, v);
-    c = c < 1 ? 1 : c;
-    return started ? c : 0;
+    constexpr uint64_t K = P == 0 ? 0x9E3779B97F4A7C15ull : (P == 1 ? 0xC2B2AE3D27D4EB4Full : 0x165667B19E3779F9ull);
+    return (acc * K + v) | (acc & 1u);
 }
 
 // Table slot and membership-filter indices (32-bit multiply-xorshift hashes of the 64-bit key).
@@ -67,13 +74,9 @@ __host__ __device__ __forceinline__ uint32_t filterHash(uint64_t k)
     return h;
 }
 
-// Key of a non-zero corner/view hash in the table of grid `salt`'s batch member (zero stays reserved
-// for empty slots; the salt is 0 for a single grid, leaving the key unchanged).
-__device__ __forceinline__ uint64_t saltedKey(uint64_t h, uint64_t salt)
-{
-    const uint64_t k = h ^ salt;
-    return k ? k : 0x9E3779B97F4A7C15ull;
-}
+// Per-grid salt of the box hashes of a batch member: even, so a salted non-empty box hash stays odd
+// and never collides with the empty-slot key 0; 0 for a single grid, leaving the key unchanged.
+__host__ __device__ __forceinline__ uint64_t boxSalt(uint32_t g) { return gridSalt(g) & ~1ull; }
 
 // ---------------------------------------------------------------------------- popcount order
 // Sort key: grid id above (R^3 - popcount), so a batch sorts grid by grid, popcount descending.
@@ -115,7 +118,7 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
         uint64_t acc = 0;
         for (int k = 0; k < R; ++k) {
             const int x = px ? R - 1 - k : k;
-            acc = foldStep(acc, (row >> x) & 1);
+            acc = boxFold<0>(acc, (row >> x) & 1);
         }
         xres[warp][line] = acc;
     }
@@ -125,7 +128,7 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
         uint64_t acc = 0;
         for (int k = 0; k < R; ++k) {
             const int y = py ? R - 1 - k : k;
-            acc = foldStep(acc, xres[warp][y + R * lane]);
+            acc = boxFold<1>(acc, xres[warp][y + R * lane]);
         }
         yv = acc;
     }
@@ -133,10 +136,10 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
     for (int k = 0; k < R; ++k) {
         const int z = pz ? R - 1 - k : k;
         const uint64_t v = __shfl_sync(0xffffffffu, yv, z);
-        acc = foldStep(acc, v);
+        acc = boxFold<2>(acc, v);
     }
     if (lane == 0) {
-        keys[gw] = (acc && gridOf) ? saltedKey(acc, gridSalt(gridOf[item])) : acc;
+        keys[gw] = gridOf ? acc ^ boxSalt(gridOf[item]) : acc; // a grid is never empty: acc is odd
         payload[gw] = item * 8 + d;
     }
 }
@@ -341,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
             for (int k = tl; k < W; k += TEAM)
                 srcW[k] = g[k];
             const uint32_t sg = p.gridOf ? p.gridOf[orig] : 0u;
-            salt = gridSalt(sg);
+            salt = boxSalt(sg);
             if (tl == 0) {
                 srcInfo[0] = p.segOff ? r - p.segOff[sg] : r;
                 srcInfo[1] = p.segOff ? p.segOff[sg] : 0u;
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                     for (int k = 0; k < R; ++k) {
                         const int c = d0 ? R - 1 - k : k;
                         const int bi = bbase + c * bs;
-                        acc = foldStep(acc, (srcW[bi >> 6] >> (bi & 63)) & 1);
+                        acc = boxFold<0>(acc, (srcW[bi >> 6] >> (bi & 63)) & 1);
                         G1[sbase + c * ss] = acc;
                     }
                 }
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
 #pragma unroll 4
                             for (int k = 0; k < R; ++k) {
                                 const int c = d1 ? R - 1 - k : k;
-                                acc = foldStep(acc, G1[sbase + c * ss]);
+                                acc = boxFold<1>(acc, G1[sbase + c * ss]);
                                 G2[sbase + c * ss] = acc;
                             }
                         }
@@ -415,19 +418,31 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                         for (int d2 = 1; d2 >= 0; --d2) {
                             uint32_t pass = 0;
                             if (valid) {
+                                // fold the whole line first, then issue every filter load of the line
+                                // before the first one is consumed
                                 uint64_t acc = 0;
-#pragma unroll 4
+                                uint32_t started = 0;
+                                uint32_t fbit[R];
+#pragma unroll
                                 for (int k = 0; k < R; ++k) {
                                     const int c = d2 ? R - 1 - k : k;
-                                    acc = foldStep(acc, G2[sbase3 + c * ss3]);
+                                    acc = boxFold<2>(acc, G2[sbase3 + c * ss3]);
                                     G3[sbase3 + c * ss3] = acc;
-                                    if (acc != 0) {
-                                        ++cProbe;
-                                        const uint32_t fb = filterHash(salt ? saltedKey(acc, salt) : acc) >> p.filterShift;
-                                        if ((__ldg(&p.filter[fb >> 5]) >> (fb & 31)) & 1)
-                                            pass |= 1u << c;
-                                    }
+                                    started |= (uint32_t)(acc & 1u) << c;
+                                    fbit[k] = filterHash(acc ^ salt) >> p.filterShift;
                                 }
+                                uint32_t word[R];
+#pragma unroll
+                                for (int k = 0; k < R; ++k) {
+                                    const int c = d2 ? R - 1 - k : k;
+                                    word[k] = ((started >> c) & 1u) ? __ldg(&p.filter[fbit[k] >> 5]) : 0u;
+                                }
+#pragma unroll
+                                for (int k = 0; k < R; ++k) {
+                                    const int c = d2 ? R - 1 - k : k;
+                                    pass |= ((word[k] >> (fbit[k] & 31)) & 1u) << c;
+                                }
+                                cProbe += __popc(started);
                             }
                             // warp-aggregated enqueue of the surviving voxels (logical index x + R y + R^2 z)
                             {
@@ -477,7 +492,7 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                 if (q < qn) {
                                     vidx = queue[q];
                                     const int x = vidx % R, y = (vidx / R) % R, z = vidx / (R * R);
-                                    const uint64_t h = salt ? saltedKey(G3[x + SY * y + SZ * z], salt) : G3[x + SY * y + SZ * z];
+                                    const uint64_t h = G3[x + SY * y + SZ * z] ^ salt;
                                     uint32_t slot = slotHash(h) & p.capMask;
                                     for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
                                         const ulonglong2 sv = p.slots[slot];
@@ -492,7 +507,57 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                     }
                                     cHit += cnt ? 1 : 0;
                                 }
-                                uint32_t hitMask = __ballot_sync(0xffffffffu, cnt != 0);
+                                const int an0 = d0 ? 0 : R - 1, an1 = d1 ? 0 : R - 1, an2 = d2 ? 0 : R - 1;
+                                // One candidate (target, corner) of a hit at permuted voxel (v0, v1, v2) of the
+                                // source of team srcTeam (find_translation.cpp:820-864).
+                                auto candidate = [&](uint32_t pay, int v0, int v1, int v2, uint32_t srcTeam, uint32_t rSrc, uint32_t tLo, uint32_t tHi) {
+                                    const uint32_t tgt = pay >> 3;
+                                    const uint32_t S = dir ^ (pay & 7);
+                                    ++cCand;
+                                    if (tgt < tLo || tgt >= tHi) // another grid of the batch
+                                        return;
+                                    const int T0 = (S & 1) ? v0 - an0 : an0 - v0;
+                                    const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
+                                    const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
+                                    if (!p.allowPerm && pid != 0)
+                                        return;
+                                    if (!p.allowSym && S != 0)
+                                        return;
+                                    if (!p.allowTrans && (T0 | T1 | T2) != 0)
+                                        return;
+                                    const uint64_t key = encodeFixed64(rSrc, pid, S, T0, T1, T2, L);
+                                    const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
+                                    if (key >= cur)
+                                        return;
+                                    ++cVer;
+                                    const uint16_t* srcLines = reinterpret_cast<const uint16_t*>(
+                                        reinterpret_cast<const uint64_t*>(smem + (size_t)srcTeam * Sh::TEAM_BYTES) + 3 * Sh::GRID + W);
+                                    if (!verifyCandidate<R>(p.grids + (size_t)tgt * W, srcLines, a0, a1, a2, S, T0, T1, T2))
+                                        return;
+                                    ++cOk;
+                                    atomicMin(&p.parents[tgt], (unsigned long long)key);
+                                };
+                                auto teamInfo = [&](uint32_t t) {
+                                    return reinterpret_cast<const uint32_t*>(smem + (size_t)t * Sh::TEAM_BYTES + (size_t)(3 * Sh::GRID + W) * 8 + 3 * R * R * 2 + N * 2) + 1;
+                                };
+                                auto permutedVoxel = [&](uint32_t v, int& v0, int& v1, int& v2) {
+                                    const int ux = v % R, uy = (v / R) % R, uz = v / (R * R);
+                                    v0 = a0 == 0 ? ux : (a0 == 1 ? uy : uz);
+                                    v1 = a1 == 0 ? ux : (a1 == 1 ? uy : uz);
+                                    v2 = a2 == 0 ? ux : (a2 == 1 ? uy : uz);
+                                };
+                                // short ranges: every lane walks its own hit's candidates
+                                constexpr uint32_t kSerialMax = 8;
+                                if (cnt != 0 && cnt <= kSerialMax) {
+                                    const uint32_t myTeam = threadIdx.x / TEAM;
+                                    const uint32_t* info = teamInfo(myTeam);
+                                    int v0, v1, v2;
+                                    permutedVoxel(vidx, v0, v1, v2);
+                                    for (uint32_t e = 0; e < cnt; ++e)
+                                        candidate(__ldg(&p.entries[start + e]), v0, v1, v2, myTeam, info[0], info[1], info[2]);
+                                }
+                                // long ranges: the warp walks one range at a time
+                                uint32_t hitMask = __ballot_sync(0xffffffffu, cnt > kSerialMax);
                                 while (hitMask) {
                                     const int src = __ffs(hitMask) - 1;
                                     hitMask &= hitMask - 1;
@@ -500,43 +565,11 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                     const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
                                     const uint32_t bv = __shfl_sync(0xffffffffu, vidx, src);
                                     const uint32_t srcTeam = ((threadIdx.x & ~31u) + src) / TEAM;
-                                    const uint32_t* info = reinterpret_cast<const uint32_t*>(smem + (size_t)srcTeam * Sh::TEAM_BYTES + (size_t)(3 * Sh::GRID + W) * 8
-                                        + 3 * R * R * 2 + N * 2) + 1;
-                                    const uint32_t rSrc = info[0], tLo = info[1], tHi = info[2];
-                                    // permuted voxel (u[a0], u[a1], u[a2]) of the queued hash
-                                    const int ux = bv % R, uy = (bv / R) % R, uz = bv / (R * R);
-                                    const int v0 = a0 == 0 ? ux : (a0 == 1 ? uy : uz);
-                                    const int v1 = a1 == 0 ? ux : (a1 == 1 ? uy : uz);
-                                    const int v2 = a2 == 0 ? ux : (a2 == 1 ? uy : uz);
-                                    const int an0 = d0 ? 0 : R - 1, an1 = d1 ? 0 : R - 1, an2 = d2 ? 0 : R - 1;
-                                    for (uint32_t e = lane; e < bc; e += 32) {
-                                        const uint32_t pay = __ldg(&p.entries[bs + e]);
-                                        const uint32_t tgt = pay >> 3;
-                                        const uint32_t S = dir ^ (pay & 7);
-                                        ++cCand;
-                                        if (tgt < tLo || tgt >= tHi) // another grid of the batch
-                                            continue;
-                                        const int T0 = (S & 1) ? v0 - an0 : an0 - v0;
-                                        const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
-                                        const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
-                                        if (!p.allowPerm && pid != 0)
-                                            continue;
-                                        if (!p.allowSym && S != 0)
-                                            continue;
-                                        if (!p.allowTrans && (T0 | T1 | T2) != 0)
-                                            continue;
-                                        const uint64_t key = encodeFixed64(rSrc, pid, S, T0, T1, T2, L);
-                                        const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
-                                        if (key >= cur)
-                                            continue;
-                                        ++cVer;
-                                        const uint16_t* srcLines = reinterpret_cast<const uint16_t*>(
-                                            reinterpret_cast<const uint64_t*>(smem + (size_t)srcTeam * Sh::TEAM_BYTES) + 3 * Sh::GRID + W);
-                                        if (!verifyCandidate<R>(p.grids + (size_t)tgt * W, srcLines, a0, a1, a2, S, T0, T1, T2))
-                                            continue;
-                                        ++cOk;
-                                        atomicMin(&p.parents[tgt], (unsigned long long)key);
-                                    }
+                                    const uint32_t* info = teamInfo(srcTeam);
+                                    int v0, v1, v2;
+                                    permutedVoxel(bv, v0, v1, v2);
+                                    for (uint32_t e = lane; e < bc; e += 32)
+                                        candidate(__ldg(&p.entries[bs + e]), v0, v1, v2, srcTeam, info[0], info[1], info[2]);
                                 }
                             }
                             if (tl == 0)
