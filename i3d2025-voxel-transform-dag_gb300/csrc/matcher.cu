@@ -41,19 +41,29 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// One step of the directional box hash, pass P (0: along the first fold axis, 1: second, 2: third).
-// The reference folds with hash_combine and clamps to 1 once started (find_translation.cpp:210-218).
-// Which hash is used does not change the result: a probe only proposes (source, target, transform)
-// candidates and every candidate is verified exactly, and verification passes precisely when the two
-// boxes agree after leading empty elements are stripped on every axis -- which makes any such hash
-// equal. The only requirements are (a) leading empty elements leave the state at zero and (b) a
-// non-empty box never hashes to zero (it would not be probed). This fold is a polynomial hash mod
-// 2^64 with an odd base per pass, and bit 0 carries "started": 0 stays 0, a non-empty box is odd.
-// It costs three integer multiply-adds and a logic op instead of the shift/add chain of hash_combine.
+// The directional box hash. The reference folds every axis with hash_combine and clamps to 1 once
+// started (find_translation.cpp:210-218). Which hash is used does not change the result: a probe only
+// proposes (source, target, transform) candidates, every candidate is verified exactly, and
+// verification passes precisely when the two boxes agree after leading empty elements are stripped
+// on every axis -- which makes any hash of that stripped form equal. The requirements are (a) leading
+// empty elements leave the state at zero and (b) a non-empty box never hashes to zero (it would not
+// be probed). Here:
+//  - pass 1 (along the first fold axis) is exact: the window of the line from the anchor to v, read
+//    as a base-2 number with the element at v as its lowest digit (leading empties add nothing), then
+//    doubled plus one if non-empty, so a non-empty window is odd;
+//  - passes 2 and 3 are a polynomial hash mod 2^64 with an odd base per pass, and bit 0 carries
+//    "started": 0 stays 0, a non-empty box stays odd. Three integer multiply-adds and a logic op.
+// Pass-1 code of `line` (bit c = element c) for the window ending at v; fromHigh: the anchor is R-1.
+__device__ __forceinline__ uint32_t lineCode(uint32_t line, int v, bool fromHigh)
+{
+    const uint32_t c = fromHigh ? (line >> v) : (__brev(line) >> (31 - v));
+    return (c << 1) | (c != 0u ? 1u : 0u);
+}
 template <int P>
 __device__ __forceinline__ uint64_t boxFold(uint64_t acc, uint64_t v)
 {
-    constexpr uint64_t K = P == 0 ? 0x9E3779B97F4A7C15ull : (P == 1 ? 0xC2B2AE3D27D4EB4Full : 0x165667B19E3779F9ull);
+    constexpr uint64_t K = P == 1 ? 0xC2B2AE3D27D4EB4Full : 0x165667B19E3779F9ull;
+    static_assert(P == 1 || P == 2, "passes 2 and 3 fold; pass 1 is lineCode");
     return (acc * K + v) | (acc & 1u);
 }
 
@@ -115,12 +125,7 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
     for (int line = lane; line < R * R; line += 32) { // line = y + R z
         const uint32_t bitOff = (uint32_t)line * R;
         const uint32_t row = (uint32_t)(g[bitOff >> 6] >> (bitOff & 63)) & rowMask;
-        uint64_t acc = 0;
-        for (int k = 0; k < R; ++k) {
-            const int x = px ? R - 1 - k : k;
-            acc = boxFold<0>(acc, (row >> x) & 1);
-        }
-        xres[warp][line] = acc;
+        xres[warp][line] = lineCode(row, px ? 0 : R - 1, px); // the whole row, ending at the far side
     }
     __syncwarp();
     uint64_t yv = 0;
@@ -375,18 +380,12 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                 // ---- pass 1 along a0 from the occupancy bits
                 if (valid) {
                     const int lo = otherLo(a0), hi = otherHi(a0);
-                    const int bs = a0 == 0 ? 1 : (a0 == 1 ? R : R * R);
-                    const int bbase = c1 * (lo == 0 ? 1 : (lo == 1 ? R : R * R)) + c2 * (hi == 1 ? R : R * R);
                     const int ss = smemStride(a0, SY, SZ);
                     const int sbase = c1 * smemStride(lo, SY, SZ) + c2 * smemStride(hi, SY, SZ);
-                    uint64_t acc = 0;
+                    const uint32_t ln = lines[a0 * R * R + tl]; // this thread's line along a0
 #pragma unroll 4
-                    for (int k = 0; k < R; ++k) {
-                        const int c = d0 ? R - 1 - k : k;
-                        const int bi = bbase + c * bs;
-                        acc = boxFold<0>(acc, (srcW[bi >> 6] >> (bi & 63)) & 1);
-                        G1[sbase + c * ss] = acc;
-                    }
+                    for (int c = 0; c < R; ++c)
+                        G1[sbase + c * ss] = lineCode(ln, c, d0);
                 }
                 __syncthreads();
                 for (int a1i = 0; a1i < 2; ++a1i) {
@@ -593,6 +592,375 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
     }
 }
 
+// ---------------------------------------------------------------------------- split search
+// The same search as searchKernel in two stages, so that neither waits on the other's latencies:
+//  1. probeKernel folds the box hashes of every (source, orientation, voxel) in shared memory, tests
+//     them against the membership filter and appends the survivors to a record list in device
+//     memory (per-warp staging in shared memory, one atomic per flush);
+//  2. lookupKernel takes one record per thread: table probe, then the candidates of a hit.
+// Record: x = box hash (salted), y = w | vidx << 32 | pid << 44 | dir << 47, with w the source's
+// index in the probed range, vidx = x + R y + R^2 z of the voxel in source coordinates, pid the axis
+// permutation 2 a0 + (a2 < a1) and dir the fold direction bits d0 | d1 << 1 | d2 << 2.
+struct ProbeParams {
+    const uint64_t* grids;
+    const uint32_t* order;
+    const uint32_t* workList; // null: the range is sorted positions
+    uint32_t begin, end; // probed range (of sorted positions or of workList)
+    const uint32_t* filter;
+    uint32_t filterShift;
+    const uint32_t* gridOf;
+    ulonglong2* recs;
+    unsigned long long* recCount; // records produced; past recCap they are counted but not stored
+    unsigned long long recCap;
+    uint16_t* srcLines; // [end - begin][3][R * R]: every source's lines, for verification
+    uint32_t* workCounter;
+    unsigned long long* counters; // [0] probes, [1] filter passes
+};
+
+template <int R>
+struct ProbeShape {
+    static constexpr int TEAM = R * R; // pass 2: thread (v0, w2); pass 3: thread (v0, v1)
+    static constexpr int TEAMS = kThreads / TEAM;
+    static constexpr int W = R * R * R / 64;
+    // G2[v0 + R v1 + PS w2]: both passes read or write R consecutive v0 per team row; for R < 16 the
+    // plane stride is padded so that the team rows of one warp fall into different banks
+    static constexpr int PS = R * R + (R < 16 ? R : 0);
+    static constexpr int STAGE = 128; // staged records per warp
+    static constexpr size_t TEAM_BYTES = (size_t)(PS * R + W) * 8 + 3 * R * R * 2; // G2, srcW, lines
+    static constexpr size_t STAGE_OFF = TEAM_BYTES * TEAMS;
+    static constexpr size_t SMEM = STAGE_OFF + (size_t)(kThreads / 32) * STAGE * 16 + 16;
+    static_assert(STAGE_OFF % 16 == 0, "stage alignment");
+};
+
+__device__ __forceinline__ int axisStride(int a, int R) { return a == 0 ? 1 : (a == 1 ? R : R * R); }
+
+template <int R>
+__global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
+{
+    using Sh = ProbeShape<R>;
+    constexpr int TEAM = Sh::TEAM, TEAMS = Sh::TEAMS, W = Sh::W, PS = Sh::PS, STAGE = Sh::STAGE;
+    constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int team = threadIdx.x / TEAM;
+    const int tl = threadIdx.x % TEAM;
+    const int tA = tl % R, tB = tl / R;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint8_t* tb = smem + (size_t)team * Sh::TEAM_BYTES;
+    uint64_t* G2 = reinterpret_cast<uint64_t*>(tb);
+    uint64_t* srcW = G2 + PS * R;
+    uint16_t* lines = reinterpret_cast<uint16_t*>(srcW + W);
+    ulonglong2* stage = reinterpret_cast<ulonglong2*>(smem + Sh::STAGE_OFF) + warp * STAGE;
+    uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::SMEM - 16);
+    uint32_t stageFill = 0; // warp-uniform
+    uint32_t cProbe = 0, cFilter = 0;
+
+    auto flushStage = [&]() {
+        if (stageFill == 0)
+            return;
+        unsigned long long g = 0;
+        if (lane == 0)
+            g = atomicAdd(p.recCount, (unsigned long long)stageFill);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        for (uint32_t i = lane; i < stageFill; i += 32)
+            if (g + i < p.recCap)
+                p.recs[g + i] = stage[i];
+        __syncwarp();
+        stageFill = 0;
+    };
+
+    for (;;) {
+        if (threadIdx.x == 0)
+            *shBase = p.begin + atomicAdd(p.workCounter, (uint32_t)TEAMS);
+        __syncthreads();
+        const uint32_t base = *shBase;
+        __syncthreads();
+        if (base >= p.end)
+            break;
+        const uint32_t wi = base + team;
+        const bool valid = wi < p.end;
+        const uint32_t wIdx = wi - p.begin;
+        uint64_t salt = 0;
+        if (valid) {
+            const uint32_t r = p.workList ? p.workList[wi] : wi;
+            const uint32_t orig = p.order[r];
+            const uint64_t* g = p.grids + (size_t)orig * W;
+            for (int k = tl; k < W; k += TEAM)
+                srcW[k] = g[k];
+            salt = p.gridOf ? boxSalt(p.gridOf[orig]) : 0ull;
+        }
+        __syncthreads();
+        if (valid) { // lines[a][u_lo + R u_hi]: the source's voxels along axis a, bit j = coordinate j
+            const uint32_t off = (uint32_t)R * (tA + R * tB); // x-line at (y, z) = (tA, tB)
+            lines[tl] = (uint16_t)((srcW[off >> 6] >> (off & 63)) & rowMask);
+            uint32_t ly = 0, lz = 0;
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const uint32_t iy = tA + R * j + R * R * tB; // (x=tA, y=j, z=tB)
+                const uint32_t iz = tA + R * tB + R * R * j; // (x=tA, y=tB, z=j)
+                ly |= (uint32_t)((srcW[iy >> 6] >> (iy & 63)) & 1) << j;
+                lz |= (uint32_t)((srcW[iz >> 6] >> (iz & 63)) & 1) << j;
+            }
+            lines[R * R + tl] = (uint16_t)ly;
+            lines[2 * R * R + tl] = (uint16_t)lz;
+        }
+        __syncthreads();
+        if (valid) {
+            uint16_t* dst = p.srcLines + (size_t)wIdx * 3 * R * R;
+            for (int k = tl; k < 3 * R * R; k += TEAM)
+                dst[k] = lines[k];
+        }
+
+        for (int a0 = 0; a0 < 3; ++a0) {
+            for (int d0 = 1; d0 >= 0; --d0) {
+                for (int a1i = 0; a1i < 2; ++a1i) {
+                    const int a1 = (a0 + 1 + a1i) % 3;
+                    const int a2 = 3 - a0 - a1;
+                    const uint32_t pid = 2 * a0 + (a2 < a1 ? 1 : 0);
+                    const int s0 = axisStride(a0, R), s1 = axisStride(a1, R), s2 = axisStride(a2, R);
+                    for (int d1 = 1; d1 >= 0; --d1) {
+                        // ---- pass 2 along a1 from the exact line codes: thread (v0, w2) = (tA, tB)
+                        if (valid) {
+                            const uint16_t* La = lines + a0 * R * R;
+                            const int sj = a1 < a2 ? 1 : R; // line index u_lo + R u_hi with u[a1] = j, u[a2] = tB
+                            const int bw = a1 < a2 ? R * tB : tB;
+                            uint64_t acc = 0;
+#pragma unroll
+                            for (int k = 0; k < R; ++k) {
+                                const int j = d1 ? R - 1 - k : k;
+                                acc = boxFold<1>(acc, lineCode(La[bw + j * sj], tA, d0));
+                                G2[tA + R * j + PS * tB] = acc;
+                            }
+                        }
+                        __syncthreads();
+                        // ---- pass 3 along a2, both directions: thread (v0, v1) = (tA, tB)
+#pragma unroll
+                        for (int d2 = 1; d2 >= 0; --d2) {
+                            uint32_t pass = 0;
+                            if (valid) {
+                                // half a line at a time: fold, then all of its filter loads in flight
+                                constexpr int H = R / 2;
+                                uint64_t acc = 0;
+                                uint32_t started = 0;
+#pragma unroll
+                                for (int h = 0; h < 2; ++h) {
+                                    uint32_t fbit[H], word[H];
+#pragma unroll
+                                    for (int kk = 0; kk < H; ++kk) {
+                                        const int k = h * H + kk;
+                                        const int w = d2 ? R - 1 - k : k;
+                                        acc = boxFold<2>(acc, G2[tA + R * tB + PS * w]);
+                                        started |= (uint32_t)(acc & 1u) << w;
+                                        fbit[kk] = filterHash(acc ^ salt) >> p.filterShift;
+                                    }
+#pragma unroll
+                                    for (int kk = 0; kk < H; ++kk) {
+                                        const int k = h * H + kk;
+                                        const int w = d2 ? R - 1 - k : k;
+                                        word[kk] = ((started >> w) & 1u) ? __ldg(&p.filter[fbit[kk] >> 5]) : 0u;
+                                    }
+#pragma unroll
+                                    for (int kk = 0; kk < H; ++kk) {
+                                        const int k = h * H + kk;
+                                        const int w = d2 ? R - 1 - k : k;
+                                        pass |= ((word[kk] >> (fbit[kk] & 31)) & 1u) << w;
+                                    }
+                                }
+                                cProbe += __popc(started);
+                            }
+                            // ---- append the survivors (warp-aggregated)
+                            const uint32_t np = __popc(pass);
+                            cFilter += np;
+                            uint32_t incl = np;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                                if ((int)lane >= o)
+                                    incl += t;
+                            }
+                            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                            if (total != 0) {
+                                if (stageFill + total > (uint32_t)STAGE)
+                                    flushStage();
+                                const bool direct = total > (uint32_t)STAGE;
+                                unsigned long long g = 0;
+                                if (direct) { // more than a stage: straight to device memory
+                                    if (lane == 0)
+                                        g = atomicAdd(p.recCount, (unsigned long long)total);
+                                    g = __shfl_sync(0xffffffffu, g, 0);
+                                }
+                                if (pass) { // re-fold the line to recover the survivors' hashes
+                                    const uint64_t meta = (uint64_t)wIdx | ((uint64_t)pid << 44)
+                                        | ((uint64_t)((uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2)) << 47);
+                                    uint32_t o = stageFill + incl - np;
+                                    uint64_t acc = 0;
+#pragma unroll 1
+                                    for (int k = 0; k < R; ++k) {
+                                        const int w = d2 ? R - 1 - k : k;
+                                        acc = boxFold<2>(acc, G2[tA + R * tB + PS * w]);
+                                        if ((pass >> w) & 1u) {
+                                            const uint32_t vidx = (uint32_t)(tA * s0 + tB * s1 + w * s2);
+                                            const ulonglong2 rec = make_ulonglong2(acc ^ salt, meta | ((uint64_t)vidx << 32));
+                                            if (!direct)
+                                                stage[o] = rec;
+                                            else if (g + (o - stageFill) < p.recCap)
+                                                p.recs[g + (o - stageFill)] = rec;
+                                            ++o;
+                                        }
+                                    }
+                                }
+                                if (!direct)
+                                    stageFill += total;
+                                __syncwarp();
+                            }
+                        }
+                        __syncthreads(); // the next pass 2 rewrites G2
+                    }
+                }
+            }
+        }
+    }
+    flushStage();
+    const uint32_t vals[2] = { cProbe, cFilter };
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        unsigned long long v = vals[k];
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v)
+            atomicAdd(&p.counters[k], v);
+    }
+}
+
+struct LookupParams {
+    const ulonglong2* recs;
+    unsigned long long count;
+    const ulonglong2* slots;
+    uint32_t capMask;
+    const uint32_t* entries;
+    const uint64_t* grids;
+    const uint32_t* order;
+    const uint32_t* workList;
+    uint32_t begin; // the probed range's first position
+    const uint16_t* srcLines;
+    unsigned long long* parents;
+    const uint32_t* gridOf;
+    const uint32_t* segOff;
+    uint32_t allowSym, allowPerm, allowTrans;
+    unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified
+};
+
+template <int R, int L>
+__global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t start = 0, cnt = 0;
+    uint64_t meta = 0;
+    if (i < p.count) {
+        const ulonglong2 rec = p.recs[i];
+        meta = rec.y;
+        uint32_t slot = slotHash(rec.x) & p.capMask;
+        for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
+            const ulonglong2 sv = p.slots[slot];
+            if (sv.x == rec.x) {
+                start = (uint32_t)sv.y;
+                cnt = (uint32_t)(sv.y >> 32);
+                break;
+            }
+            if (sv.x == 0)
+                break;
+            slot = (slot + 1) & p.capMask;
+        }
+    }
+    uint32_t cHit = cnt ? 1u : 0u, cCand = 0, cVer = 0, cOk = 0;
+
+    // every candidate (target, corner) of the hit recorded in `m` (find_translation.cpp:820-864)
+    struct Src {
+        uint32_t rSrc, tLo, tHi;
+        const uint16_t* lines;
+        int a0, a1, a2, v0, v1, v2, an0, an1, an2;
+        uint32_t pid, dir;
+    };
+    auto source = [&](uint64_t m) {
+        Src s;
+        const uint32_t w = (uint32_t)m;
+        const uint32_t vidx = (uint32_t)(m >> 32) & 0xFFFu;
+        s.pid = (uint32_t)(m >> 44) & 7u;
+        s.dir = (uint32_t)(m >> 47) & 7u;
+        const uint32_t r = p.workList ? p.workList[p.begin + w] : p.begin + w;
+        const uint32_t g = p.gridOf ? p.gridOf[p.order[r]] : 0u;
+        s.rSrc = p.segOff ? r - p.segOff[g] : r;
+        s.tLo = p.segOff ? p.segOff[g] : 0u;
+        s.tHi = p.segOff ? p.segOff[g + 1] : 0xFFFFFFFFu;
+        s.lines = p.srcLines + (size_t)w * 3 * R * R;
+        s.a0 = (int)(s.pid >> 1);
+        const int lo = otherLo(s.a0), hi = otherHi(s.a0);
+        s.a1 = (s.pid & 1) ? hi : lo;
+        s.a2 = (s.pid & 1) ? lo : hi;
+        const int ux = (int)(vidx % R), uy = (int)((vidx / R) % R), uz = (int)(vidx / (R * R));
+        s.v0 = s.a0 == 0 ? ux : (s.a0 == 1 ? uy : uz);
+        s.v1 = s.a1 == 0 ? ux : (s.a1 == 1 ? uy : uz);
+        s.v2 = s.a2 == 0 ? ux : (s.a2 == 1 ? uy : uz);
+        s.an0 = (s.dir & 1) ? 0 : R - 1;
+        s.an1 = (s.dir & 2) ? 0 : R - 1;
+        s.an2 = (s.dir & 4) ? 0 : R - 1;
+        return s;
+    };
+    auto candidate = [&](uint32_t pay, const Src& s) {
+        const uint32_t tgt = pay >> 3;
+        const uint32_t S = s.dir ^ (pay & 7);
+        ++cCand;
+        if (tgt < s.tLo || tgt >= s.tHi) // another grid of the batch
+            return;
+        const int T0 = (S & 1) ? s.v0 - s.an0 : s.an0 - s.v0;
+        const int T1 = (S & 2) ? s.v1 - s.an1 : s.an1 - s.v1;
+        const int T2 = (S & 4) ? s.v2 - s.an2 : s.an2 - s.v2;
+        if (!p.allowPerm && s.pid != 0)
+            return;
+        if (!p.allowSym && S != 0)
+            return;
+        if (!p.allowTrans && (T0 | T1 | T2) != 0)
+            return;
+        const uint64_t key = encodeFixed64(s.rSrc, s.pid, S, T0, T1, T2, L);
+        const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
+        if (key >= cur)
+            return;
+        ++cVer;
+        if (!verifyCandidate<R>(p.grids + (size_t)tgt * (R * R * R / 64), s.lines, s.a0, s.a1, s.a2, S, T0, T1, T2))
+            return;
+        ++cOk;
+        atomicMin(&p.parents[tgt], (unsigned long long)key);
+    };
+    // short ranges: every lane walks its own hit's candidates
+    constexpr uint32_t kSerialMax = 8;
+    if (cnt != 0 && cnt <= kSerialMax) {
+        const Src s = source(meta);
+        for (uint32_t e = 0; e < cnt; ++e)
+            candidate(__ldg(&p.entries[start + e]), s);
+    }
+    // long ranges: the warp walks one range at a time
+    uint32_t hitMask = __ballot_sync(0xffffffffu, cnt > kSerialMax);
+    while (hitMask) {
+        const int src = __ffs(hitMask) - 1;
+        hitMask &= hitMask - 1;
+        const uint32_t bs = __shfl_sync(0xffffffffu, start, src);
+        const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
+        const uint64_t bm = __shfl_sync(0xffffffffu, meta, src);
+        const Src s = source(bm);
+        for (uint32_t e = lane; e < bc; e += 32)
+            candidate(__ldg(&p.entries[bs + e]), s);
+    }
+    const uint32_t vals[4] = { cHit, cCand, cVer, cOk };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        unsigned long long v = vals[k];
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v)
+            atomicAdd(&p.counters[2 + k], v);
+    }
+}
+
 // ---------------------------------------------------------------------------- resolve
 __global__ void decodeParentsKernel(const unsigned long long* __restrict__ parents, uint32_t n, const uint32_t* __restrict__ order, uint64_t sentinelKey,
     uint32_t level, uint64_t* __restrict__ parentTP, uint32_t* __restrict__ isUnique, const uint32_t* __restrict__ gridOf = nullptr,
@@ -727,14 +1095,18 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<unsigned long long> counters(8, s);
     TDAG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, s));
 
-    const size_t smem = SearchShape<R>::SMEM;
-    TDAG_CUDA(cudaFuncSetAttribute(searchKernel<R, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = ProbeShape<R>::SMEM;
+    TDAG_CUDA(cudaFuncSetAttribute(probeKernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int perSM = 0;
-    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, searchKernel<R, L>, kThreads, smem));
+    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, probeKernel<R>, kThreads, smem));
     if (ctx.tuning.search_ctas_per_sm)
         perSM = std::min<int>(perSM, (int)ctx.tuning.search_ctas_per_sm);
     perSM = std::max(perSM, 1);
     const uint32_t maxBlocks = (uint32_t)ctx.numSMs * perSM;
+    // survivor records: at most a quarter of the free device memory per probed range
+    size_t freeBytes = 0, totalBytes = 0;
+    TDAG_CUDA(cudaMemGetInfo(&freeBytes, &totalBytes));
+    const uint64_t maxRecords = std::max<uint64_t>(1u << 20, freeBytes / 4 / sizeof(ulonglong2));
 
     // Source batches. Single grid: doubling ranges of sorted positions, starting at a few waves of
     // teams. Batch: the same fractions of every grid (1/256, 1/128, ..., 1/2, 1), as a list of sorted
@@ -743,7 +1115,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     std::vector<uint32_t> workList;
     std::vector<std::vector<unsigned long long>> minKeys; // per batch, per grid
     if (!batched) {
-        const uint32_t minBatch = std::max<uint32_t>(maxBlocks * SearchShape<R>::TEAMS * 2, n / 256);
+        const uint32_t minBatch = std::max<uint32_t>(maxBlocks * ProbeShape<R>::TEAMS * 2, n / 256);
         while (bounds.back() < n) {
             const uint32_t b = bounds.back();
             bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 2ull * b)));
@@ -777,6 +1149,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
     DevBuf<uint64_t> k2(m, s);
     DevBuf<uint32_t> p2(m, s);
+    uint32_t maxBatch = 1;
+    for (size_t bi = 0; bi + 1 < bounds.size(); ++bi)
+        maxBatch = std::max(maxBatch, bounds[bi + 1] - bounds[bi]);
+    DevBuf<uint16_t> srcLines((size_t)maxBatch * 3 * R * R, s);
+    DevBuf<ulonglong2> recs;
+    DevBuf<unsigned long long> recCount(1, s);
+    double recsPerSource = R * R * 2.0; // first estimate; then a running average of the probed ranges
+    unsigned long long probeCounts[2] = { 0, 0 }; // probes and filter passes before the current range
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi) {
         const uint32_t b0 = bounds[bi], b1 = bounds[bi + 1];
         if (b0 == b1)
@@ -798,31 +1178,78 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             TDAG_LAUNCHED();
             buildTable(ctx, k2.get(), p2.get(), live, table);
         }
-        SearchParams sp {};
-        sp.grids = grids;
-        sp.order = order.get();
-        sp.begin = b0;
-        sp.end = b1;
-        sp.slots = table.slots.get();
-        sp.capMask = table.capMask;
-        sp.entries = table.entries.get();
-        sp.filter = table.filter.get();
-        sp.filterShift = table.filterShift;
-        sp.parents = parents.get();
-        sp.workCounter = work.get();
-        sp.counters = counters.get();
-        sp.allowSym = cfg.symmetry ? 1 : 0;
-        sp.allowPerm = cfg.axis_permutation ? 1 : 0;
-        sp.allowTrans = cfg.translation ? 1 : 0;
-        sp.gridOf = gridOf;
-        sp.segOff = segOff;
-        sp.workList = batched ? workListDev.get() : nullptr;
-        TDAG_CUDA(cudaMemsetAsync(work.get(), 0, 4, s));
-        const uint64_t groups = ((uint64_t)(b1 - b0) + SearchShape<R>::TEAMS - 1) / SearchShape<R>::TEAMS;
-        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
+        ProbeParams pp {};
+        pp.grids = grids;
+        pp.order = order.get();
+        pp.workList = batched ? workListDev.get() : nullptr;
+        pp.filter = table.filter.get();
+        pp.filterShift = table.filterShift;
+        pp.gridOf = gridOf;
+        pp.recCount = recCount.get();
+        pp.workCounter = work.get();
+        pp.counters = counters.get();
+        LookupParams lp {};
+        lp.slots = table.slots.get();
+        lp.capMask = table.capMask;
+        lp.entries = table.entries.get();
+        lp.grids = grids;
+        lp.order = order.get();
+        lp.workList = pp.workList;
+        lp.parents = parents.get();
+        lp.gridOf = gridOf;
+        lp.segOff = segOff;
+        lp.allowSym = cfg.symmetry ? 1 : 0;
+        lp.allowPerm = cfg.axis_permutation ? 1 : 0;
+        lp.allowTrans = cfg.translation ? 1 : 0;
+        lp.counters = counters.get();
         TDAG_CUDA(cudaEventRecord(ctx.ev[0], s));
-        searchKernel<R, L><<<blocks, kThreads, smem, s>>>(sp);
-        TDAG_LAUNCHED();
+        // Probe ranges of the batch sized so that their records fit; a range whose records overflow
+        // the buffer is probed again after the buffer grew to the exact count (or, past the memory
+        // limit, as two halves).
+        for (uint32_t pos = b0; pos < b1;) {
+            uint32_t cs = (uint32_t)std::min<uint64_t>(b1 - pos, std::max<uint64_t>(1, (uint64_t)((double)maxRecords / (recsPerSource * 1.25 + 1.0))));
+            unsigned long long produced = 0;
+            for (;;) {
+                const uint64_t want = std::min<uint64_t>(maxRecords, (uint64_t)((double)cs * recsPerSource * 1.25) + 4096);
+                if (recs.n < want)
+                    recs = DevBuf<ulonglong2>(want, s);
+                pp.recs = recs.get();
+                pp.recCap = recs.n;
+                pp.begin = pos;
+                pp.end = pos + cs;
+                pp.srcLines = srcLines.get();
+                TDAG_CUDA(cudaMemsetAsync(work.get(), 0, 4, s));
+                TDAG_CUDA(cudaMemsetAsync(recCount.get(), 0, 8, s));
+                const uint64_t groups = ((uint64_t)cs + ProbeShape<R>::TEAMS - 1) / ProbeShape<R>::TEAMS;
+                const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
+                probeKernel<R><<<blocks, kThreads, smem, s>>>(pp);
+                TDAG_LAUNCHED();
+                TDAG_CUDA(cudaMemcpyAsync(&produced, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
+                TDAG_CUDA(cudaStreamSynchronize(s));
+                if (produced <= pp.recCap)
+                    break;
+                // the discarded run's probe and filter counts are rolled back
+                TDAG_CUDA(cudaMemcpyAsync(counters.get(), probeCounts, 16, cudaMemcpyHostToDevice, s));
+                if (produced <= maxRecords) {
+                    recsPerSource = std::max(recsPerSource, (double)produced / cs);
+                    recs = DevBuf<ulonglong2>(produced, s);
+                } else {
+                    TDAG_CHECK(cs > 1, TDAG_ERR_OOM, "one source produced more probe records than fit in device memory");
+                    cs = (cs + 1) / 2;
+                }
+            }
+            TDAG_CUDA(cudaMemcpyAsync(probeCounts, counters.get(), 16, cudaMemcpyDeviceToHost, s));
+            recsPerSource = 0.5 * recsPerSource + 0.5 * ((double)produced / cs);
+            if (produced) {
+                lp.recs = recs.get();
+                lp.count = produced;
+                lp.begin = pos;
+                lp.srcLines = srcLines.get();
+                lookupKernel<R, L><<<(unsigned)((produced + kThreads - 1) / kThreads), kThreads, 0, s>>>(lp);
+                TDAG_LAUNCHED();
+            }
+            pos += cs;
+        }
         TDAG_CUDA(cudaEventRecord(ctx.ev[1], s));
         TDAG_CUDA(cudaEventSynchronize(ctx.ev[1]));
         float ms = 0;
