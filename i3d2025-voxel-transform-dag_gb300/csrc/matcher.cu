@@ -76,13 +76,11 @@ __host__ __device__ __forceinline__ uint32_t slotHash(uint64_t k)
     h ^= h >> 13;
     return h;
 }
-__host__ __device__ __forceinline__ uint32_t filterHash(uint64_t k)
-{
-    uint32_t h = ((uint32_t)k ^ (uint32_t)(k >> 32)) * 0x9E3779B1u;
-    h ^= h >> 16;
-    h *= 0x7FEB352Du;
-    return h;
-}
+// Membership filter: a blocked Bloom filter, two bits of one 32-bit word per key (filterShift =
+// 32 - log2(filter bits), so the word index is the top log2(bits) - 5 bits of a multiplicative hash).
+__host__ __device__ __forceinline__ uint32_t filterFold(uint64_t k) { return (uint32_t)k ^ (uint32_t)(k >> 32); }
+__host__ __device__ __forceinline__ uint32_t filterWordIndex(uint32_t x, uint32_t filterShift) { return (x * 0x9E3779B1u) >> (filterShift + 5); }
+__host__ __device__ __forceinline__ uint32_t filterBits(uint32_t x) { return (1u << (x & 31u)) | (1u << ((x >> 5) & 31u)); }
 
 // Per-grid salt of the box hashes of a batch member: even, so a salted non-empty box hash stays odd
 // and never collides with the empty-slot key 0; 0 for a single grid, leaving the key unchanged.
@@ -205,8 +203,8 @@ __global__ void tableRangesKernel(ulonglong2* __restrict__ slots, const uint32_t
     const uint64_t key = slots[s].x;
     slots[s].y = (uint64_t)tstart[s] | ((uint64_t)tcount[s] << 32);
     if (key != 0) {
-        const uint32_t fb = filterHash(key) >> filterShift;
-        atomicOr(&filter[fb >> 5], 1u << (fb & 31));
+        const uint32_t x = filterFold(key);
+        atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
     }
 }
 
@@ -421,25 +419,26 @@ __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
                                 // before the first one is consumed
                                 uint64_t acc = 0;
                                 uint32_t started = 0;
-                                uint32_t fbit[R];
+                                uint32_t fx[R];
 #pragma unroll
                                 for (int k = 0; k < R; ++k) {
                                     const int c = d2 ? R - 1 - k : k;
                                     acc = boxFold<2>(acc, G2[sbase3 + c * ss3]);
                                     G3[sbase3 + c * ss3] = acc;
                                     started |= (uint32_t)(acc & 1u) << c;
-                                    fbit[k] = filterHash(acc ^ salt) >> p.filterShift;
+                                    fx[k] = filterFold(acc ^ salt);
                                 }
                                 uint32_t word[R];
 #pragma unroll
                                 for (int k = 0; k < R; ++k) {
                                     const int c = d2 ? R - 1 - k : k;
-                                    word[k] = ((started >> c) & 1u) ? __ldg(&p.filter[fbit[k] >> 5]) : 0u;
+                                    word[k] = ((started >> c) & 1u) ? __ldg(&p.filter[filterWordIndex(fx[k], p.filterShift)]) : 0u;
                                 }
 #pragma unroll
                                 for (int k = 0; k < R; ++k) {
                                     const int c = d2 ? R - 1 - k : k;
-                                    pass |= ((word[k] >> (fbit[k] & 31)) & 1u) << c;
+                                    const uint32_t bits = filterBits(fx[k]);
+                                    pass |= ((word[k] & bits) == bits ? 1u : 0u) << c;
                                 }
                                 cProbe += __popc(started);
                             }
@@ -619,53 +618,102 @@ struct ProbeParams {
 
 template <int R>
 struct ProbeShape {
-    static constexpr int TEAM = R * R; // pass 2: thread (v0, w2); pass 3: thread (v0, v1)
+    static constexpr int TEAM = R * R; // pass 2: thread per (v0, w2); pass 3: thread per (v0, v1)
     static constexpr int TEAMS = kThreads / TEAM;
     static constexpr int W = R * R * R / 64;
-    // G2[v0 + R v1 + PS w2]: both passes read or write R consecutive v0 per team row; for R < 16 the
-    // plane stride is padded so that the team rows of one warp fall into different banks
+    // G2[v0 + R v1 + PS w2]: both passes read or write runs of consecutive v0 per team row; for R < 16
+    // the plane stride is padded so that the team rows of one warp fall into different banks
     static constexpr int PS = R * R + (R < 16 ? R : 0);
-    static constexpr int STAGE = 128; // staged records per warp
-    static constexpr size_t TEAM_BYTES = (size_t)(PS * R + W) * 8 + 3 * R * R * 2; // G2, srcW, lines
+    static constexpr int CHUNK = 4; // pass-3 elements whose filter loads are in flight together
+    static constexpr int STAGE = 96; // staged records per warp (four CTAs of R = 16 fit an SM)
+    static constexpr int FLUSH = STAGE / 2; // a warp flushes once this many are staged
+    // per team: G2 (u64), srcW (u64), lines[3][R*R] and linesT[3][R*R] (u16)
+    static constexpr size_t LINES_OFF = (size_t)(PS * R + W) * 8;
+    static constexpr size_t TEAM_BYTES = LINES_OFF + 6 * R * R * 2;
     static constexpr size_t STAGE_OFF = TEAM_BYTES * TEAMS;
-    static constexpr size_t SMEM = STAGE_OFF + (size_t)(kThreads / 32) * STAGE * 16 + 16;
-    static_assert(STAGE_OFF % 16 == 0, "stage alignment");
+    static constexpr size_t COUNT_OFF = STAGE_OFF + (size_t)(kThreads / 32) * STAGE * 16; // per-warp stage counts
+    static constexpr size_t BOX_OFF = COUNT_OFF + (kThreads / 32) * 4; // per team: lo x y z, hi + 1 x y z
+    static constexpr size_t SMEM = BOX_OFF + TEAMS * 24 + 16;
+    static_assert(STAGE_OFF % 16 == 0 && TEAM_BYTES % 8 == 0, "alignment");
+    static_assert(R == 4 || LINES_OFF % 16 == 0, "pass-2 rows are read as 16-byte vectors");
+    static_assert(R % CHUNK == 0, "chunks tile a line");
 };
 
 __device__ __forceinline__ int axisStride(int a, int R) { return a == 0 ? 1 : (a == 1 ? R : R * R); }
 
+// The R line codes of one pass-2 row (R consecutive u16, 8-byte aligned for R = 4, else 16-byte),
+// two per word.
 template <int R>
-__global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
+__device__ __forceinline__ void loadRow(const uint16_t* row, uint32_t (&lv)[R / 2])
+{
+    if constexpr (R == 4) {
+        const uint2 v = *reinterpret_cast<const uint2*>(row);
+        lv[0] = v.x;
+        lv[1] = v.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < R / 8; ++q) {
+            const uint4 v = reinterpret_cast<const uint4*>(row)[q];
+            lv[4 * q] = v.x;
+            lv[4 * q + 1] = v.y;
+            lv[4 * q + 2] = v.z;
+            lv[4 * q + 3] = v.w;
+        }
+    }
+}
+
+// Only boxes that hold a voxel are probed. With the source's bounding box [lo, hi] per axis, the box
+// from the anchor to v is empty unless v is past the box's start on every axis (v >= lo when folding
+// up from 0, v <= hi when folding down from R-1). A team therefore runs pass 2 on the (v0, w2) pairs
+// with v0 past the start along a0 and w2 in [lo, hi] along a2, and pass 3 on the (v0, v1) pairs past
+// the start along a0 and a1, folding each line from its first plane that can be non-empty (rounded
+// down to a chunk; the skipped elements hash to 0, exactly as if they had been folded). Planes along
+// a2 outside [lo, hi] are empty and read as 0. SALTED: batch members' keys carry their grid salt.
+template <int R, bool SALTED>
+__global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
 {
     using Sh = ProbeShape<R>;
-    constexpr int TEAM = Sh::TEAM, TEAMS = Sh::TEAMS, W = Sh::W, PS = Sh::PS, STAGE = Sh::STAGE;
+    constexpr int TEAM = Sh::TEAM, TEAMS = Sh::TEAMS, W = Sh::W, PS = Sh::PS, STAGE = Sh::STAGE, C = Sh::CHUNK;
     constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
     extern __shared__ __align__(16) uint8_t smem[];
     const int team = threadIdx.x / TEAM;
     const int tl = threadIdx.x % TEAM;
-    const int tA = tl % R, tB = tl / R;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint8_t* tb = smem + (size_t)team * Sh::TEAM_BYTES;
     uint64_t* G2 = reinterpret_cast<uint64_t*>(tb);
     uint64_t* srcW = G2 + PS * R;
-    uint16_t* lines = reinterpret_cast<uint16_t*>(srcW + W);
+    uint16_t* lines = reinterpret_cast<uint16_t*>(tb + Sh::LINES_OFF); // [a][u_lo + R u_hi]
+    uint16_t* linesT = lines + 3 * R * R; // [a][u_hi + R u_lo]
     ulonglong2* stage = reinterpret_cast<ulonglong2*>(smem + Sh::STAGE_OFF) + warp * STAGE;
+    uint32_t* stageCnt = reinterpret_cast<uint32_t*>(smem + Sh::COUNT_OFF) + warp;
+    uint32_t* box = reinterpret_cast<uint32_t*>(smem + Sh::BOX_OFF) + team * 6;
     uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::SMEM - 16);
-    uint32_t stageFill = 0; // warp-uniform
+    // lanes of this thread's team within its warp (teams of 16 share a warp)
+    const unsigned teamMask = TEAM >= 32 ? 0xffffffffu : (((1u << TEAM) - 1u) << (lane & ~(uint32_t)(TEAM - 1)));
     uint32_t cProbe = 0, cFilter = 0;
+    if (lane == 0)
+        *stageCnt = 0;
+    __syncwarp();
 
-    auto flushStage = [&]() {
-        if (stageFill == 0)
+    // Warp-uniform: copy the staged records (at most STAGE; reservations past it were written
+    // directly by their lanes) to the record list.
+    auto flushStage = [&](uint32_t minCount) {
+        __syncwarp();
+        const uint32_t cnt = *reinterpret_cast<volatile uint32_t*>(stageCnt);
+        if (cnt < minCount || cnt == 0)
             return;
+        const uint32_t nrec = cnt < (uint32_t)STAGE ? cnt : (uint32_t)STAGE;
         unsigned long long g = 0;
         if (lane == 0)
-            g = atomicAdd(p.recCount, (unsigned long long)stageFill);
+            g = atomicAdd(p.recCount, (unsigned long long)nrec);
         g = __shfl_sync(0xffffffffu, g, 0);
-        for (uint32_t i = lane; i < stageFill; i += 32)
+        for (uint32_t i = lane; i < nrec; i += 32)
             if (g + i < p.recCap)
                 p.recs[g + i] = stage[i];
         __syncwarp();
-        stageFill = 0;
+        if (lane == 0)
+            *stageCnt = 0;
+        __syncwarp();
     };
 
     for (;;) {
@@ -686,12 +734,18 @@ __global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
             const uint64_t* g = p.grids + (size_t)orig * W;
             for (int k = tl; k < W; k += TEAM)
                 srcW[k] = g[k];
-            salt = p.gridOf ? boxSalt(p.gridOf[orig]) : 0ull;
+            if (SALTED)
+                salt = boxSalt(p.gridOf[orig]);
+        }
+        if (tl == 0) {
+            box[0] = box[1] = box[2] = R;
+            box[3] = box[4] = box[5] = 0;
         }
         __syncthreads();
         if (valid) { // lines[a][u_lo + R u_hi]: the source's voxels along axis a, bit j = coordinate j
+            const int tA = tl % R, tB = tl / R;
             const uint32_t off = (uint32_t)R * (tA + R * tB); // x-line at (y, z) = (tA, tB)
-            lines[tl] = (uint16_t)((srcW[off >> 6] >> (off & 63)) & rowMask);
+            const uint32_t lx = (uint32_t)(srcW[off >> 6] >> (off & 63)) & rowMask;
             uint32_t ly = 0, lz = 0;
 #pragma unroll
             for (int j = 0; j < R; ++j) {
@@ -700,8 +754,24 @@ __global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
                 ly |= (uint32_t)((srcW[iy >> 6] >> (iy & 63)) & 1) << j;
                 lz |= (uint32_t)((srcW[iz >> 6] >> (iz & 63)) & 1) << j;
             }
+            lines[tl] = (uint16_t)lx;
             lines[R * R + tl] = (uint16_t)ly;
             lines[2 * R * R + tl] = (uint16_t)lz;
+            const int tt = tB + R * tA;
+            linesT[tt] = (uint16_t)lx;
+            linesT[R * R + tt] = (uint16_t)ly;
+            linesT[2 * R * R + tt] = (uint16_t)lz;
+            // bounding box: lowest set coordinate and highest + 1 along every axis
+            const uint32_t l3[3] = { lx, ly, lz };
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const uint32_t lo = __reduce_min_sync(teamMask, l3[a] ? (uint32_t)(__ffs(l3[a]) - 1) : (uint32_t)R);
+                const uint32_t hi = __reduce_max_sync(teamMask, l3[a] ? (uint32_t)(32 - __clz(l3[a])) : 0u);
+                if ((lane & (uint32_t)(TEAM >= 32 ? 31 : TEAM - 1)) == 0) {
+                    atomicMin(&box[a], lo);
+                    atomicMax(&box[3 + a], hi);
+                }
+            }
         }
         __syncthreads();
         if (valid) {
@@ -709,109 +779,104 @@ __global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
             for (int k = tl; k < 3 * R * R; k += TEAM)
                 dst[k] = lines[k];
         }
+        const int lo[3] = { (int)box[0], (int)box[1], (int)box[2] };
+        const int hi[3] = { (int)box[3] - 1, (int)box[4] - 1, (int)box[5] - 1 };
+        auto loOf = [&](int a) { return a == 0 ? lo[0] : (a == 1 ? lo[1] : lo[2]); };
+        auto hiOf = [&](int a) { return a == 0 ? hi[0] : (a == 1 ? hi[1] : hi[2]); };
 
         for (int a0 = 0; a0 < 3; ++a0) {
             for (int d0 = 1; d0 >= 0; --d0) {
+                // active v0: the window along a0 ending at v0 holds a voxel
+                const int v0s = d0 ? 0 : loOf(a0);
+                const int n0 = d0 ? hiOf(a0) + 1 : R - loOf(a0);
+                const int r0 = n0 > 0 ? tl % n0 : 0, q0 = n0 > 0 ? tl / n0 : R;
+                const int v0 = v0s + r0;
                 for (int a1i = 0; a1i < 2; ++a1i) {
                     const int a1 = (a0 + 1 + a1i) % 3;
                     const int a2 = 3 - a0 - a1;
                     const uint32_t pid = 2 * a0 + (a2 < a1 ? 1 : 0);
                     const int s0 = axisStride(a0, R), s1 = axisStride(a1, R), s2 = axisStride(a2, R);
+                    const int lo2 = loOf(a2), hi2 = hiOf(a2);
                     for (int d1 = 1; d1 >= 0; --d1) {
-                        // ---- pass 2 along a1 from the exact line codes: thread (v0, w2) = (tA, tB)
-                        if (valid) {
-                            const uint16_t* La = lines + a0 * R * R;
-                            const int sj = a1 < a2 ? 1 : R; // line index u_lo + R u_hi with u[a1] = j, u[a2] = tB
-                            const int bw = a1 < a2 ? R * tB : tB;
+                        // ---- pass 2 along a1 from the exact line codes, thread (v0, w2 = lo2 + q0);
+                        // the row holds the lines along a0 at u[a1] = j, u[a2] = w2, for every j
+                        if (valid && q0 <= hi2 - lo2) {
+                            const int w2 = lo2 + q0;
+                            uint32_t lv[R / 2];
+                            loadRow<R>((a1 < a2 ? lines : linesT) + a0 * R * R + R * w2, lv);
                             uint64_t acc = 0;
 #pragma unroll
                             for (int k = 0; k < R; ++k) {
                                 const int j = d1 ? R - 1 - k : k;
-                                acc = boxFold<1>(acc, lineCode(La[bw + j * sj], tA, d0));
-                                G2[tA + R * j + PS * tB] = acc;
+                                const uint32_t ln = (lv[j >> 1] >> ((j & 1) * 16)) & 0xFFFFu;
+                                acc = boxFold<1>(acc, lineCode(ln, v0, d0));
+                                G2[v0 + R * j + PS * w2] = acc;
                             }
                         }
                         __syncthreads();
-                        // ---- pass 3 along a2, both directions: thread (v0, v1) = (tA, tB)
+                        // ---- pass 3 along a2, both directions, thread (v0, v1 = v1s + q0)
+                        const int v1s = d1 ? 0 : loOf(a1);
+                        const int n1 = d1 ? hiOf(a1) + 1 : R - loOf(a1);
+                        const bool act3 = valid && q0 < n1;
+                        const int v1 = v1s + q0;
+                        const uint64_t* line3 = G2 + v0 + R * v1;
 #pragma unroll
                         for (int d2 = 1; d2 >= 0; --d2) {
-                            uint32_t pass = 0;
-                            if (valid) {
-                                // half a line at a time: fold, then all of its filter loads in flight
-                                constexpr int H = R / 2;
+                            if (act3) {
+                                const uint64_t meta = (uint64_t)wIdx | ((uint64_t)pid << 44)
+                                    | ((uint64_t)((uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2)) << 47);
+                                const int k0 = d2 ? R - 1 - hi2 : lo2; // fold index of the first plane that can hold a voxel
                                 uint64_t acc = 0;
-                                uint32_t started = 0;
-#pragma unroll
-                                for (int h = 0; h < 2; ++h) {
-                                    uint32_t fbit[H], word[H];
-#pragma unroll
-                                    for (int kk = 0; kk < H; ++kk) {
-                                        const int k = h * H + kk;
-                                        const int w = d2 ? R - 1 - k : k;
-                                        acc = boxFold<2>(acc, G2[tA + R * tB + PS * w]);
-                                        started |= (uint32_t)(acc & 1u) << w;
-                                        fbit[kk] = filterHash(acc ^ salt) >> p.filterShift;
-                                    }
-#pragma unroll
-                                    for (int kk = 0; kk < H; ++kk) {
-                                        const int k = h * H + kk;
-                                        const int w = d2 ? R - 1 - k : k;
-                                        word[kk] = ((started >> w) & 1u) ? __ldg(&p.filter[fbit[kk] >> 5]) : 0u;
-                                    }
-#pragma unroll
-                                    for (int kk = 0; kk < H; ++kk) {
-                                        const int k = h * H + kk;
-                                        const int w = d2 ? R - 1 - k : k;
-                                        pass |= ((word[kk] >> (fbit[kk] & 31)) & 1u) << w;
-                                    }
-                                }
-                                cProbe += __popc(started);
-                            }
-                            // ---- append the survivors (warp-aggregated)
-                            const uint32_t np = __popc(pass);
-                            cFilter += np;
-                            uint32_t incl = np;
-#pragma unroll
-                            for (int o = 1; o < 32; o <<= 1) {
-                                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                                if ((int)lane >= o)
-                                    incl += t;
-                            }
-                            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                            if (total != 0) {
-                                if (stageFill + total > (uint32_t)STAGE)
-                                    flushStage();
-                                const bool direct = total > (uint32_t)STAGE;
-                                unsigned long long g = 0;
-                                if (direct) { // more than a stage: straight to device memory
-                                    if (lane == 0)
-                                        g = atomicAdd(p.recCount, (unsigned long long)total);
-                                    g = __shfl_sync(0xffffffffu, g, 0);
-                                }
-                                if (pass) { // re-fold the line to recover the survivors' hashes
-                                    const uint64_t meta = (uint64_t)wIdx | ((uint64_t)pid << 44)
-                                        | ((uint64_t)((uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2)) << 47);
-                                    uint32_t o = stageFill + incl - np;
-                                    uint64_t acc = 0;
 #pragma unroll 1
-                                    for (int k = 0; k < R; ++k) {
-                                        const int w = d2 ? R - 1 - k : k;
-                                        acc = boxFold<2>(acc, G2[tA + R * tB + PS * w]);
-                                        if ((pass >> w) & 1u) {
-                                            const uint32_t vidx = (uint32_t)(tA * s0 + tB * s1 + w * s2);
-                                            const ulonglong2 rec = make_ulonglong2(acc ^ salt, meta | ((uint64_t)vidx << 32));
-                                            if (!direct)
-                                                stage[o] = rec;
-                                            else if (g + (o - stageFill) < p.recCap)
-                                                p.recs[g + (o - stageFill)] = rec;
-                                            ++o;
+                                for (int kq = k0 & ~(C - 1); kq < R; kq += C) {
+                                    uint64_t key[C];
+                                    uint32_t word[C], bits[C];
+#pragma unroll
+                                    for (int c = 0; c < C; ++c) {
+                                        const int w = d2 ? R - 1 - (kq + c) : kq + c;
+                                        const uint64_t gv = line3[PS * w];
+                                        acc = boxFold<2>(acc, (w >= lo2 && w <= hi2) ? gv : 0ull);
+                                        key[c] = SALTED ? acc ^ salt : acc; // the salt is even: bit 0 still says "non-empty"
+                                    }
+#pragma unroll
+                                    for (int c = 0; c < C; ++c) {
+                                        const uint32_t x = filterFold(key[c]);
+                                        bits[c] = filterBits(x);
+                                        const bool nonEmpty = key[c] & 1u;
+                                        cProbe += nonEmpty ? 1u : 0u;
+                                        word[c] = nonEmpty ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
+                                    }
+                                    uint32_t hit = 0;
+#pragma unroll
+                                    for (int c = 0; c < C; ++c)
+                                        hit |= ((word[c] & bits[c]) == bits[c] ? 1u : 0u) << c;
+                                    if (hit) {
+                                        const uint32_t k = __popc(hit);
+                                        cFilter += k;
+                                        uint32_t o = atomicAdd(stageCnt, k);
+                                        const uint32_t over = o + k > (uint32_t)STAGE ? o + k - max(o, (uint32_t)STAGE) : 0u;
+                                        unsigned long long g = 0;
+                                        if (over) // the stage is full: these go straight to the record list
+                                            g = atomicAdd(p.recCount, (unsigned long long)over);
+#pragma unroll
+                                        for (int c = 0; c < C; ++c) {
+                                            if ((hit >> c) & 1u) {
+                                                const int w = d2 ? R - 1 - (kq + c) : kq + c;
+                                                const uint32_t vidx = (uint32_t)(v0 * s0 + v1 * s1 + w * s2);
+                                                const ulonglong2 rec = make_ulonglong2(key[c], meta | ((uint64_t)vidx << 32));
+                                                if (o < (uint32_t)STAGE)
+                                                    stage[o] = rec;
+                                                else if (g < p.recCap)
+                                                    p.recs[g++] = rec;
+                                                else
+                                                    ++g;
+                                                ++o;
+                                            }
                                         }
                                     }
                                 }
-                                if (!direct)
-                                    stageFill += total;
-                                __syncwarp();
                             }
+                            flushStage((uint32_t)Sh::FLUSH);
                         }
                         __syncthreads(); // the next pass 2 rewrites G2
                     }
@@ -819,7 +884,7 @@ __global__ void __launch_bounds__(kThreads, 3) probeKernel(ProbeParams p)
             }
         }
     }
-    flushStage();
+    flushStage(1);
     const uint32_t vals[2] = { cProbe, cFilter };
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -852,27 +917,8 @@ struct LookupParams {
 template <int R, int L>
 __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
 {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t start = 0, cnt = 0;
-    uint64_t meta = 0;
-    if (i < p.count) {
-        const ulonglong2 rec = p.recs[i];
-        meta = rec.y;
-        uint32_t slot = slotHash(rec.x) & p.capMask;
-        for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
-            const ulonglong2 sv = p.slots[slot];
-            if (sv.x == rec.x) {
-                start = (uint32_t)sv.y;
-                cnt = (uint32_t)(sv.y >> 32);
-                break;
-            }
-            if (sv.x == 0)
-                break;
-            slot = (slot + 1) & p.capMask;
-        }
-    }
-    uint32_t cHit = cnt ? 1u : 0u, cCand = 0, cVer = 0, cOk = 0;
+    uint32_t cHit = 0, cCand = 0, cVer = 0, cOk = 0;
 
     // every candidate (target, corner) of the hit recorded in `m` (find_translation.cpp:820-864)
     struct Src {
@@ -931,24 +977,48 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         ++cOk;
         atomicMin(&p.parents[tgt], (unsigned long long)key);
     };
-    // short ranges: every lane walks its own hit's candidates
-    constexpr uint32_t kSerialMax = 8;
-    if (cnt != 0 && cnt <= kSerialMax) {
-        const Src s = source(meta);
-        for (uint32_t e = 0; e < cnt; ++e)
-            candidate(__ldg(&p.entries[start + e]), s);
-    }
-    // long ranges: the warp walks one range at a time
-    uint32_t hitMask = __ballot_sync(0xffffffffu, cnt > kSerialMax);
-    while (hitMask) {
-        const int src = __ffs(hitMask) - 1;
-        hitMask &= hitMask - 1;
-        const uint32_t bs = __shfl_sync(0xffffffffu, start, src);
-        const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
-        const uint64_t bm = __shfl_sync(0xffffffffu, meta, src);
-        const Src s = source(bm);
-        for (uint32_t e = lane; e < bc; e += 32)
-            candidate(__ldg(&p.entries[bs + e]), s);
+    // persistent warps: each takes 32 consecutive records per step
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < p.count; i0 += stride) {
+        const uint64_t i = i0 + lane;
+        uint32_t start = 0, cnt = 0;
+        uint64_t meta = 0;
+        if (i < p.count) {
+            const ulonglong2 rec = p.recs[i];
+            meta = rec.y;
+            uint32_t slot = slotHash(rec.x) & p.capMask;
+            for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
+                const ulonglong2 sv = p.slots[slot];
+                if (sv.x == rec.x) {
+                    start = (uint32_t)sv.y;
+                    cnt = (uint32_t)(sv.y >> 32);
+                    break;
+                }
+                if (sv.x == 0)
+                    break;
+                slot = (slot + 1) & p.capMask;
+            }
+        }
+        cHit += cnt ? 1u : 0u;
+        // short ranges: every lane walks its own hit's candidates
+        constexpr uint32_t kSerialMax = 8;
+        if (cnt != 0 && cnt <= kSerialMax) {
+            const Src s = source(meta);
+            for (uint32_t e = 0; e < cnt; ++e)
+                candidate(__ldg(&p.entries[start + e]), s);
+        }
+        // long ranges: the warp walks one range at a time
+        uint32_t hitMask = __ballot_sync(0xffffffffu, cnt > kSerialMax);
+        while (hitMask) {
+            const int src = __ffs(hitMask) - 1;
+            hitMask &= hitMask - 1;
+            const uint32_t bs = __shfl_sync(0xffffffffu, start, src);
+            const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
+            const uint64_t bm = __shfl_sync(0xffffffffu, meta, src);
+            const Src s = source(bm);
+            for (uint32_t e = lane; e < bc; e += 32)
+                candidate(__ldg(&p.entries[bs + e]), s);
+        }
     }
     const uint32_t vals[4] = { cHit, cCand, cVer, cOk };
 #pragma unroll
@@ -1096,9 +1166,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, s));
 
     const size_t smem = ProbeShape<R>::SMEM;
-    TDAG_CUDA(cudaFuncSetAttribute(probeKernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto probe = batched ? probeKernel<R, true> : probeKernel<R, false>;
+    TDAG_CUDA(cudaFuncSetAttribute(probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int perSM = 0;
-    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, probeKernel<R>, kThreads, smem));
+    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, probe, kThreads, smem));
     if (ctx.tuning.search_ctas_per_sm)
         perSM = std::min<int>(perSM, (int)ctx.tuning.search_ctas_per_sm);
     perSM = std::max(perSM, 1);
@@ -1107,6 +1178,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     size_t freeBytes = 0, totalBytes = 0;
     TDAG_CUDA(cudaMemGetInfo(&freeBytes, &totalBytes));
     const uint64_t maxRecords = std::max<uint64_t>(1u << 20, freeBytes / 4 / sizeof(ulonglong2));
+    int lookupPerSM = 0;
+    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
+    const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
     // Source batches. Single grid: doubling ranges of sorted positions, starting at a few waves of
     // teams. Batch: the same fractions of every grid (1/256, 1/128, ..., 1/2, 1), as a list of sorted
@@ -1157,6 +1231,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<unsigned long long> recCount(1, s);
     double recsPerSource = R * R * 2.0; // first estimate; then a running average of the probed ranges
     unsigned long long probeCounts[2] = { 0, 0 }; // probes and filter passes before the current range
+    // per-batch diagnostics on stderr (TDAG_TRACE): probe and lookup time, records
+    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+    cudaEvent_t traceEv[2] = { nullptr, nullptr };
+    if (trace)
+        for (auto& e : traceEv)
+            TDAG_CUDA(cudaEventCreate(&e));
+    float traceProbeMs = 0, traceLookupMs = 0;
+    unsigned long long traceRecords = 0;
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi) {
         const uint32_t b0 = bounds[bi], b1 = bounds[bi + 1];
         if (b0 == b1)
@@ -1222,10 +1304,19 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemsetAsync(recCount.get(), 0, 8, s));
                 const uint64_t groups = ((uint64_t)cs + ProbeShape<R>::TEAMS - 1) / ProbeShape<R>::TEAMS;
                 const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
-                probeKernel<R><<<blocks, kThreads, smem, s>>>(pp);
+                if (trace)
+                    TDAG_CUDA(cudaEventRecord(traceEv[0], s));
+                probe<<<blocks, kThreads, smem, s>>>(pp);
                 TDAG_LAUNCHED();
+                if (trace)
+                    TDAG_CUDA(cudaEventRecord(traceEv[1], s));
                 TDAG_CUDA(cudaMemcpyAsync(&produced, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
+                if (trace) {
+                    float pm = 0;
+                    TDAG_CUDA(cudaEventElapsedTime(&pm, traceEv[0], traceEv[1]));
+                    traceProbeMs += pm;
+                }
                 if (produced <= pp.recCap)
                     break;
                 // the discarded run's probe and filter counts are rolled back
@@ -1245,8 +1336,20 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 lp.count = produced;
                 lp.begin = pos;
                 lp.srcLines = srcLines.get();
-                lookupKernel<R, L><<<(unsigned)((produced + kThreads - 1) / kThreads), kThreads, 0, s>>>(lp);
+                const uint64_t warpsNeeded = (produced + 31) / 32;
+                const unsigned lblocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)lookupBlocks, (warpsNeeded + kThreads / 32 - 1) / (kThreads / 32)));
+                if (trace)
+                    TDAG_CUDA(cudaEventRecord(traceEv[0], s));
+                lookupKernel<R, L><<<lblocks, kThreads, 0, s>>>(lp);
                 TDAG_LAUNCHED();
+                if (trace) {
+                    TDAG_CUDA(cudaEventRecord(traceEv[1], s));
+                    TDAG_CUDA(cudaEventSynchronize(traceEv[1]));
+                    float lm = 0;
+                    TDAG_CUDA(cudaEventElapsedTime(&lm, traceEv[0], traceEv[1]));
+                    traceLookupMs += lm;
+                    traceRecords += produced;
+                }
             }
             pos += cs;
         }
@@ -1255,13 +1358,18 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         float ms = 0;
         TDAG_CUDA(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]));
         searchMs += ms;
-        if (std::getenv("TDAG_TRACE")) { // per-batch diagnostics on stderr
+        if (trace) {
             unsigned long long c[8];
             TDAG_CUDA(cudaMemcpy(c, counters.get(), 64, cudaMemcpyDeviceToHost));
-            std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu\n", L, bi,
-                b1 - b0, (unsigned long long)table.numEntries, ms, c[0], c[1], c[2], c[3], c[4]);
+            std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f (probe %.3f lookup %.3f records %llu) | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu\n",
+                L, bi, b1 - b0, (unsigned long long)table.numEntries, ms, traceProbeMs, traceLookupMs, traceRecords, c[0], c[1], c[2], c[3], c[4]);
+            traceProbeMs = traceLookupMs = 0;
+            traceRecords = 0;
         }
     }
+    for (auto e : traceEv)
+        if (e)
+            cudaEventDestroy(e);
     table = Table();
     flags.release();
     liveIdx.release();
