@@ -147,6 +147,86 @@ __global__ void cornerHashKernel(const uint64_t* __restrict__ grids, uint32_t n,
     }
 }
 
+// The two axes other than a, in increasing order.
+__device__ __forceinline__ int otherLo(int a) { return a == 0 ? 1 : 0; }
+__device__ __forceinline__ int otherHi(int a) { return a == 2 ? 1 : 2; }
+
+// ---------------------------------------------------------------------------- permuted corner views
+// The reference search folds every source in all six axis orders (a0, a1, a2) and eight directions
+// and looks the box hashes up among the targets' eight corner views (find_translation.cpp:780-870).
+// Permuting axes commutes with cropping and turns shifts and mirrors into shifts and mirrors, so
+// t = crop(shift_T(mirror_S(perm_a(s)))) holds exactly when b(t) = crop(shift_T'(mirror_S'(s))) with
+// b = a^-1 and S', T' the mirror bits and translation re-indexed by b. The split search therefore
+// folds each source in the identity order only (8 directions instead of 48 orientations) and looks
+// its box hashes up among 48 views per target: for each axis order b (pidB = 2 b0 + (b2 < b1)) and
+// corner c' (bit i: pass i folds down from R-1), the whole grid folded along b0, then b1, then b2.
+// Every (source, target, transform) the reference finds is found once, and the lookup maps it back
+// to the reference's (perm, sym, translation). payload = item << 6 | pidB << 3 | c'.
+template <int R>
+__global__ void __launch_bounds__(kThreads) cornerViewsKernel(const uint64_t* __restrict__ grids, uint32_t n, uint32_t perms, uint64_t* __restrict__ keys,
+    uint32_t* __restrict__ payload, const uint32_t* __restrict__ gridOf)
+{
+    constexpr int W = R * R * R / 64;
+    constexpr int WARPS = kThreads / 32;
+    constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
+    __shared__ uint64_t sGrid[WARPS][W];
+    __shared__ uint16_t sLines[WARPS][3 * R * R]; // [a][u_lo + R u_hi]
+    __shared__ uint64_t sG2[WARPS][6 * 4 * R]; // [(pidB * 4 + c0 + 2 c1) * R + w2]
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t item = blockIdx.x * WARPS + warp;
+    if (item >= n) // warp-uniform
+        return;
+    const uint64_t* g = grids + (size_t)item * W;
+    for (int k = lane; k < W; k += 32)
+        sGrid[warp][k] = g[k];
+    __syncwarp();
+    for (int t = lane; t < R * R; t += 32) {
+        const int tA = t % R, tB = t / R;
+        const uint32_t off = (uint32_t)R * (tA + R * tB); // x-line at (y, z) = (tA, tB)
+        uint32_t ly = 0, lz = 0;
+        for (int j = 0; j < R; ++j) {
+            const uint32_t iy = tA + R * j + R * R * tB; // (x=tA, y=j, z=tB)
+            const uint32_t iz = tA + R * tB + R * R * j; // (x=tA, y=tB, z=j)
+            ly |= (uint32_t)((sGrid[warp][iy >> 6] >> (iy & 63)) & 1) << j;
+            lz |= (uint32_t)((sGrid[warp][iz >> 6] >> (iz & 63)) & 1) << j;
+        }
+        sLines[warp][t] = (uint16_t)((uint32_t)(sGrid[warp][off >> 6] >> (off & 63)) & rowMask);
+        sLines[warp][R * R + t] = (uint16_t)ly;
+        sLines[warp][2 * R * R + t] = (uint16_t)lz;
+    }
+    __syncwarp();
+    // pass 2: for every axis order, pass-1 and pass-2 direction and coordinate w2 along b2, the fold
+    // along b1 of the pass-1 codes of the whole lines along b0
+    for (int ch = lane; ch < (int)perms * 4 * R; ch += 32) {
+        const int w2 = ch % R, c01 = (ch / R) & 3, pb = ch / (4 * R);
+        const int b0 = pb >> 1, lo = otherLo(b0), hi = otherHi(b0);
+        const int b1 = (pb & 1) ? hi : lo, b2 = (pb & 1) ? lo : hi;
+        const int c0 = c01 & 1, c1 = c01 >> 1;
+        const uint16_t* La = sLines[warp] + b0 * R * R;
+        const int sj = b1 < b2 ? 1 : R, bw = b1 < b2 ? R * w2 : w2; // line index with u[b1] = j, u[b2] = w2
+        uint64_t acc = 0;
+        for (int k = 0; k < R; ++k) {
+            const int j = c1 ? R - 1 - k : k;
+            acc = boxFold<1>(acc, lineCode(La[bw + j * sj], c0 ? 0 : R - 1, c0));
+        }
+        sG2[warp][ch] = acc;
+    }
+    __syncwarp();
+    // pass 3 along b2: one view per (pidB, c')
+    const uint32_t views = perms * 8;
+    const uint64_t salt = gridOf ? boxSalt(gridOf[item]) : 0ull;
+    for (uint32_t v = lane; v < views; v += 32) {
+        const uint32_t pb = v >> 3, cp = v & 7;
+        const uint64_t* G = sG2[warp] + (pb * 4 + (cp & 3)) * R;
+        uint64_t acc = 0;
+        for (int k = 0; k < R; ++k)
+            acc = boxFold<2>(acc, G[(cp >> 2) ? R - 1 - k : k]);
+        const size_t e = (size_t)item * views + v;
+        keys[e] = acc ^ salt; // a grid is never empty: acc is odd, and the salt is even
+        payload[e] = (item << 6) | (pb << 3) | cp;
+    }
+}
+
 // ---------------------------------------------------------------------------- corner-hash table
 // slots: (key, start | count << 32) pairs; entries: payload (item * 8 + corner) grouped by key.
 __global__ void tableInsertKernel(const uint64_t* __restrict__ ekeys, size_t m, ulonglong2* __restrict__ slots, uint32_t* __restrict__ tcount,
@@ -215,7 +295,7 @@ __global__ void liveEntriesKernel(const uint64_t* __restrict__ ekeys, const uint
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m)
         return;
-    const uint32_t t = epay[e] >> 3;
+    const uint32_t t = epay[e] >> 6; // payload of a permuted corner view: item << 6 | pidB << 3 | c'
     const unsigned long long mk = gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext;
     flags[e] = (ekeys[e] != 0) && (parents[t] > mk);
 }
@@ -267,8 +347,6 @@ struct SearchShape {
 };
 
 __device__ __forceinline__ int smemStride(int a, int SY, int SZ) { return a == 0 ? 1 : (a == 1 ? SY : SZ); }
-__device__ __forceinline__ int otherLo(int a) { return a == 0 ? 1 : 0; }
-__device__ __forceinline__ int otherHi(int a) { return a == 2 ? 1 : 2; }
 
 // Exact verification: target == translate(mirror(permute(source, P), S), T) (find_translation.cpp:857-862),
 // row by row. lines[a][u_lo + R u_hi] holds the source's voxels along axis a (bit j = coordinate j).
@@ -621,25 +699,23 @@ struct ProbeShape {
     static constexpr int TEAM = R * R; // pass 2: thread per (v0, w2); pass 3: thread per (v0, v1)
     static constexpr int TEAMS = kThreads / TEAM;
     static constexpr int W = R * R * R / 64;
-    // G2[v0 + R v1 + PS w2]: both passes read or write runs of consecutive v0 per team row; for R < 16
-    // the plane stride is padded so that the team rows of one warp fall into different banks
+    // G2[x + R y + PS z]: both passes read or write runs of consecutive x per team row; for R < 16 the
+    // plane stride is padded so that the team rows of one warp fall into different banks
     static constexpr int PS = R * R + (R < 16 ? R : 0);
     static constexpr int CHUNK = 4; // pass-3 elements whose filter loads are in flight together
     static constexpr int STAGE = 96; // staged records per warp (four CTAs of R = 16 fit an SM)
     static constexpr int FLUSH = STAGE / 2; // a warp flushes once this many are staged
-    // per team: G2 (u64), srcW (u64), lines[3][R*R] and linesT[3][R*R] (u16)
+    // per team: G2 (u64), srcW (u64), x-lines[R*R] (u16)
     static constexpr size_t LINES_OFF = (size_t)(PS * R + W) * 8;
-    static constexpr size_t TEAM_BYTES = LINES_OFF + 6 * R * R * 2;
+    static constexpr size_t TEAM_BYTES = (LINES_OFF + R * R * 2 + 15) & ~(size_t)15;
     static constexpr size_t STAGE_OFF = TEAM_BYTES * TEAMS;
     static constexpr size_t COUNT_OFF = STAGE_OFF + (size_t)(kThreads / 32) * STAGE * 16; // per-warp stage counts
     static constexpr size_t BOX_OFF = COUNT_OFF + (kThreads / 32) * 4; // per team: lo x y z, hi + 1 x y z
     static constexpr size_t SMEM = BOX_OFF + TEAMS * 24 + 16;
-    static_assert(STAGE_OFF % 16 == 0 && TEAM_BYTES % 8 == 0, "alignment");
+    static_assert(STAGE_OFF % 16 == 0 && TEAM_BYTES % 16 == 0, "alignment");
     static_assert(R == 4 || LINES_OFF % 16 == 0, "pass-2 rows are read as 16-byte vectors");
     static_assert(R % CHUNK == 0, "chunks tile a line");
 };
-
-__device__ __forceinline__ int axisStride(int a, int R) { return a == 0 ? 1 : (a == 1 ? R : R * R); }
 
 // The R line codes of one pass-2 row (R consecutive u16, 8-byte aligned for R = 4, else 16-byte),
 // two per word.
@@ -662,13 +738,15 @@ __device__ __forceinline__ void loadRow(const uint16_t* row, uint32_t (&lv)[R / 
     }
 }
 
+// Every source is folded in the identity axis order (x, then y, then z) in its eight directions; the
+// other five axis orders are covered by the targets' permuted corner views (cornerViewsKernel).
 // Only boxes that hold a voxel are probed. With the source's bounding box [lo, hi] per axis, the box
 // from the anchor to v is empty unless v is past the box's start on every axis (v >= lo when folding
-// up from 0, v <= hi when folding down from R-1). A team therefore runs pass 2 on the (v0, w2) pairs
-// with v0 past the start along a0 and w2 in [lo, hi] along a2, and pass 3 on the (v0, v1) pairs past
-// the start along a0 and a1, folding each line from its first plane that can be non-empty (rounded
-// down to a chunk; the skipped elements hash to 0, exactly as if they had been folded). Planes along
-// a2 outside [lo, hi] are empty and read as 0. SALTED: batch members' keys carry their grid salt.
+// up from 0, v <= hi when folding down from R-1). A team therefore runs pass 2 on the (x, z) pairs
+// with x past the start and z in [lo, hi], and pass 3 on the (x, y) pairs past the start along x and
+// y, folding each z line from its first plane that can be non-empty (rounded down to a chunk; the
+// skipped elements hash to 0, exactly as if they had been folded). Planes outside [lo, hi] along z are
+// empty and read as 0. SALTED: batch members' keys carry their grid salt.
 template <int R, bool SALTED>
 __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
 {
@@ -682,8 +760,7 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
     uint8_t* tb = smem + (size_t)team * Sh::TEAM_BYTES;
     uint64_t* G2 = reinterpret_cast<uint64_t*>(tb);
     uint64_t* srcW = G2 + PS * R;
-    uint16_t* lines = reinterpret_cast<uint16_t*>(tb + Sh::LINES_OFF); // [a][u_lo + R u_hi]
-    uint16_t* linesT = lines + 3 * R * R; // [a][u_hi + R u_lo]
+    uint16_t* xLines = reinterpret_cast<uint16_t*>(tb + Sh::LINES_OFF); // [y + R z]
     ulonglong2* stage = reinterpret_cast<ulonglong2*>(smem + Sh::STAGE_OFF) + warp * STAGE;
     uint32_t* stageCnt = reinterpret_cast<uint32_t*>(smem + Sh::COUNT_OFF) + warp;
     uint32_t* box = reinterpret_cast<uint32_t*>(smem + Sh::BOX_OFF) + team * 6;
@@ -754,13 +831,11 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
                 ly |= (uint32_t)((srcW[iy >> 6] >> (iy & 63)) & 1) << j;
                 lz |= (uint32_t)((srcW[iz >> 6] >> (iz & 63)) & 1) << j;
             }
-            lines[tl] = (uint16_t)lx;
-            lines[R * R + tl] = (uint16_t)ly;
-            lines[2 * R * R + tl] = (uint16_t)lz;
-            const int tt = tB + R * tA;
-            linesT[tt] = (uint16_t)lx;
-            linesT[R * R + tt] = (uint16_t)ly;
-            linesT[2 * R * R + tt] = (uint16_t)lz;
+            xLines[tl] = (uint16_t)lx;
+            uint16_t* dst = p.srcLines + (size_t)wIdx * 3 * R * R; // all three orientations, for verification
+            dst[tl] = (uint16_t)lx;
+            dst[R * R + tl] = (uint16_t)ly;
+            dst[2 * R * R + tl] = (uint16_t)lz;
             // bounding box: lowest set coordinate and highest + 1 along every axis
             const uint32_t l3[3] = { lx, ly, lz };
 #pragma unroll
@@ -774,113 +849,95 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
             }
         }
         __syncthreads();
-        if (valid) {
-            uint16_t* dst = p.srcLines + (size_t)wIdx * 3 * R * R;
-            for (int k = tl; k < 3 * R * R; k += TEAM)
-                dst[k] = lines[k];
-        }
-        const int lo[3] = { (int)box[0], (int)box[1], (int)box[2] };
-        const int hi[3] = { (int)box[3] - 1, (int)box[4] - 1, (int)box[5] - 1 };
-        auto loOf = [&](int a) { return a == 0 ? lo[0] : (a == 1 ? lo[1] : lo[2]); };
-        auto hiOf = [&](int a) { return a == 0 ? hi[0] : (a == 1 ? hi[1] : hi[2]); };
+        const int loX = (int)box[0], loY = (int)box[1], loZ = (int)box[2];
+        const int hiX = (int)box[3] - 1, hiY = (int)box[4] - 1, hiZ = (int)box[5] - 1;
 
-        for (int a0 = 0; a0 < 3; ++a0) {
-            for (int d0 = 1; d0 >= 0; --d0) {
-                // active v0: the window along a0 ending at v0 holds a voxel
-                const int v0s = d0 ? 0 : loOf(a0);
-                const int n0 = d0 ? hiOf(a0) + 1 : R - loOf(a0);
-                const int r0 = n0 > 0 ? tl % n0 : 0, q0 = n0 > 0 ? tl / n0 : R;
-                const int v0 = v0s + r0;
-                for (int a1i = 0; a1i < 2; ++a1i) {
-                    const int a1 = (a0 + 1 + a1i) % 3;
-                    const int a2 = 3 - a0 - a1;
-                    const uint32_t pid = 2 * a0 + (a2 < a1 ? 1 : 0);
-                    const int s0 = axisStride(a0, R), s1 = axisStride(a1, R), s2 = axisStride(a2, R);
-                    const int lo2 = loOf(a2), hi2 = hiOf(a2);
-                    for (int d1 = 1; d1 >= 0; --d1) {
-                        // ---- pass 2 along a1 from the exact line codes, thread (v0, w2 = lo2 + q0);
-                        // the row holds the lines along a0 at u[a1] = j, u[a2] = w2, for every j
-                        if (valid && q0 <= hi2 - lo2) {
-                            const int w2 = lo2 + q0;
-                            uint32_t lv[R / 2];
-                            loadRow<R>((a1 < a2 ? lines : linesT) + a0 * R * R + R * w2, lv);
-                            uint64_t acc = 0;
+        for (int d0 = 1; d0 >= 0; --d0) {
+            // active x: the window along x ending at x holds a voxel
+            const int v0s = d0 ? 0 : loX;
+            const int n0 = d0 ? hiX + 1 : R - loX;
+            const int r0 = n0 > 0 ? tl % n0 : 0, q0 = n0 > 0 ? tl / n0 : R;
+            const int v0 = v0s + r0;
+            for (int d1 = 1; d1 >= 0; --d1) {
+                // ---- pass 2 along y from the exact x-line codes, thread (x, z = loZ + q0)
+                if (valid && q0 <= hiZ - loZ) {
+                    const int w2 = loZ + q0;
+                    uint32_t lv[R / 2];
+                    loadRow<R>(xLines + R * w2, lv);
+                    uint64_t acc = 0;
 #pragma unroll
-                            for (int k = 0; k < R; ++k) {
-                                const int j = d1 ? R - 1 - k : k;
-                                const uint32_t ln = (lv[j >> 1] >> ((j & 1) * 16)) & 0xFFFFu;
-                                acc = boxFold<1>(acc, lineCode(ln, v0, d0));
-                                G2[v0 + R * j + PS * w2] = acc;
-                            }
-                        }
-                        __syncthreads();
-                        // ---- pass 3 along a2, both directions, thread (v0, v1 = v1s + q0)
-                        const int v1s = d1 ? 0 : loOf(a1);
-                        const int n1 = d1 ? hiOf(a1) + 1 : R - loOf(a1);
-                        const bool act3 = valid && q0 < n1;
-                        const int v1 = v1s + q0;
-                        const uint64_t* line3 = G2 + v0 + R * v1;
+                    for (int k = 0; k < R; ++k) {
+                        const int j = d1 ? R - 1 - k : k;
+                        const uint32_t ln = (lv[j >> 1] >> ((j & 1) * 16)) & 0xFFFFu;
+                        acc = boxFold<1>(acc, lineCode(ln, v0, d0));
+                        G2[v0 + R * j + PS * w2] = acc;
+                    }
+                }
+                __syncthreads();
+                // ---- pass 3 along z, both directions, thread (x, y = v1s + q0)
+                const int v1s = d1 ? 0 : loY;
+                const int n1 = d1 ? hiY + 1 : R - loY;
+                const bool act3 = valid && q0 < n1;
+                const int v1 = v1s + q0;
+                const uint64_t* line3 = G2 + v0 + R * v1;
 #pragma unroll
-                        for (int d2 = 1; d2 >= 0; --d2) {
-                            if (act3) {
-                                const uint64_t meta = (uint64_t)wIdx | ((uint64_t)pid << 44)
-                                    | ((uint64_t)((uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2)) << 47);
-                                const int k0 = d2 ? R - 1 - hi2 : lo2; // fold index of the first plane that can hold a voxel
-                                uint64_t acc = 0;
+                for (int d2 = 1; d2 >= 0; --d2) {
+                    if (act3) {
+                        const uint64_t meta = (uint64_t)wIdx | ((uint64_t)((uint32_t)d0 | ((uint32_t)d1 << 1) | ((uint32_t)d2 << 2)) << 47);
+                        const int k0 = d2 ? R - 1 - hiZ : loZ; // fold index of the first plane that can hold a voxel
+                        uint64_t acc = 0;
 #pragma unroll 1
-                                for (int kq = k0 & ~(C - 1); kq < R; kq += C) {
-                                    uint64_t key[C];
-                                    uint32_t word[C], bits[C];
+                        for (int kq = k0 & ~(C - 1); kq < R; kq += C) {
+                            uint64_t key[C];
+                            uint32_t word[C], bits[C];
 #pragma unroll
-                                    for (int c = 0; c < C; ++c) {
+                            for (int c = 0; c < C; ++c) {
+                                const int w = d2 ? R - 1 - (kq + c) : kq + c;
+                                const uint64_t gv = line3[PS * w];
+                                acc = boxFold<2>(acc, (w >= loZ && w <= hiZ) ? gv : 0ull);
+                                key[c] = SALTED ? acc ^ salt : acc; // the salt is even: bit 0 still says "non-empty"
+                            }
+#pragma unroll
+                            for (int c = 0; c < C; ++c) {
+                                const uint32_t x = filterFold(key[c]);
+                                bits[c] = filterBits(x);
+                                const bool nonEmpty = key[c] & 1u;
+                                cProbe += nonEmpty ? 1u : 0u;
+                                word[c] = nonEmpty ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
+                            }
+                            uint32_t hit = 0;
+#pragma unroll
+                            for (int c = 0; c < C; ++c)
+                                hit |= ((word[c] & bits[c]) == bits[c] ? 1u : 0u) << c;
+                            if (hit) {
+                                const uint32_t k = __popc(hit);
+                                cFilter += k;
+                                uint32_t o = atomicAdd(stageCnt, k);
+                                const uint32_t over = o + k > (uint32_t)STAGE ? o + k - max(o, (uint32_t)STAGE) : 0u;
+                                unsigned long long g = 0;
+                                if (over) // the stage is full: these go straight to the record list
+                                    g = atomicAdd(p.recCount, (unsigned long long)over);
+#pragma unroll
+                                for (int c = 0; c < C; ++c) {
+                                    if ((hit >> c) & 1u) {
                                         const int w = d2 ? R - 1 - (kq + c) : kq + c;
-                                        const uint64_t gv = line3[PS * w];
-                                        acc = boxFold<2>(acc, (w >= lo2 && w <= hi2) ? gv : 0ull);
-                                        key[c] = SALTED ? acc ^ salt : acc; // the salt is even: bit 0 still says "non-empty"
-                                    }
-#pragma unroll
-                                    for (int c = 0; c < C; ++c) {
-                                        const uint32_t x = filterFold(key[c]);
-                                        bits[c] = filterBits(x);
-                                        const bool nonEmpty = key[c] & 1u;
-                                        cProbe += nonEmpty ? 1u : 0u;
-                                        word[c] = nonEmpty ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
-                                    }
-                                    uint32_t hit = 0;
-#pragma unroll
-                                    for (int c = 0; c < C; ++c)
-                                        hit |= ((word[c] & bits[c]) == bits[c] ? 1u : 0u) << c;
-                                    if (hit) {
-                                        const uint32_t k = __popc(hit);
-                                        cFilter += k;
-                                        uint32_t o = atomicAdd(stageCnt, k);
-                                        const uint32_t over = o + k > (uint32_t)STAGE ? o + k - max(o, (uint32_t)STAGE) : 0u;
-                                        unsigned long long g = 0;
-                                        if (over) // the stage is full: these go straight to the record list
-                                            g = atomicAdd(p.recCount, (unsigned long long)over);
-#pragma unroll
-                                        for (int c = 0; c < C; ++c) {
-                                            if ((hit >> c) & 1u) {
-                                                const int w = d2 ? R - 1 - (kq + c) : kq + c;
-                                                const uint32_t vidx = (uint32_t)(v0 * s0 + v1 * s1 + w * s2);
-                                                const ulonglong2 rec = make_ulonglong2(key[c], meta | ((uint64_t)vidx << 32));
-                                                if (o < (uint32_t)STAGE)
-                                                    stage[o] = rec;
-                                                else if (g < p.recCap)
-                                                    p.recs[g++] = rec;
-                                                else
-                                                    ++g;
-                                                ++o;
-                                            }
-                                        }
+                                        const uint32_t vidx = (uint32_t)(v0 + R * v1 + R * R * w);
+                                        const ulonglong2 rec = make_ulonglong2(key[c], meta | ((uint64_t)vidx << 32));
+                                        if (o < (uint32_t)STAGE)
+                                            stage[o] = rec;
+                                        else if (g < p.recCap)
+                                            p.recs[g++] = rec;
+                                        else
+                                            ++g;
+                                        ++o;
                                     }
                                 }
                             }
-                            flushStage((uint32_t)Sh::FLUSH);
                         }
-                        __syncthreads(); // the next pass 2 rewrites G2
                     }
+                    flushStage((uint32_t)Sh::FLUSH);
                 }
+                __syncthreads(); // the next pass 2 rewrites G2
             }
         }
     }
@@ -920,59 +977,66 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
     const uint32_t lane = threadIdx.x & 31;
     uint32_t cHit = 0, cCand = 0, cVer = 0, cOk = 0;
 
-    // every candidate (target, corner) of the hit recorded in `m` (find_translation.cpp:820-864)
+    // every candidate (target, corner view) of the hit recorded in `m` (find_translation.cpp:820-864)
     struct Src {
-        uint32_t rSrc, tLo, tHi;
+        uint32_t rSrc, tLo, tHi, dir;
         const uint16_t* lines;
-        int a0, a1, a2, v0, v1, v2, an0, an1, an2;
-        uint32_t pid, dir;
+        int ux, uy, uz;
     };
     auto source = [&](uint64_t m) {
         Src s;
         const uint32_t w = (uint32_t)m;
         const uint32_t vidx = (uint32_t)(m >> 32) & 0xFFFu;
-        s.pid = (uint32_t)(m >> 44) & 7u;
-        s.dir = (uint32_t)(m >> 47) & 7u;
+        s.dir = (uint32_t)(m >> 47) & 7u; // fold directions along x, y, z
         const uint32_t r = p.workList ? p.workList[p.begin + w] : p.begin + w;
         const uint32_t g = p.gridOf ? p.gridOf[p.order[r]] : 0u;
         s.rSrc = p.segOff ? r - p.segOff[g] : r;
         s.tLo = p.segOff ? p.segOff[g] : 0u;
         s.tHi = p.segOff ? p.segOff[g + 1] : 0xFFFFFFFFu;
         s.lines = p.srcLines + (size_t)w * 3 * R * R;
-        s.a0 = (int)(s.pid >> 1);
-        const int lo = otherLo(s.a0), hi = otherHi(s.a0);
-        s.a1 = (s.pid & 1) ? hi : lo;
-        s.a2 = (s.pid & 1) ? lo : hi;
-        const int ux = (int)(vidx % R), uy = (int)((vidx / R) % R), uz = (int)(vidx / (R * R));
-        s.v0 = s.a0 == 0 ? ux : (s.a0 == 1 ? uy : uz);
-        s.v1 = s.a1 == 0 ? ux : (s.a1 == 1 ? uy : uz);
-        s.v2 = s.a2 == 0 ? ux : (s.a2 == 1 ? uy : uz);
-        s.an0 = (s.dir & 1) ? 0 : R - 1;
-        s.an1 = (s.dir & 2) ? 0 : R - 1;
-        s.an2 = (s.dir & 4) ? 0 : R - 1;
+        s.ux = (int)(vidx % R);
+        s.uy = (int)((vidx / R) % R);
+        s.uz = (int)(vidx / (R * R));
         return s;
     };
+    // The view folded the target along b0, b1, b2 (pidB) from corner c'; the source was folded along
+    // x, y, z in directions dir. In the reference's terms the source orientation is a = b^-1 (source
+    // axis a_i lies along target axis i) with fold directions d_i = dir[a_i], the target corner is
+    // c_i = c'[a_i], and S = d ^ c, v_i = u[a_i].
     auto candidate = [&](uint32_t pay, const Src& s) {
-        const uint32_t tgt = pay >> 3;
-        const uint32_t S = s.dir ^ (pay & 7);
+        const uint32_t tgt = pay >> 6;
+        const uint32_t pb = (pay >> 3) & 7u, cp = pay & 7u;
         ++cCand;
         if (tgt < s.tLo || tgt >= s.tHi) // another grid of the batch
             return;
-        const int T0 = (S & 1) ? s.v0 - s.an0 : s.an0 - s.v0;
-        const int T1 = (S & 2) ? s.v1 - s.an1 : s.an1 - s.v1;
-        const int T2 = (S & 4) ? s.v2 - s.an2 : s.an2 - s.v2;
-        if (!p.allowPerm && s.pid != 0)
+        const int b0 = (int)(pb >> 1), blo = otherLo(b0), bhi = otherHi(b0);
+        const int b1 = (pb & 1) ? bhi : blo;
+        const int a0 = b0 == 0 ? 0 : (b1 == 0 ? 1 : 2);
+        const int a1 = b0 == 1 ? 0 : (b1 == 1 ? 1 : 2);
+        const int a2 = 3 - a0 - a1;
+        const uint32_t pid = 2 * (uint32_t)a0 + (a2 < a1 ? 1u : 0u);
+        const uint32_t xs = s.dir ^ cp;
+        const uint32_t S = ((xs >> a0) & 1u) | (((xs >> a1) & 1u) << 1) | (((xs >> a2) & 1u) << 2);
+        auto coord = [&](int a) { return a == 0 ? s.ux : (a == 1 ? s.uy : s.uz); };
+        const int v0 = coord(a0), v1 = coord(a1), v2 = coord(a2);
+        const int an0 = ((s.dir >> a0) & 1u) ? 0 : R - 1;
+        const int an1 = ((s.dir >> a1) & 1u) ? 0 : R - 1;
+        const int an2 = ((s.dir >> a2) & 1u) ? 0 : R - 1;
+        const int T0 = (S & 1) ? v0 - an0 : an0 - v0;
+        const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
+        const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
+        if (!p.allowPerm && pid != 0)
             return;
         if (!p.allowSym && S != 0)
             return;
         if (!p.allowTrans && (T0 | T1 | T2) != 0)
             return;
-        const uint64_t key = encodeFixed64(s.rSrc, s.pid, S, T0, T1, T2, L);
+        const uint64_t key = encodeFixed64(s.rSrc, pid, S, T0, T1, T2, L);
         const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
         if (key >= cur)
             return;
         ++cVer;
-        if (!verifyCandidate<R>(p.grids + (size_t)tgt * (R * R * R / 64), s.lines, s.a0, s.a1, s.a2, S, T0, T1, T2))
+        if (!verifyCandidate<R>(p.grids + (size_t)tgt * (R * R * R / 64), s.lines, a0, a1, a2, S, T0, T1, T2))
             return;
         ++cOk;
         atomicMin(&p.parents[tgt], (unsigned long long)key);
@@ -1151,11 +1215,13 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         radixSortPairs(key.get(), order.get(), n, 0, bits, s);
     }
 
-    // corner hashes: 8 per item; zero hashes (empty grids) are never entries
-    const size_t m = (size_t)n * 8;
+    // permuted corner views: 48 per item (8 when axis permutation is off: only the identity order)
+    TDAG_CHECK(n < (1u << 26), TDAG_ERR_ARG, "too many items for one matcher level (corner-view payloads hold 26-bit item indices)");
+    const uint32_t perms = cfg.axis_permutation ? 6u : 1u;
+    const size_t m = (size_t)n * perms * 8;
     DevBuf<uint64_t> ekeys(m, s);
     DevBuf<uint32_t> epay(m, s);
-    cornerHashKernel<R><<<gridFor(m * 32, kThreads), kThreads, 0, s>>>(grids, n, ekeys.get(), epay.get(), gridOf);
+    cornerViewsKernel<R><<<gridFor(n, kThreads / 32), kThreads, 0, s>>>(grids, n, perms, ekeys.get(), epay.get(), gridOf);
     TDAG_LAUNCHED();
 
     const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, L);
