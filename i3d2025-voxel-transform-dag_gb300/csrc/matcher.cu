@@ -288,6 +288,47 @@ __global__ void tableRangesKernel(ulonglong2* __restrict__ slots, const uint32_t
     }
 }
 
+// Runs of equal keys in a key-sorted entry array: flags[i] = 1 where a run starts.
+__global__ void markRunsKernel(const uint64_t* __restrict__ keys, size_t m, uint32_t* __restrict__ flags)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m)
+        flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// starts[run] = first entry of the run; starts[runs] = m.
+__global__ void runStartsKernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ runIdx, size_t m, uint32_t* __restrict__ starts, uint32_t runs)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m && flags[i])
+        starts[runIdx[i]] = (uint32_t)i;
+    if (i == 0)
+        starts[runs] = (uint32_t)m;
+}
+
+// One slot per run: (key, first entry | count << 32), and the key's filter bits. The keys are
+// distinct, so inserts contend only where probe sequences meet.
+__global__ void insertRunsKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t runs, ulonglong2* __restrict__ slots,
+    uint32_t capMask, uint32_t* __restrict__ filter, uint32_t filterShift, uint32_t* status)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= runs)
+        return;
+    const uint32_t start = starts[d], cnt = starts[d + 1] - start;
+    const uint64_t key = keys[start];
+    uint32_t slot = slotHash(key) & capMask;
+    for (uint32_t probe = 0; probe <= capMask; ++probe) {
+        if (atomicCAS(&slots[slot].x, 0ull, (unsigned long long)key) == 0ull) {
+            slots[slot].y = (uint64_t)start | ((uint64_t)cnt << 32);
+            const uint32_t x = filterFold(key);
+            atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
+            return;
+        }
+        slot = (slot + 1) & capMask;
+    }
+    setDeviceError(status, TDAG_ERR_TABLE_FULL, 201);
+}
+
 // Entries still able to receive a lower parent: parent[target] > minKey of the next source batch.
 __global__ void liveEntriesKernel(const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay, size_t m, const unsigned long long* __restrict__ parents,
     unsigned long long minKeyNext, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gridOf, const unsigned long long* __restrict__ minKeyOfGrid)
@@ -1138,52 +1179,55 @@ uint64_t pow2AtLeast(uint64_t v)
     return p;
 }
 
+// Corner-view table over entries sorted by key: one slot (key, first entry | count << 32) per run of
+// equal keys, the entries being the sorted payload array itself (not owned), and the membership
+// filter over the distinct keys.
 struct Table {
     DevBuf<ulonglong2> slots;
-    DevBuf<uint32_t> entries;
     DevBuf<uint32_t> filter;
+    const uint32_t* entries = nullptr;
     uint32_t capMask = 0, filterShift = 31;
-    uint64_t numEntries = 0;
+    uint64_t numEntries = 0, distinct = 0;
 };
 
-// Build the corner-hash table over m entries (non-zero keys).
-void buildTable(Context& ctx, const uint64_t* ekeys, const uint32_t* epay, size_t m, Table& t)
+void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, size_t m, Table& t)
 {
     cudaStream_t s = ctx.stream;
+    TDAG_CHECK(m < (1ull << 32), TDAG_ERR_ARG, "corner-view table too large");
+    DevBuf<uint32_t> flags(std::max<size_t>(m, 1), s), runIdx(std::max<size_t>(m, 1), s);
+    uint64_t runs = 0;
+    if (m) {
+        markRunsKernel<<<gridFor(m, 256), 256, 0, s>>>(keys, m, flags.get());
+        TDAG_LAUNCHED();
+        runs = exclusiveScanU32Total(flags.get(), runIdx.get(), m, s);
+    }
+    DevBuf<uint32_t> starts(runs + 1, s);
+    if (m) {
+        runStartsKernel<<<gridFor(m, 256), 256, 0, s>>>(flags.get(), runIdx.get(), m, starts.get(), (uint32_t)runs);
+        TDAG_LAUNCHED();
+    }
     const uint32_t loadPct = ctx.tuning.table_load_percent ? std::min(85u, std::max(25u, ctx.tuning.table_load_percent)) : 50u;
-    const uint64_t cap = pow2AtLeast(std::max<uint64_t>(64, m * 100 / loadPct + 1));
-    TDAG_CHECK(cap <= (1ull << 31), TDAG_ERR_ARG, "corner-hash table too large");
+    const uint64_t cap = pow2AtLeast(std::max<uint64_t>(64, runs * 100 / loadPct + 1));
+    TDAG_CHECK(cap <= (1ull << 31), TDAG_ERR_ARG, "corner-view table too large");
     t.slots = DevBuf<ulonglong2>(cap, s);
     t.capMask = (uint32_t)(cap - 1);
-    DevBuf<uint32_t> tcount(cap, s), tstart(cap, s), slotOfEntry(std::max<size_t>(m, 1), s), numDistinct(1, s);
     TDAG_CUDA(cudaMemsetAsync(t.slots.get(), 0, cap * sizeof(ulonglong2), s));
-    TDAG_CUDA(cudaMemsetAsync(tcount.get(), 0, cap * 4, s));
-    TDAG_CUDA(cudaMemsetAsync(numDistinct.get(), 0, 4, s));
-    if (m) {
-        tableInsertKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys, m, t.slots.get(), tcount.get(), slotOfEntry.get(), t.capMask, numDistinct.get(), ctx.status);
-        TDAG_LAUNCHED();
-    }
-    t.numEntries = exclusiveScanU32Total(tcount.get(), tstart.get(), cap, s);
-    uint32_t distinct = 0;
-    TDAG_CUDA(cudaMemcpyAsync(&distinct, numDistinct.get(), 4, cudaMemcpyDeviceToHost, s));
-    ctx.checkStatus("corner-hash table");
-    t.entries = DevBuf<uint32_t>(std::max<uint64_t>(t.numEntries, 1), s);
-    if (m) {
-        DevBuf<uint32_t> tfill(cap, s);
-        TDAG_CUDA(cudaMemsetAsync(tfill.get(), 0, cap * 4, s));
-        tableScatterKernel<<<gridFor(m, 256), 256, 0, s>>>(epay, slotOfEntry.get(), m, tstart.get(), tfill.get(), t.entries.get());
-        TDAG_LAUNCHED();
-    }
     const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
-    const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, (uint64_t)distinct * bitsPerKey));
+    const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey));
     uint32_t log2F = 0;
     while ((1ull << log2F) < filterBits)
         ++log2F;
     t.filterShift = 32 - log2F;
     t.filter = DevBuf<uint32_t>(filterBits / 32, s);
     TDAG_CUDA(cudaMemsetAsync(t.filter.get(), 0, filterBits / 8, s));
-    tableRangesKernel<<<gridFor(cap, 256), 256, 0, s>>>(t.slots.get(), tstart.get(), tcount.get(), (uint32_t)cap, t.filter.get(), t.filterShift);
-    TDAG_LAUNCHED();
+    if (runs) {
+        insertRunsKernel<<<gridFor(runs, 256), 256, 0, s>>>(keys, starts.get(), (uint32_t)runs, t.slots.get(), t.capMask, t.filter.get(), t.filterShift, ctx.status);
+        TDAG_LAUNCHED();
+    }
+    t.entries = pays;
+    t.numEntries = m;
+    t.distinct = runs;
+    ctx.checkStatus("corner-view table");
 }
 
 template <int L>
@@ -1282,13 +1326,21 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     if (!workList.empty())
         TDAG_CUDA(cudaMemcpyAsync(workListDev.get(), workList.data(), workList.size() * 4, cudaMemcpyHostToDevice, s));
 
+    // equal view keys side by side (the sort is stable: a run keeps item order)
+    radixSortPairs(ekeys.get(), epay.get(), m, 0, 64, s);
     Table table;
-    buildTable(ctx, ekeys.get(), epay.get(), m, table);
-    uint64_t entriesInitial = table.numEntries;
+    buildRunTable(ctx, ekeys.get(), epay.get(), m, table);
+    const uint64_t entriesInitial = table.numEntries;
     float searchMs = 0;
     DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
     DevBuf<uint64_t> k2(m, s);
     DevBuf<uint32_t> p2(m, s);
+    // the live entries, still sorted by key (pruning compacts them stably), and the spare pair
+    uint64_t* curKeys = ekeys.get();
+    uint32_t* curPays = epay.get();
+    uint64_t* spareKeys = k2.get();
+    uint32_t* sparePays = p2.get();
+    size_t mCur = m;
     uint32_t maxBatch = 1;
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi)
         maxBatch = std::max(maxBatch, bounds[bi + 1] - bounds[bi]);
@@ -1316,15 +1368,18 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
             }
-            liveEntriesKernel<<<gridFor(m, 256), 256, 0, s>>>(ekeys.get(), epay.get(), m, parents.get(), minKeyNext, flags.get(), gridOf,
+            liveEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, mCur, parents.get(), minKeyNext, flags.get(), gridOf,
                 batched ? minKeyDev.get() : nullptr);
             TDAG_LAUNCHED();
-            const uint32_t live = compactFlags(flags.get(), liveIdx.get(), m, s);
+            const uint32_t live = compactFlags(flags.get(), liveIdx.get(), mCur, s);
             if (live == 0)
                 break;
-            gatherEntriesKernel<<<gridFor(live, 256), 256, 0, s>>>(liveIdx.get(), live, ekeys.get(), epay.get(), k2.get(), p2.get());
+            gatherEntriesKernel<<<gridFor(live, 256), 256, 0, s>>>(liveIdx.get(), live, curKeys, curPays, spareKeys, sparePays);
             TDAG_LAUNCHED();
-            buildTable(ctx, k2.get(), p2.get(), live, table);
+            std::swap(curKeys, spareKeys);
+            std::swap(curPays, sparePays);
+            mCur = live;
+            buildRunTable(ctx, curKeys, curPays, mCur, table);
         }
         ProbeParams pp {};
         pp.grids = grids;
@@ -1339,7 +1394,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         LookupParams lp {};
         lp.slots = table.slots.get();
         lp.capMask = table.capMask;
-        lp.entries = table.entries.get();
+        lp.entries = table.entries;
         lp.grids = grids;
         lp.order = order.get();
         lp.workList = pp.workList;
