@@ -27,6 +27,7 @@
 //   shared memory, looked up in the table (16-byte slots: key + range) and each hit's candidate range
 //   is spread across the warp.
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <functional>
 #include <mutex>
@@ -306,27 +307,120 @@ __global__ void runStartsKernel(const uint32_t* __restrict__ flags, const uint32
         starts[runs] = (uint32_t)m;
 }
 
-// One slot per run: (key, first entry | count << 32), and the key's filter bits. The keys are
-// distinct, so inserts contend only where probe sequences meet.
-__global__ void insertRunsKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t runs, ulonglong2* __restrict__ slots,
-    uint32_t capMask, uint32_t* __restrict__ filter, uint32_t filterShift, uint32_t* status)
+// Slot placement for runs sorted by key. A run's home slot is the top log2(cap) bits of its key, so
+// the homes are non-decreasing in run order, and linear probing places run d at
+//   pos_d = max(home_d, pos_{d-1} + 1) = d + max over j <= d of (home_j - j),
+// an inclusive max-scan: no atomics, and the slots are written in increasing order. The slot array
+// ends past max(cap - 1, pos of the last run) with an empty slot, so probes never wrap.
+constexpr int kPlaceThreads = 256;
+constexpr int kPlaceItems = 16;
+constexpr int kPlaceTile = kPlaceThreads * kPlaceItems;
+
+__device__ __forceinline__ long long runHomeMinusIndex(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t d, uint32_t homeShift)
 {
-    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= runs)
-        return;
-    const uint32_t start = starts[d], cnt = starts[d + 1] - start;
-    const uint64_t key = keys[start];
-    uint32_t slot = slotHash(key) & capMask;
-    for (uint32_t probe = 0; probe <= capMask; ++probe) {
-        if (atomicCAS(&slots[slot].x, 0ull, (unsigned long long)key) == 0ull) {
-            slots[slot].y = (uint64_t)start | ((uint64_t)cnt << 32);
-            const uint32_t x = filterFold(key);
-            atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
-            return;
-        }
-        slot = (slot + 1) & capMask;
+    return (long long)(keys[starts[d]] >> homeShift) - (long long)d;
+}
+
+// Block-wide inclusive max-scan of one value per thread (kPlaceThreads threads); returns the
+// exclusive prefix (LLONG_MIN for thread 0) and the block maximum.
+__device__ __forceinline__ long long blockExclusiveMax(long long v, long long* sm, long long& total)
+{
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, inc, o);
+        if ((int)lane >= o)
+            inc = max(inc, t);
     }
-    setDeviceError(status, TDAG_ERR_TABLE_FULL, 201);
+    if (lane == 31)
+        sm[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int NW = kPlaceThreads / 32;
+        long long w = lane < NW ? sm[lane] : LLONG_MIN;
+        long long wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, wi, o);
+            if ((int)lane >= o)
+                wi = max(wi, t);
+        }
+        const long long wex = __shfl_up_sync(0xffffffffu, wi, 1);
+        if (lane < NW)
+            sm[lane] = lane == 0 ? LLONG_MIN : wex;
+        if (lane == NW - 1)
+            sm[NW] = wi;
+    }
+    __syncthreads();
+    const long long ex = __shfl_up_sync(0xffffffffu, inc, 1);
+    const long long res = max(sm[warp], lane == 0 ? LLONG_MIN : ex);
+    total = sm[kPlaceThreads / 32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(kPlaceThreads) runPlaceReduceKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t runs,
+    uint32_t homeShift, long long* __restrict__ tileMax)
+{
+    __shared__ long long sm[kPlaceThreads / 32 + 1];
+    long long m = LLONG_MIN;
+    const uint32_t base = blockIdx.x * kPlaceTile;
+#pragma unroll 4
+    for (int k = 0; k < kPlaceItems; ++k) {
+        const uint32_t d = base + k * kPlaceThreads + threadIdx.x;
+        if (d < runs)
+            m = max(m, runHomeMinusIndex(keys, starts, d, homeShift));
+    }
+    long long total;
+    blockExclusiveMax(m, sm, total);
+    if (threadIdx.x == 0)
+        tileMax[blockIdx.x] = total;
+}
+
+// One block: tileMax becomes its exclusive max-scan; *total = the maximum over all tiles.
+__global__ void __launch_bounds__(kPlaceThreads) tileMaxScanKernel(long long* __restrict__ tileMax, uint32_t numTiles, long long* __restrict__ total)
+{
+    __shared__ long long sm[kPlaceThreads / 32 + 1];
+    long long carry = LLONG_MIN;
+    for (uint32_t b = 0; b < numTiles; b += kPlaceThreads) {
+        const uint32_t i = b + threadIdx.x;
+        const long long v = i < numTiles ? tileMax[i] : LLONG_MIN;
+        long long blockMax;
+        const long long ex = blockExclusiveMax(v, sm, blockMax);
+        if (i < numTiles)
+            tileMax[i] = max(carry, ex);
+        carry = max(carry, blockMax);
+    }
+    if (threadIdx.x == 0)
+        *total = carry;
+}
+
+// Places every run of the tile: slots[pos] = (key, first entry | count << 32), and sets its filter bits.
+__global__ void __launch_bounds__(kPlaceThreads) runPlaceKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t runs,
+    uint32_t homeShift, const long long* __restrict__ tilePrefix, ulonglong2* __restrict__ slots, uint32_t* __restrict__ filter, uint32_t filterShift)
+{
+    __shared__ long long sm[kPlaceThreads / 32 + 1];
+    const uint32_t first = blockIdx.x * kPlaceTile + threadIdx.x * kPlaceItems; // this thread's consecutive runs
+    long long m = LLONG_MIN;
+    for (int k = 0; k < kPlaceItems; ++k) {
+        const uint32_t d = first + k;
+        if (d < runs)
+            m = max(m, runHomeMinusIndex(keys, starts, d, homeShift));
+    }
+    long long total;
+    long long run = max(blockExclusiveMax(m, sm, total), tilePrefix[blockIdx.x]);
+    for (int k = 0; k < kPlaceItems; ++k) {
+        const uint32_t d = first + k;
+        if (d >= runs)
+            break;
+        const uint32_t start = starts[d], cnt = starts[d + 1] - start;
+        const uint64_t key = keys[start];
+        run = max(run, (long long)(key >> homeShift) - (long long)d);
+        slots[(uint64_t)((long long)d + run)] = make_ulonglong2(key, (uint64_t)start | ((uint64_t)cnt << 32));
+        const uint32_t x = filterFold(key);
+        atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
+    }
 }
 
 // Entries still able to receive a lower parent: parent[target] > minKey of the next source batch.
@@ -997,8 +1091,9 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
 struct LookupParams {
     const ulonglong2* recs;
     unsigned long long count;
-    const ulonglong2* slots;
-    uint32_t capMask;
+    const ulonglong2* slots; // run table: home slot = key >> homeShift, slotCount slots
+    uint32_t homeShift;
+    unsigned long long slotCount;
     const uint32_t* entries;
     const uint64_t* grids;
     const uint32_t* order;
@@ -1091,8 +1186,8 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         if (i < p.count) {
             const ulonglong2 rec = p.recs[i];
             meta = rec.y;
-            uint32_t slot = slotHash(rec.x) & p.capMask;
-            for (uint32_t probe = 0; probe <= p.capMask; ++probe) {
+            // from the home slot up to the key or an empty slot (the array ends with one)
+            for (uint64_t slot = rec.x >> p.homeShift; slot < p.slotCount; ++slot) {
                 const ulonglong2 sv = p.slots[slot];
                 if (sv.x == rec.x) {
                     start = (uint32_t)sv.y;
@@ -1101,7 +1196,6 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
                 }
                 if (sv.x == 0)
                     break;
-                slot = (slot + 1) & p.capMask;
             }
         }
         cHit += cnt ? 1u : 0u;
@@ -1186,8 +1280,8 @@ struct Table {
     DevBuf<ulonglong2> slots;
     DevBuf<uint32_t> filter;
     const uint32_t* entries = nullptr;
-    uint32_t capMask = 0, filterShift = 31;
-    uint64_t numEntries = 0, distinct = 0;
+    uint32_t homeShift = 58, filterShift = 31; // home slot = key >> homeShift
+    uint64_t slotCount = 0, numEntries = 0, distinct = 0;
 };
 
 void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, size_t m, Table& t)
@@ -1209,9 +1303,10 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
     const uint32_t loadPct = ctx.tuning.table_load_percent ? std::min(85u, std::max(25u, ctx.tuning.table_load_percent)) : 50u;
     const uint64_t cap = pow2AtLeast(std::max<uint64_t>(64, runs * 100 / loadPct + 1));
     TDAG_CHECK(cap <= (1ull << 31), TDAG_ERR_ARG, "corner-view table too large");
-    t.slots = DevBuf<ulonglong2>(cap, s);
-    t.capMask = (uint32_t)(cap - 1);
-    TDAG_CUDA(cudaMemsetAsync(t.slots.get(), 0, cap * sizeof(ulonglong2), s));
+    uint32_t log2Cap = 0;
+    while ((1ull << log2Cap) < cap)
+        ++log2Cap;
+    t.homeShift = 64 - log2Cap;
     const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
     const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey));
     uint32_t log2F = 0;
@@ -1220,8 +1315,25 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
     t.filterShift = 32 - log2F;
     t.filter = DevBuf<uint32_t>(filterBits / 32, s);
     TDAG_CUDA(cudaMemsetAsync(t.filter.get(), 0, filterBits / 8, s));
+    // slot positions: max-scan of home - index over the runs
+    const uint32_t tiles = (uint32_t)std::max<uint64_t>(1, (runs + kPlaceTile - 1) / kPlaceTile);
+    DevBuf<long long> tileMax(tiles, s), maxAll(1, s);
+    long long maxHomeMinusIndex = 0;
     if (runs) {
-        insertRunsKernel<<<gridFor(runs, 256), 256, 0, s>>>(keys, starts.get(), (uint32_t)runs, t.slots.get(), t.capMask, t.filter.get(), t.filterShift, ctx.status);
+        runPlaceReduceKernel<<<tiles, kPlaceThreads, 0, s>>>(keys, starts.get(), (uint32_t)runs, t.homeShift, tileMax.get());
+        TDAG_LAUNCHED();
+        tileMaxScanKernel<<<1, kPlaceThreads, 0, s>>>(tileMax.get(), tiles, maxAll.get());
+        TDAG_LAUNCHED();
+        TDAG_CUDA(cudaMemcpyAsync(&maxHomeMinusIndex, maxAll.get(), 8, cudaMemcpyDeviceToHost, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+    }
+    // last run at runs - 1 + max(home - index); probes start at homes up to cap - 1; one empty slot after both
+    const uint64_t slotCount = std::max<uint64_t>(cap, runs ? (uint64_t)((long long)runs + maxHomeMinusIndex) : 0) + 1;
+    t.slots = DevBuf<ulonglong2>(slotCount, s);
+    t.slotCount = slotCount;
+    TDAG_CUDA(cudaMemsetAsync(t.slots.get(), 0, slotCount * sizeof(ulonglong2), s));
+    if (runs) {
+        runPlaceKernel<<<tiles, kPlaceThreads, 0, s>>>(keys, starts.get(), (uint32_t)runs, t.homeShift, tileMax.get(), t.slots.get(), t.filter.get(), t.filterShift);
         TDAG_LAUNCHED();
     }
     t.entries = pays;
@@ -1393,7 +1505,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         pp.counters = counters.get();
         LookupParams lp {};
         lp.slots = table.slots.get();
-        lp.capMask = table.capMask;
+        lp.homeShift = table.homeShift;
+        lp.slotCount = table.slotCount;
         lp.entries = table.entries;
         lp.grids = grids;
         lp.order = order.get();
