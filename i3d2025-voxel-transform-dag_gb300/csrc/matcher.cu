@@ -83,6 +83,16 @@ __host__ __device__ __forceinline__ uint32_t filterFold(uint64_t k) { return (ui
 __host__ __device__ __forceinline__ uint32_t filterWordIndex(uint32_t x, uint32_t filterShift) { return (x * 0x9E3779B1u) >> (filterShift + 5); }
 __host__ __device__ __forceinline__ uint32_t filterBits(uint32_t x) { return (1u << (x & 31u)) | (1u << ((x >> 5) & 31u)); }
 
+// Table key of a corner view in the split search: the (salted) hash times an odd constant -- a
+// bijection that spreads the small hashes of boxes whose content starts at their far end (leading
+// empties add nothing to the fold) over the high bits -- cut to its top 40 bits, with bit 0 set so it
+// is never the empty slot 0. A probe looks its box hash up reduced the same way. Matching on 40 bits
+// can only add candidates, which verification rejects; the view sort needs 5 radix digits instead of
+// 8, and the top bits serve as the home slot.
+constexpr uint64_t kViewKeyMask = ~((1ull << 24) - 1);
+constexpr uint32_t kViewKeyLowBit = 24; // the view sort starts at this bit
+__host__ __device__ __forceinline__ uint64_t viewKey(uint64_t h) { return ((h * 0x9E3779B97F4A7C15ull) & kViewKeyMask) | 1ull; }
+
 // Per-grid salt of the box hashes of a batch member: even, so a salted non-empty box hash stays odd
 // and never collides with the empty-slot key 0; 0 for a single grid, leaving the key unchanged.
 __host__ __device__ __forceinline__ uint64_t boxSalt(uint32_t g) { return gridSalt(g) & ~1ull; }
@@ -223,7 +233,7 @@ __global__ void __launch_bounds__(kThreads) cornerViewsKernel(const uint64_t* __
         for (int k = 0; k < R; ++k)
             acc = boxFold<2>(acc, G[(cp >> 2) ? R - 1 - k : k]);
         const size_t e = (size_t)item * views + v;
-        keys[e] = acc ^ salt; // a grid is never empty: acc is odd, and the salt is even
+        keys[e] = viewKey(acc ^ salt);
         payload[e] = (item << 6) | (pb << 3) | cp;
     }
 }
@@ -423,26 +433,37 @@ __global__ void __launch_bounds__(kPlaceThreads) runPlaceKernel(const uint64_t* 
     }
 }
 
-// Entries still able to receive a lower parent: parent[target] > minKey of the next source batch.
-__global__ void liveEntriesKernel(const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay, size_t m, const unsigned long long* __restrict__ parents,
-    unsigned long long minKeyNext, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gridOf, const unsigned long long* __restrict__ minKeyOfGrid)
+// Targets that a source at or after the next batch could still give a lower parent: live[t] = 1 when
+// parent[t] > the next batch's minimum key; *count = the live targets.
+__global__ void targetLiveKernel(const unsigned long long* __restrict__ parents, uint32_t n, unsigned long long minKeyNext, const uint32_t* __restrict__ gridOf,
+    const unsigned long long* __restrict__ minKeyOfGrid, uint8_t* __restrict__ live, uint32_t* __restrict__ count)
 {
-    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= m)
-        return;
-    const uint32_t t = epay[e] >> 6; // payload of a permuted corner view: item << 6 | pidB << 3 | c'
-    const unsigned long long mk = gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext;
-    flags[e] = (ekeys[e] != 0) && (parents[t] > mk);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool l = t < n && parents[t] > (gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext);
+    if (t < n)
+        live[t] = l ? 1 : 0;
+    const uint32_t votes = __ballot_sync(0xffffffffu, l);
+    if ((threadIdx.x & 31) == 0 && votes)
+        atomicAdd(count, (uint32_t)__popc(votes));
 }
 
-__global__ void gatherEntriesKernel(const uint32_t* __restrict__ idx, uint32_t n, const uint64_t* __restrict__ ekeys, const uint32_t* __restrict__ epay,
-    uint64_t* __restrict__ k2, uint32_t* __restrict__ p2)
+// flags[e] = 1 for the entries of live targets (payload of a permuted corner view: item << 6 | view).
+__global__ void entryLiveKernel(const uint32_t* __restrict__ pays, size_t m, const uint8_t* __restrict__ live, uint32_t* __restrict__ flags)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    k2[i] = ekeys[idx[i]];
-    p2[i] = epay[idx[i]];
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m)
+        flags[e] = live[pays[e] >> 6];
+}
+
+// Stable compaction of the flagged entries to their exclusive-scan offsets (keeps the key order).
+__global__ void compactEntriesKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pays, const uint32_t* __restrict__ flags,
+    const uint32_t* __restrict__ offs, size_t m, uint64_t* __restrict__ keysOut, uint32_t* __restrict__ paysOut)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m && flags[e]) {
+        keysOut[offs[e]] = keys[e];
+        paysOut[offs[e]] = pays[e];
+    }
 }
 
 // ---------------------------------------------------------------------------- search
@@ -1024,21 +1045,21 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
 #pragma unroll 1
                         for (int kq = k0 & ~(C - 1); kq < R; kq += C) {
                             uint64_t key[C];
-                            uint32_t word[C], bits[C];
+                            uint32_t word[C], bits[C], nonEmpty = 0;
 #pragma unroll
                             for (int c = 0; c < C; ++c) {
                                 const int w = d2 ? R - 1 - (kq + c) : kq + c;
                                 const uint64_t gv = line3[PS * w];
                                 acc = boxFold<2>(acc, (w >= loZ && w <= hiZ) ? gv : 0ull);
-                                key[c] = SALTED ? acc ^ salt : acc; // the salt is even: bit 0 still says "non-empty"
+                                nonEmpty |= (uint32_t)(acc & 1u) << c;
+                                key[c] = viewKey(SALTED ? acc ^ salt : acc);
                             }
+                            cProbe += __popc(nonEmpty);
 #pragma unroll
                             for (int c = 0; c < C; ++c) {
                                 const uint32_t x = filterFold(key[c]);
                                 bits[c] = filterBits(x);
-                                const bool nonEmpty = key[c] & 1u;
-                                cProbe += nonEmpty ? 1u : 0u;
-                                word[c] = nonEmpty ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
+                                word[c] = ((nonEmpty >> c) & 1u) ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
                             }
                             uint32_t hit = 0;
 #pragma unroll
@@ -1359,6 +1380,19 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const uint32_t* gridOf = batched ? seg->gridOf : nullptr;
     const uint32_t* segOff = batched ? seg->offDev : nullptr;
 
+    // per-stage diagnostics on stderr (TDAG_TRACE)
+    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+    std::vector<std::pair<const char*, cudaEvent_t>> marks;
+    auto mark = [&](const char* name) {
+        if (!trace)
+            return;
+        cudaEvent_t e;
+        TDAG_CUDA(cudaEventCreate(&e));
+        TDAG_CUDA(cudaEventRecord(e, s));
+        marks.emplace_back(name, e);
+    };
+    mark("start");
+
     // popcount order (grid by grid in a batch)
     DevBuf<uint32_t> order(n, s);
     {
@@ -1377,8 +1411,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const size_t m = (size_t)n * perms * 8;
     DevBuf<uint64_t> ekeys(m, s);
     DevBuf<uint32_t> epay(m, s);
+    mark("order");
     cornerViewsKernel<R><<<gridFor(n, kThreads / 32), kThreads, 0, s>>>(grids, n, perms, ekeys.get(), epay.get(), gridOf);
     TDAG_LAUNCHED();
+    mark("views");
 
     const uint64_t sentinelKey = encodeFixed64(0xFFFFFFFFull, 0, 0, 0, 0, 0, L);
     DevBuf<unsigned long long> parents(n, s);
@@ -1439,9 +1475,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         TDAG_CUDA(cudaMemcpyAsync(workListDev.get(), workList.data(), workList.size() * 4, cudaMemcpyHostToDevice, s));
 
     // equal view keys side by side (the sort is stable: a run keeps item order)
-    radixSortPairs(ekeys.get(), epay.get(), m, 0, 64, s);
+    radixSortPairs(ekeys.get(), epay.get(), m, kViewKeyLowBit, 64, s);
+    mark("view sort");
     Table table;
     buildRunTable(ctx, ekeys.get(), epay.get(), m, table);
+    mark("table");
     const uint64_t entriesInitial = table.numEntries;
     float searchMs = 0;
     DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
@@ -1453,6 +1491,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     uint64_t* spareKeys = k2.get();
     uint32_t* sparePays = p2.get();
     size_t mCur = m;
+    DevBuf<uint8_t> targetLive(n, s);
+    DevBuf<uint32_t> liveCount(1, s);
     uint32_t maxBatch = 1;
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi)
         maxBatch = std::max(maxBatch, bounds[bi + 1] - bounds[bi]);
@@ -1462,7 +1502,6 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     double recsPerSource = R * R * 2.0; // first estimate; then a running average of the probed ranges
     unsigned long long probeCounts[2] = { 0, 0 }; // probes and filter passes before the current range
     // per-batch diagnostics on stderr (TDAG_TRACE): probe and lookup time, records
-    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
     cudaEvent_t traceEv[2] = { nullptr, nullptr };
     if (trace)
         for (auto& e : traceEv)
@@ -1480,13 +1519,16 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
             }
-            liveEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, mCur, parents.get(), minKeyNext, flags.get(), gridOf,
-                batched ? minKeyDev.get() : nullptr);
+            TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 4, s));
+            targetLiveKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, minKeyNext, gridOf, batched ? minKeyDev.get() : nullptr, targetLive.get(),
+                liveCount.get());
             TDAG_LAUNCHED();
-            const uint32_t live = compactFlags(flags.get(), liveIdx.get(), mCur, s);
+            entryLiveKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curPays, mCur, targetLive.get(), flags.get());
+            TDAG_LAUNCHED();
+            const uint64_t live = exclusiveScanU32Total(flags.get(), liveIdx.get(), mCur, s);
             if (live == 0)
                 break;
-            gatherEntriesKernel<<<gridFor(live, 256), 256, 0, s>>>(liveIdx.get(), live, curKeys, curPays, spareKeys, sparePays);
+            compactEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, flags.get(), liveIdx.get(), mCur, spareKeys, sparePays);
             TDAG_LAUNCHED();
             std::swap(curKeys, spareKeys);
             std::swap(curPays, sparePays);
@@ -1610,6 +1652,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     k2.release();
     p2.release();
 
+    mark("batches");
     // resolve
     DevBuf<uint64_t> parentTP(n, s);
     DevBuf<uint32_t> isUnique(n, s), newIdx(n, s);
@@ -1638,6 +1681,21 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         stats->verified += c[5];
         stats->table_entries += entriesInitial;
         stats->search_ms += searchMs;
+    }
+    mark("resolve");
+    if (trace) {
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        std::string line = "[tdag] L" + std::to_string(L) + " stages ms:";
+        for (size_t k = 1; k < marks.size(); ++k) {
+            float ms = 0;
+            TDAG_CUDA(cudaEventElapsedTime(&ms, marks[k - 1].second, marks[k].second));
+            char buf[64];
+            std::snprintf(buf, sizeof buf, " %s %.3f", marks[k].first, ms);
+            line += buf;
+        }
+        std::fprintf(stderr, "%s (search %.3f)\n", line.c_str(), searchMs);
+        for (auto& mk : marks)
+            cudaEventDestroy(mk.second);
     }
     ctx.checkStatus("matcher level " + std::to_string(L));
     return out;
