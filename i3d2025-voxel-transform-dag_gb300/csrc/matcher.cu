@@ -1440,7 +1440,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
     const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
-    // Source batches. Single grid: doubling ranges of sorted positions, starting at eight teams per SM
+    // Source batches. Single grid: ranges of sorted positions growing eightfold (every batch costs a
+    // table rebuild, so a few large batches beat many small ones), starting at eight teams per SM
     // (fixed, so that the schedule does not move with the probe kernel's occupancy). Batch: the same fractions of every grid (1/256, 1/128, ..., 1/2, 1), as a list of sorted
     // positions per batch, with each grid's own next-batch start for the pruning keys.
     std::vector<uint32_t> bounds { 0 };
@@ -1450,7 +1451,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, n / 256);
         while (bounds.back() < n) {
             const uint32_t b = bounds.back();
-            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 2ull * b)));
+            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 8ull * b)));
         }
     } else {
         constexpr int kBatches = 9;
