@@ -10,8 +10,10 @@ available). SVO build and toDAG happen once before timing.
 value   : solid input voxels / device time of the build, input and output resident in HBM.
 e2e     : the same through tdag_build() with pinned host buffers: host->device copy of the SVDAG,
           the build, and the device->host copy of the Transform DAG inside the timed region.
-roofline: the dominant kernel (the translation search of the level with the largest device time),
-          algorithmic bytes per launch / its CUDA-event duration, against MEASURED_PEAKS.json.
+roofline: the dominant kernel -- the translation probe kernel of the level with the largest probe
+          time -- algorithmic DRAM bytes over its CUDA-event device time, against MEASURED_PEAKS.json;
+          beside it (l2_probe) its filter loads per second against this GPU's random-load ceiling for
+          L2-resident buffers (tdag_l2_probe_peak), the resource that actually bounds it.
 cpu_baseline / --impl reference: the CPU oracle (a restatement of the reference's CPU path, all
           host threads) on a bounded sub-volume sample of the same grid.
 
@@ -326,11 +328,25 @@ def choose_sample(host, requested: int, budget_s: float):
 GRID_BYTES = {2: 8, 3: 64, 4: 512}
 
 
-def search_algorithmic_bytes(level: int, st: dict) -> float:
-    """Translation search of one level: every source grid read once (M*G), one 16-byte (hash, range)
-    table slot per non-empty probe (P*16), two grids per verification (V*2G)."""
+def probe_algorithmic_bytes(level: int, st: dict) -> float:
+    """Probe kernel of one level (DRAM): every source grid read once (M*G), its three line
+    orientations written for verification (M*3R^2*2), one 16-byte record per filter survivor (F*16).
+    The filter words the probes read (4 bytes each) stay in L2 and are counted in l2_probe instead."""
+    R = 1 << level
     G = GRID_BYTES[level]
-    return st["items"] * G + st["probes"] * 16 + st["verifications"] * 2 * G
+    return st["items"] * G + st["items"] * 3 * R * R * 2 + st["filter_pass"] * 16
+
+
+def l2_probe_peak(ctx) -> float:
+    """Random 4-byte loads per second from an L2-resident buffer: the maximum over 4, 16 and 64 MiB."""
+    import tdag
+    from tdag import _abi
+    best = 0.0
+    for mib in (4, 16, 64):
+        v = ctypes.c_double(0.0)
+        _abi.check(tdag.lib().tdag_l2_probe_peak(ctx.handle, mib << 20, 1 << 30, ctypes.byref(v)))
+        best = max(best, v.value)
+    return best
 
 
 def load_peaks():
@@ -343,7 +359,8 @@ def load_peaks():
 
 
 def load_traffic(level: int):
-    p = os.path.join(REPO, "profiles", "search_traffic.json")
+    """DRAM bytes (read + write) of the level's probe launches from an ncu capture, if recorded."""
+    p = os.path.join(REPO, "profiles", "probe_traffic.json")
     if not os.path.exists(p):
         return None
     try:
@@ -481,17 +498,24 @@ def run_ours(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, e2e_s)
     e2e_value = voxels * args.steps * world / e2e_s / 1e6
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel: the probe kernel of the level with the largest probe time
     last = stats_list[-1]
     lvl_times = {L: sum(s["translation"][L]["search_ms"] for s in stats_list) / len(stats_list) for L in (2, 3, 4)}
-    dom = max(lvl_times, key=lambda L: lvl_times[L])
-    ms = lvl_times[dom]
-    alg = search_algorithmic_bytes(dom, last["translation"][dom])
+    probe_times = {L: sum(s["translation"][L]["probe_ms"] for s in stats_list) / len(stats_list) for L in (2, 3, 4)}
+    dom = max(probe_times, key=lambda L: probe_times[L])
+    ms = probe_times[dom]
+    st = last["translation"][dom]
+    alg = probe_algorithmic_bytes(dom, st)
     achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else None
     peak, peak_kind = load_peaks()
-    roof = {"bound": "hbm", "kernel": f"searchKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
+    l2_peak = l2_probe_peak(ctx)
+    probes_per_s = st["probes"] / (ms / 1e3) if ms > 0 else None
+    roof = {"bound": "hbm", "kernel": f"probeKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-            "traffic": load_traffic(dom), "algorithmic_bytes_per_launch": alg, "launch_ms": ms}
+            "traffic": load_traffic(dom), "algorithmic_bytes": alg, "device_ms": ms,
+            "l2_probe": {"achieved_loads_per_s": probes_per_s, "peak_loads_per_s": l2_peak,
+                         "frac": (probes_per_s / l2_peak) if probes_per_s and l2_peak else None,
+                         "peak_source": "tdag_l2_probe_peak on this GPU (max over 4/16/64 MiB buffers)"}}
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -504,7 +528,8 @@ def run_ours(args, world, rank, local, pg):
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats_list)),
         "subgrids_matched_per_s": sum(last["translation"][L]["items"] for L in (2, 3, 4)) / (dev_ms / args.steps / 1e3),
         "stage_ms": {"hierarchical": last["hierarchical_ms"], "translation": last["translation_ms"],
-                     "search_L4": lvl_times[4], "search_L3": lvl_times[3], "search_L2": lvl_times[2]},
+                     "search_L4": lvl_times[4], "search_L3": lvl_times[3], "search_L2": lvl_times[2],
+                     "probe_L4": probe_times[4], "probe_L3": probe_times[3], "probe_L2": probe_times[2]},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc

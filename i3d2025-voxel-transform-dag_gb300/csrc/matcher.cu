@@ -406,30 +406,57 @@ __global__ void __launch_bounds__(kPlaceThreads) tileMaxScanKernel(long long* __
         *total = carry;
 }
 
-// Places every run of the tile: slots[pos] = (key, first entry | count << 32), and sets its filter bits.
+// Places every run of the tile: slots[pos] = (key, first entry | count << 32), and sets its filter
+// bits. Warp w owns the tile's runs [w * 512, (w + 1) * 512), 32 consecutive runs per step (coalesced):
+// a first sweep gives the warps' maxima, a second scans with a carried prefix and writes.
 __global__ void __launch_bounds__(kPlaceThreads) runPlaceKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ starts, uint32_t runs,
     uint32_t homeShift, const long long* __restrict__ tilePrefix, ulonglong2* __restrict__ slots, uint32_t* __restrict__ filter, uint32_t filterShift)
 {
-    __shared__ long long sm[kPlaceThreads / 32 + 1];
-    const uint32_t first = blockIdx.x * kPlaceTile + threadIdx.x * kPlaceItems; // this thread's consecutive runs
+    constexpr int WARPS = kPlaceThreads / 32, STEPS = kPlaceTile / kPlaceThreads; // 512 runs per warp
+    __shared__ long long warpMax[WARPS];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t segBase = blockIdx.x * kPlaceTile + warp * (32 * STEPS);
     long long m = LLONG_MIN;
-    for (int k = 0; k < kPlaceItems; ++k) {
-        const uint32_t d = first + k;
+    for (int it = 0; it < STEPS; ++it) {
+        const uint32_t d = segBase + it * 32 + lane;
         if (d < runs)
             m = max(m, runHomeMinusIndex(keys, starts, d, homeShift));
     }
-    long long total;
-    long long run = max(blockExclusiveMax(m, sm, total), tilePrefix[blockIdx.x]);
-    for (int k = 0; k < kPlaceItems; ++k) {
-        const uint32_t d = first + k;
-        if (d >= runs)
-            break;
-        const uint32_t start = starts[d], cnt = starts[d + 1] - start;
-        const uint64_t key = keys[start];
-        run = max(run, (long long)(key >> homeShift) - (long long)d);
-        slots[(uint64_t)((long long)d + run)] = make_ulonglong2(key, (uint64_t)start | ((uint64_t)cnt << 32));
-        const uint32_t x = filterFold(key);
-        atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0)
+        warpMax[warp] = m;
+    __syncthreads();
+    long long carry = tilePrefix[blockIdx.x];
+    for (uint32_t w = 0; w < warp; ++w)
+        carry = max(carry, warpMax[w]);
+    for (int it = 0; it < STEPS; ++it) {
+        const uint32_t d = segBase + it * 32 + lane;
+        const bool valid = d < runs;
+        uint32_t start = 0, cnt = 0;
+        uint64_t key = 0;
+        long long v = LLONG_MIN;
+        if (valid) {
+            start = starts[d];
+            cnt = starts[d + 1] - start;
+            key = keys[start];
+            v = (long long)(key >> homeShift) - (long long)d;
+        }
+        long long inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, inc, o);
+            if ((int)lane >= o)
+                inc = max(inc, t);
+        }
+        if (valid) {
+            const long long run = max(carry, inc);
+            slots[(uint64_t)((long long)d + run)] = make_ulonglong2(key, (uint64_t)start | ((uint64_t)cnt << 32));
+            const uint32_t x = filterFold(key);
+            atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
+        }
+        carry = max(carry, __shfl_sync(0xffffffffu, inc, 31));
     }
 }
 
@@ -1482,7 +1509,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     buildRunTable(ctx, ekeys.get(), epay.get(), m, table);
     mark("table");
     const uint64_t entriesInitial = table.numEntries;
-    float searchMs = 0;
+    float searchMs = 0, probeMs = 0;
     DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
     DevBuf<uint64_t> k2(m, s);
     DevBuf<uint32_t> p2(m, s);
@@ -1500,7 +1527,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint16_t> srcLines((size_t)maxBatch * 3 * R * R, s);
     DevBuf<ulonglong2> recs;
     DevBuf<unsigned long long> recCount(1, s);
-    double recsPerSource = R * R * 2.0; // first estimate; then a running average of the probed ranges
+    double recsPerSource = 2.0 * R * R * R; // first estimate (the first batch's big sources pass the filter most); then a running average
     unsigned long long probeCounts[2] = { 0, 0 }; // probes and filter passes before the current range
     // per-batch diagnostics on stderr (TDAG_TRACE): probe and lookup time, records
     cudaEvent_t traceEv[2] = { nullptr, nullptr };
@@ -1581,17 +1608,16 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemsetAsync(recCount.get(), 0, 8, s));
                 const uint64_t groups = ((uint64_t)cs + ProbeShape<R>::TEAMS - 1) / ProbeShape<R>::TEAMS;
                 const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
-                if (trace)
-                    TDAG_CUDA(cudaEventRecord(traceEv[0], s));
+                TDAG_CUDA(cudaEventRecord(ctx.ev[5], s)); // ev[2..4] time the build's stages
                 probe<<<blocks, kThreads, smem, s>>>(pp);
                 TDAG_LAUNCHED();
-                if (trace)
-                    TDAG_CUDA(cudaEventRecord(traceEv[1], s));
+                TDAG_CUDA(cudaEventRecord(ctx.ev[6], s));
                 TDAG_CUDA(cudaMemcpyAsync(&produced, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
-                if (trace) {
-                    float pm = 0;
-                    TDAG_CUDA(cudaEventElapsedTime(&pm, traceEv[0], traceEv[1]));
+                {
+                    float pm = 0; // the stream was synchronised for the record count
+                    TDAG_CUDA(cudaEventElapsedTime(&pm, ctx.ev[5], ctx.ev[6]));
+                    probeMs += pm;
                     traceProbeMs += pm;
                 }
                 if (produced <= pp.recCap)
@@ -1682,6 +1708,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         stats->verified += c[5];
         stats->table_entries += entriesInitial;
         stats->search_ms += searchMs;
+        stats->probe_ms += probeMs;
     }
     mark("resolve");
     if (trace) {

@@ -44,7 +44,7 @@ class LevelStats(ctypes.Structure):
     _fields_ = [("items", ctypes.c_uint64), ("unique", ctypes.c_uint64), ("probes", ctypes.c_uint64),
                 ("filter_pass", ctypes.c_uint64), ("hits", ctypes.c_uint64), ("candidates", ctypes.c_uint64),
                 ("verifications", ctypes.c_uint64), ("verified", ctypes.c_uint64),
-                ("table_entries", ctypes.c_uint64), ("search_ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+                ("table_entries", ctypes.c_uint64), ("search_ms", ctypes.c_float), ("probe_ms", ctypes.c_float)]
 
 
 class Stats(ctypes.Structure):
@@ -86,6 +86,7 @@ EXPORTED = (
     "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
     "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
+    "tdag_l2_probe_peak",  # include/tdag_diag.h
 )
 
 _lib = None
@@ -127,6 +128,7 @@ def lib(path: str = None):
         L.tdag_find_duplicates_level_noalloc.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.POINTER(Config),
                                                          vp, vp, vp]
         L.tdag_result_to_host.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(ctypes.POINTER(Result))]
+        L.tdag_l2_probe_peak.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

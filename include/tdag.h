@@ -68,9 +68,9 @@ typedef struct tdag_level_stats {
     uint64_t candidates; /* candidate (target, corner) pairs examined */
     uint64_t verifications; /* exact grid comparisons */
     uint64_t verified; /* comparisons that matched */
-    uint64_t table_entries; /* non-zero corner hashes in the table */
-    float search_ms; /* device time of the search kernel(s) */
-    float reserved;
+    uint64_t table_entries; /* corner views in the table (translation levels) */
+    float search_ms; /* device time of the search kernels (probe and lookup) */
+    float probe_ms; /* device time of the probe kernel alone */
 } tdag_level_stats;
 
 typedef struct tdag_stats {
