@@ -16,6 +16,9 @@
 // Child codes: a child pointer (h, tau) with canonical invariance group Inv(h) is represented by
 // (h, min ID of the coset tau * Inv(h)), which is equal for two pointers exactly when
 // TaggedPointer::operator== (:79-122) says they are equal.
+#include <cstdlib>
+#include <utility>
+
 #include "common.cuh"
 #include "internal.cuh"
 #include "class_table.cuh"
@@ -516,6 +519,20 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
     HierOutput out;
     out.levels.resize(in.rootLevel + 1);
     out.handleOff.resize(in.rootLevel + 1);
+    // per-level diagnostics on stderr (TDAG_TRACE): device time, items and kept items
+    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+    std::vector<cudaEvent_t> traceEv;
+    std::vector<std::pair<uint64_t, uint64_t>> traceCounts;
+    auto traceMark = [&](uint64_t items, uint64_t kept) {
+        if (!trace)
+            return;
+        cudaEvent_t e;
+        TDAG_CUDA(cudaEventCreate(&e));
+        TDAG_CUDA(cudaEventRecord(e, s));
+        traceEv.push_back(e);
+        traceCounts.emplace_back(items, kept);
+    };
+    traceMark(0, 0);
     DevBuf<uint64_t> prevMap, prevInv;
     DevBuf<uint32_t> prevHandleOffDev;
     auto uploadOffsets = [&](const std::vector<uint64_t>& off) {
@@ -552,6 +569,7 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
             stats->hierarchical[2].items = n;
             stats->hierarchical[2].unique = u;
         }
+        traceMark(n, u);
     }
     for (uint32_t level = 3; level <= in.rootLevel; ++level) {
         const uint32_t n = (uint32_t)in.nodeCounts[level];
@@ -594,6 +612,22 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
             stats->hierarchical[level].items = n;
             stats->hierarchical[level].unique = u;
         }
+        traceMark(n, u);
+    }
+    if (trace) {
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        std::string line = "[tdag] hierarchical ms (items -> kept):";
+        for (size_t k = 1; k < traceEv.size(); ++k) {
+            float ms = 0;
+            TDAG_CUDA(cudaEventElapsedTime(&ms, traceEv[k - 1], traceEv[k]));
+            char buf[96];
+            std::snprintf(buf, sizeof buf, " L%zu %.3f (%llu -> %llu)", k + 1, ms, (unsigned long long)traceCounts[k].first,
+                (unsigned long long)traceCounts[k].second);
+            line += buf;
+        }
+        std::fprintf(stderr, "%s\n", line.c_str());
+        for (auto e : traceEv)
+            cudaEventDestroy(e);
     }
     return out;
 }

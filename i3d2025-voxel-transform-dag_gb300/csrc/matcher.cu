@@ -1469,8 +1469,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
 
     // Source batches. Single grid: ranges of sorted positions growing eightfold (every batch costs a
     // table rebuild, so a few large batches beat many small ones), starting at eight teams per SM
-    // (fixed, so that the schedule does not move with the probe kernel's occupancy). Batch: the same fractions of every grid (1/256, 1/128, ..., 1/2, 1), as a list of sorted
-    // positions per batch, with each grid's own next-batch start for the pruning keys.
+    // (fixed, so that the schedule does not move with the probe kernel's occupancy). Batch: the same
+    // fractions of every grid (1/512, 1/64, 1/8, 1), as a list of sorted positions per batch, with
+    // each grid's own next-batch start for the pruning keys.
     std::vector<uint32_t> bounds { 0 };
     std::vector<uint32_t> workList;
     std::vector<std::vector<unsigned long long>> minKeys; // per batch, per grid
@@ -1481,8 +1482,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 8ull * b)));
         }
     } else {
-        constexpr int kBatches = 9;
-        auto frac = [](uint64_t cnt, int k) { return k == 0 ? 0ull : (k >= kBatches ? cnt : (cnt >> (kBatches - k))); };
+        constexpr int kBatches = 4; // fractions 1/512, 1/64, 1/8, 1: eightfold growth, as for a single grid
+        auto frac = [](uint64_t cnt, int k) { return k == 0 ? 0ull : (k >= kBatches ? cnt : (cnt >> (3 * (kBatches - k)))); };
         workList.reserve(n);
         for (int k = 0; k < kBatches; ++k) {
             std::vector<unsigned long long> mk(numGrids);

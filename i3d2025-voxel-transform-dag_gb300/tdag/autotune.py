@@ -14,9 +14,9 @@ from typing import Dict, List, Optional, Sequence, Tuple
 import tdag
 
 DEFAULT_SPACE = {
-    "table_load_percent": (50, 70, 85),
-    "filter_bits_per_key": (16, 32, 64),
-    "search_ctas_per_sm": (1, 2),
+    "table_load_percent": (50, 70),
+    "filter_bits_per_key": (16, 32),
+    "search_ctas_per_sm": (2, 3, 4),
 }
 
 
