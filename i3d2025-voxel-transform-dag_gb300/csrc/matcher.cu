@@ -1247,24 +1247,30 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
             }
         }
         cHit += cnt ? 1u : 0u;
-        // short ranges: every lane walks its own hit's candidates
-        constexpr uint32_t kSerialMax = 8;
-        if (cnt != 0 && cnt <= kSerialMax) {
-            const Src s = source(meta);
-            for (uint32_t e = 0; e < cnt; ++e)
-                candidate(__ldg(&p.entries[start + e]), s);
+        // The warp's candidates, all hits' ranges end to end, dealt 32 at a time over the lanes: lane
+        // j's hit is the first lane whose inclusive prefix of counts exceeds j (binary search by shuffles).
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o)
+                incl += t;
         }
-        // long ranges: the warp walks one range at a time
-        uint32_t hitMask = __ballot_sync(0xffffffffu, cnt > kSerialMax);
-        while (hitMask) {
-            const int src = __ffs(hitMask) - 1;
-            hitMask &= hitMask - 1;
-            const uint32_t bs = __shfl_sync(0xffffffffu, start, src);
-            const uint32_t bc = __shfl_sync(0xffffffffu, cnt, src);
-            const uint64_t bm = __shfl_sync(0xffffffffu, meta, src);
-            const Src s = source(bm);
-            for (uint32_t e = lane; e < bc; e += 32)
-                candidate(__ldg(&p.entries[bs + e]), s);
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t excl = incl - cnt;
+        for (uint32_t jb = 0; jb < total; jb += 32) {
+            const uint32_t j = jb + lane;
+            uint32_t h = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, incl, h + step - 1) <= j)
+                    h += step;
+            h = min(h, 31u); // lanes past the total search to 32
+            const uint32_t hs = __shfl_sync(0xffffffffu, start, h);
+            const uint32_t hx = __shfl_sync(0xffffffffu, excl, h);
+            const uint64_t hm = __shfl_sync(0xffffffffu, meta, h);
+            if (j < total)
+                candidate(__ldg(&p.entries[hs + (j - hx)]), source(hm));
         }
     }
     const uint32_t vals[4] = { cHit, cCand, cVer, cOk };
