@@ -40,6 +40,8 @@ const TransformTables& hostTables()
             const uint32_t sa = a & 7, pa = a >> 3;
             for (uint32_t i = 0; i < 8; ++i)
                 tt.pos[a][i] = (uint8_t)(applyPerm(i, pa) ^ sa);
+            for (uint32_t i = 0; i < 8; ++i)
+                tt.invPos[a][tt.pos[a][i]] = (uint8_t)i;
             for (uint32_t b = 0; b < 48; ++b) {
                 const uint32_t sb = b & 7, pb = b >> 3;
                 // (a∘b)(v) = Pa(Pb(v)) ^ Pa(Sb) ^ Sa ; (Pa∘Pb)[k] = pb[pa[k]]

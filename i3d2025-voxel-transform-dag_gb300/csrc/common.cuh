@@ -177,6 +177,7 @@ struct TransformTables {
     uint8_t compose[48][48]; // compose[a][b] = a ∘ b
     uint8_t inverse[48];
     uint8_t pos[48][8]; // image of a 2x2x2 child index
+    uint8_t invPos[48][8]; // invPos[t][pos[t][i]] = i
     uint8_t byteMap[48][256]; // image of a 2x2x2 occupancy byte (bit i = child i)
 };
 const TransformTables& hostTables();

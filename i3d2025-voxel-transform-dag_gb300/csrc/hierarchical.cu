@@ -33,6 +33,7 @@ struct SmemTables {
     uint8_t compose[48][48];
     uint8_t inverse[48];
     uint8_t pos[48][8];
+    uint8_t invPos[48][8];
 };
 
 __device__ __forceinline__ void loadTables(SmemTables& s, const TransformTables* g)
@@ -43,8 +44,10 @@ __device__ __forceinline__ void loadTables(SmemTables& s, const TransformTables*
         dst[i] = src[i];
     for (int i = threadIdx.x; i < 48; i += blockDim.x)
         s.inverse[i] = g->inverse[i];
-    for (int i = threadIdx.x; i < 48 * 8; i += blockDim.x)
+    for (int i = threadIdx.x; i < 48 * 8; i += blockDim.x) {
         (&s.pos[0][0])[i] = (&g->pos[0][0])[i];
+        (&s.invPos[0][0])[i] = (&g->invPos[0][0])[i];
+    }
 }
 
 // Transform of a 4x4x4 Morton mask: byte k is the 2x2x2 block at child position k; the transform
@@ -60,19 +63,23 @@ __device__ __forceinline__ uint64_t transformLeaf(uint64_t m, uint32_t t, const 
     return out;
 }
 
+__device__ __forceinline__ void compareExchange(uint64_t& a, uint64_t& b)
+{
+    const uint64_t lo = a < b ? a : b;
+    b = a < b ? b : a;
+    a = lo;
+}
+
 __device__ __forceinline__ uint64_t sortedPtrHash(uint64_t p[8])
 {
-    // insertion sort of 8 values, then hash_combine over them (:365-377)
-#pragma unroll
-    for (int i = 1; i < 8; ++i) {
-        uint64_t v = p[i];
-        int j = i - 1;
-        while (j >= 0 && p[j] > v) {
-            p[j + 1] = p[j];
-            --j;
-        }
-        p[j + 1] = v;
-    }
+    // sort the 8 child pointers ascending, then hash_combine over them (:365-377); a fixed
+    // 19-comparator sorting network keeps the array in registers
+    compareExchange(p[0], p[2]); compareExchange(p[1], p[3]); compareExchange(p[4], p[6]); compareExchange(p[5], p[7]);
+    compareExchange(p[0], p[4]); compareExchange(p[1], p[5]); compareExchange(p[2], p[6]); compareExchange(p[3], p[7]);
+    compareExchange(p[0], p[1]); compareExchange(p[2], p[3]); compareExchange(p[4], p[5]); compareExchange(p[6], p[7]);
+    compareExchange(p[2], p[4]); compareExchange(p[3], p[5]);
+    compareExchange(p[1], p[4]); compareExchange(p[3], p[6]);
+    compareExchange(p[1], p[2]); compareExchange(p[3], p[4]); compareExchange(p[5], p[6]);
     uint64_t seed = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
@@ -200,11 +207,36 @@ __device__ __forceinline__ uint64_t childCode(const Child& c, uint32_t t, const 
     return ((uint64_t)c.h << 6) | rep;
 }
 
-__device__ __forceinline__ void transformedCodes(const Child ch[8], uint32_t t, const SmemTables& st, uint64_t allowed, uint64_t out[8])
+// A thread's 8 children, kept in shared memory so that they can be gathered by a runtime position
+// (a register array indexed at run time would live in local memory).
+struct ChildSlots {
+    uint32_t h[8][kThreads];
+    uint8_t tau[8][kThreads];
+    uint64_t inv[8][kThreads];
+    __device__ void put(int k, const Child& c)
+    {
+        h[k][threadIdx.x] = c.h;
+        tau[k][threadIdx.x] = (uint8_t)c.tau;
+        inv[k][threadIdx.x] = c.inv;
+    }
+    __device__ Child get(int k) const { return Child { h[k][threadIdx.x], tau[k][threadIdx.x], inv[k][threadIdx.x] }; }
+};
+
+// Codes of the 8 children after transform t, in output position order: out[j] is the child that t
+// moves to position j.
+__device__ __forceinline__ void transformedCodes(const ChildSlots& cs, uint32_t t, const SmemTables& st, uint64_t allowed, uint64_t out[8])
 {
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-        out[st.pos[t][k]] = childCode(ch[k], t, st, allowed);
+    for (int j = 0; j < 8; ++j)
+        out[j] = childCode(cs.get(st.invPos[t][j]), t, st, allowed);
+}
+
+// The identity's codes straight from registers (position j holds child j).
+__device__ __forceinline__ void identityCodes(const Child ch[8], const SmemTables& st, uint64_t allowed, uint64_t out[8])
+{
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        out[j] = childCode(ch[j], 0, st, allowed);
 }
 
 __device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8])
@@ -222,6 +254,7 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
     const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff)
 {
     __shared__ SmemTables st;
+    __shared__ ChildSlots cs;
     loadTables(st, tables);
     __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,15 +268,16 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         ch[k] = loadChild(node, k, prevMap, prevInv);
+        cs.put(k, ch[k]);
         p[k] = ch[k].h == kEmpty32 ? (uint64_t)kEmpty32 : (uint64_t)(ch[k].h - hbase);
     }
     key[i] = sortedPtrHash(p);
     uint64_t best[8], cur[8];
-    transformedCodes(ch, 0, st, allowed, best);
+    identityCodes(ch, st, allowed, best);
     for (uint32_t t = 1; t < 48; ++t) {
         if (!((allowed >> t) & 1))
             continue;
-        transformedCodes(ch, t, st, allowed, cur);
+        transformedCodes(cs, t, st, allowed, cur);
         if (lexLess(cur, best)) {
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -264,6 +298,7 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
     uint32_t* __restrict__ isCanon, uint32_t level, uint32_t* status)
 {
     __shared__ SmemTables st;
+    __shared__ ChildSlots cs;
     loadTables(st, tables);
     __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -273,16 +308,18 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
     canonOf[i] = c;
     Child ch[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 8; ++k) {
         ch[k] = loadChild(nodes + (size_t)i * 8, k, prevMap, prevInv);
+        cs.put(k, ch[k]);
+    }
     uint64_t target[8], cur[8];
     if (c == i) {
-        transformedCodes(ch, 0, st, allowed, target);
+        identityCodes(ch, st, allowed, target);
         uint64_t inv = 1; // identity
         for (uint32_t t = 1; t < 48; ++t) {
             if (!((allowed >> t) & 1))
                 continue;
-            transformedCodes(ch, t, st, allowed, cur);
+            transformedCodes(cs, t, st, allowed, cur);
             bool eq = true;
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -298,12 +335,12 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             cc[k] = loadChild(nodes + (size_t)c * 8, k, prevMap, prevInv);
-        transformedCodes(cc, 0, st, allowed, target);
+        identityCodes(cc, st, allowed, target);
         uint32_t found = 0xFF;
         for (uint32_t t = 0; t < 48; ++t) {
             if (!((allowed >> t) & 1))
                 continue;
-            transformedCodes(ch, t, st, allowed, cur);
+            transformedCodes(cs, t, st, allowed, cur);
             bool eq = true;
 #pragma unroll
             for (int k = 0; k < 8; ++k)
