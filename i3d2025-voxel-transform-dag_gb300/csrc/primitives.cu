@@ -220,22 +220,32 @@ __global__ void radixHistKernel(const uint64_t* __restrict__ keys, size_t n, uin
     counts[(size_t)threadIdx.x * numTiles + blockIdx.x] = hist[threadIdx.x];
 }
 
-__global__ void radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn, uint64_t* __restrict__ keysOut,
-    uint32_t* __restrict__ valsOut, size_t n, uint32_t shift, const uint32_t* __restrict__ offsets, uint32_t numTiles)
+// Stable scatter of one tile: items are ranked by digit as in the histogram pass (warp-major,
+// then round, then lane == tile order), placed in shared memory in (digit, rank) order, and written
+// out digit run by digit run, so consecutive threads store consecutive addresses.
+constexpr size_t kScatterSmem = (size_t)kSortTile * (8 + 4) + (size_t)(kSortWarps + 2) * 256 * 4;
+
+__global__ void __launch_bounds__(kSortThreads) radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+    uint64_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut, size_t n, uint32_t shift, const uint32_t* __restrict__ offsets, uint32_t numTiles)
 {
-    __shared__ uint32_t warpHist[kSortWarps][256];
-    __shared__ uint32_t base[kSortWarps][256];
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t* sk = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kSortTile);
+    uint32_t (*warpBase)[256] = reinterpret_cast<uint32_t (*)[256]>(sv + kSortTile);
+    uint32_t* tileStart = &warpBase[kSortWarps][0];
+    uint32_t* globalBase = tileStart + 256;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads)
-        (&warpHist[0][0])[d] = 0;
+        (&warpBase[0][0])[d] = 0;
     __syncthreads();
-    const size_t warpBase = (size_t)blockIdx.x * kSortTile + (size_t)warp * (32 * kSortRounds);
+    const size_t tileBase = (size_t)blockIdx.x * kSortTile;
+    const size_t warpItems = tileBase + (size_t)warp * (32 * kSortRounds);
     uint64_t key[kSortRounds];
     uint32_t val[kSortRounds];
     const uint32_t ltMask = (1u << lane) - 1u;
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
-        const size_t i = warpBase + (size_t)r * 32 + lane;
+        const size_t i = warpItems + (size_t)r * 32 + lane;
         const bool valid = i < n;
         key[r] = valid ? keysIn[i] : 0;
         val[r] = valid ? valsIn[i] : 0;
@@ -243,38 +253,71 @@ __global__ void radixScatterKernel(const uint64_t* __restrict__ keysIn, const ui
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
         if (valid && (peers & ltMask) == 0)
-            warpHist[warp][digit] += __popc(peers);
+            warpBase[warp][digit] += __popc(peers);
         __syncwarp();
     }
     __syncthreads();
     {
+        // thread d: the tile's count of digit d, its exclusive prefix over digits, and the warps'
+        // starting ranks within the digit
         const uint32_t d = threadIdx.x; // 256 threads == 256 digits
-        uint32_t run = offsets[(size_t)d * numTiles + blockIdx.x];
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w)
+            cnt += warpBase[w][d];
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o)
+                incl += t;
+        }
+        __shared__ uint32_t warpTotals[kSortWarps];
+        if (lane == 31)
+            warpTotals[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; ++w)
+            before += warpTotals[w];
+        const uint32_t start = before + incl - cnt;
+        tileStart[d] = start;
+        globalBase[d] = offsets[(size_t)d * numTiles + blockIdx.x];
+        uint32_t run = start;
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) {
-            base[w][d] = run;
-            run += warpHist[w][d];
+            const uint32_t c = warpBase[w][d];
+            warpBase[w][d] = run;
+            run += c;
         }
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
-        const size_t i = warpBase + (size_t)r * 32 + lane;
+        const size_t i = warpItems + (size_t)r * 32 + lane;
         const bool valid = i < n;
         const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
         uint32_t pos = 0;
         if (valid)
-            pos = base[warp][digit] + __popc(peers & ltMask);
+            pos = warpBase[warp][digit] + __popc(peers & ltMask);
         __syncwarp();
         if (valid && (peers & ltMask) == 0)
-            base[warp][digit] += __popc(peers);
+            warpBase[warp][digit] += __popc(peers);
         __syncwarp();
         if (valid) {
-            keysOut[pos] = key[r];
-            valsOut[pos] = val[r];
+            sk[pos] = key[r];
+            sv[pos] = val[r];
         }
+    }
+    __syncthreads();
+    const uint32_t tileItems = (uint32_t)((n - tileBase) < (size_t)kSortTile ? (n - tileBase) : (size_t)kSortTile);
+    for (uint32_t i = threadIdx.x; i < tileItems; i += kSortThreads) {
+        const uint64_t k = sk[i];
+        const uint32_t d = (uint32_t)(k >> shift) & 0xFF;
+        const uint32_t out = globalBase[d] + (i - tileStart[d]);
+        keysOut[out] = k;
+        valsOut[out] = sv[i];
     }
 }
 } // namespace
@@ -285,6 +328,14 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
         return;
     TDAG_CHECK(n < (1ull << 32), TDAG_ERR_ARG, "radix sort size exceeds 2^32");
     const uint32_t numTiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+    static bool smemSet[64] = {}; // the shared-memory limit is set once per device
+    int dev = 0;
+    TDAG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !smemSet[dev]) {
+        TDAG_CUDA(cudaFuncSetAttribute(radixScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
+        if (dev >= 0 && dev < 64)
+            smemSet[dev] = true;
+    }
     DevBuf<uint64_t> k2(n, s);
     DevBuf<uint32_t> v2(n, s);
     DevBuf<uint32_t> counts((size_t)256 * numTiles, s), offs((size_t)256 * numTiles, s);
@@ -297,7 +348,7 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
         radixHistKernel<<<numTiles, kSortThreads, 0, s>>>(kin, n, shift, counts.get(), numTiles);
         TDAG_LAUNCHED();
         exclusiveScanU32(counts.get(), offs.get(), (size_t)256 * numTiles, s);
-        radixScatterKernel<<<numTiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
+        radixScatterKernel<<<numTiles, kSortThreads, kScatterSmem, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
         TDAG_LAUNCHED();
         std::swap(kin, kout);
         std::swap(vin, vout);
