@@ -172,39 +172,46 @@ __global__ void __launch_bounds__(kThreads) leafResolveKernel(const uint64_t* __
 struct Child {
     uint32_t h; // handle at the level below (0xFFFFFFFF: empty)
     uint32_t tau; // transform ID of the child pointer
-    uint64_t inv; // invariance mask of the child's canonical
 };
 
-__device__ __forceinline__ Child loadChild(const uint32_t* __restrict__ node, int k, const uint64_t* __restrict__ prevMap, const uint64_t* __restrict__ prevInv)
+__device__ __forceinline__ Child loadChild(const uint32_t* __restrict__ node, int k, const uint64_t* __restrict__ prevMap)
 {
     const uint32_t c = node[k];
     if (c == kEmpty32)
-        return Child { kEmpty32, 0, ~0ull };
+        return Child { kEmpty32, 0 };
     const uint64_t tp = prevMap[c];
-    const uint32_t h = (uint32_t)tpPtr(tp);
-    return Child { h, tpTransformId(tp), prevInv[h] };
+    return Child { (uint32_t)tpPtr(tp), tpTransformId(tp) };
+}
+
+// Coset representatives of the level's kept nodes: rep[h * 48 + tau] = the smallest transform ID in
+// tau ∘ Inv(h), Inv(h) the invariance group of canonical h. Two child pointers (h, tau), (h, tau')
+// denote the same child exactly when their cosets agree (transform_dag_hierarchical.cpp:70-123).
+__global__ void cosetRepKernel(const uint64_t* __restrict__ inv, uint32_t u, const TransformTables* __restrict__ tables, uint8_t* __restrict__ rep)
+{
+    __shared__ uint8_t compose[48][48];
+    for (int i = threadIdx.x; i < 48 * 48; i += blockDim.x)
+        (&compose[0][0])[i] = (&tables->compose[0][0])[i];
+    __syncthreads();
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)u * 48)
+        return;
+    const uint32_t h = (uint32_t)(i / 48), tau = (uint32_t)(i % 48);
+    uint64_t bits = inv[h];
+    uint32_t r = 63;
+    while (bits) {
+        const uint32_t g = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        r = compose[tau][g] < r ? compose[tau][g] : r;
+    }
+    rep[i] = (uint8_t)r;
 }
 
 // code of child (h, t ∘ tau) with coset normalisation
-__device__ __forceinline__ uint64_t childCode(const Child& c, uint32_t t, const SmemTables& st, uint64_t allowed)
+__device__ __forceinline__ uint64_t childCode(const Child& c, uint32_t t, const SmemTables& st, const uint8_t* __restrict__ rep)
 {
     if (c.h == kEmpty32)
         return (uint64_t)kEmpty32 << 6;
-    const uint32_t tau = st.compose[t][c.tau];
-    uint32_t rep;
-    if (c.inv == allowed) {
-        rep = 0;
-    } else {
-        rep = 63;
-        uint64_t bits = c.inv;
-        while (bits) {
-            const uint32_t g = __ffsll((long long)bits) - 1;
-            bits &= bits - 1;
-            const uint32_t v = st.compose[tau][g];
-            rep = v < rep ? v : rep;
-        }
-    }
-    return ((uint64_t)c.h << 6) | rep;
+    return ((uint64_t)c.h << 6) | __ldg(&rep[(size_t)c.h * 48 + st.compose[t][c.tau]]);
 }
 
 // A thread's 8 children, kept in shared memory so that they can be gathered by a runtime position
@@ -212,31 +219,29 @@ __device__ __forceinline__ uint64_t childCode(const Child& c, uint32_t t, const 
 struct ChildSlots {
     uint32_t h[8][kThreads];
     uint8_t tau[8][kThreads];
-    uint64_t inv[8][kThreads];
     __device__ void put(int k, const Child& c)
     {
         h[k][threadIdx.x] = c.h;
         tau[k][threadIdx.x] = (uint8_t)c.tau;
-        inv[k][threadIdx.x] = c.inv;
     }
-    __device__ Child get(int k) const { return Child { h[k][threadIdx.x], tau[k][threadIdx.x], inv[k][threadIdx.x] }; }
+    __device__ Child get(int k) const { return Child { h[k][threadIdx.x], tau[k][threadIdx.x] }; }
 };
 
 // Codes of the 8 children after transform t, in output position order: out[j] is the child that t
 // moves to position j.
-__device__ __forceinline__ void transformedCodes(const ChildSlots& cs, uint32_t t, const SmemTables& st, uint64_t allowed, uint64_t out[8])
+__device__ __forceinline__ void transformedCodes(const ChildSlots& cs, uint32_t t, const SmemTables& st, const uint8_t* __restrict__ rep, uint64_t out[8])
 {
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-        out[j] = childCode(cs.get(st.invPos[t][j]), t, st, allowed);
+        out[j] = childCode(cs.get(st.invPos[t][j]), t, st, rep);
 }
 
 // The identity's codes straight from registers (position j holds child j).
-__device__ __forceinline__ void identityCodes(const Child ch[8], const SmemTables& st, uint64_t allowed, uint64_t out[8])
+__device__ __forceinline__ void identityCodes(const Child ch[8], const SmemTables& st, const uint8_t* __restrict__ rep, uint64_t out[8])
 {
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-        out[j] = childCode(ch[j], 0, st, allowed);
+        out[j] = childCode(ch[j], 0, st, rep);
 }
 
 __device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8])
@@ -250,7 +255,7 @@ __device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8]
 }
 
 __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
-    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key,
+    const uint8_t* __restrict__ prevRep, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key,
     const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff)
 {
     __shared__ SmemTables st;
@@ -267,17 +272,17 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
     const uint32_t hbase = gridOf ? prevHandleOff[gridOf[i]] : 0u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        ch[k] = loadChild(node, k, prevMap, prevInv);
+        ch[k] = loadChild(node, k, prevMap);
         cs.put(k, ch[k]);
         p[k] = ch[k].h == kEmpty32 ? (uint64_t)kEmpty32 : (uint64_t)(ch[k].h - hbase);
     }
     key[i] = sortedPtrHash(p);
     uint64_t best[8], cur[8];
-    identityCodes(ch, st, allowed, best);
+    identityCodes(ch, st, prevRep, best);
     for (uint32_t t = 1; t < 48; ++t) {
         if (!((allowed >> t) & 1))
             continue;
-        transformedCodes(cs, t, st, allowed, cur);
+        transformedCodes(cs, t, st, prevRep, cur);
         if (lexLess(cur, best)) {
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
 }
 
 __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
-    const uint64_t* __restrict__ prevInv, const TransformTables* __restrict__ tables, uint64_t allowed, const uint32_t* __restrict__ slotOf,
+    const uint8_t* __restrict__ prevRep, const TransformTables* __restrict__ tables, uint64_t allowed, const uint32_t* __restrict__ slotOf,
     const uint32_t* __restrict__ minIdx, uint32_t* __restrict__ canonOf, uint8_t* __restrict__ tOf, uint64_t* __restrict__ invOf,
     uint32_t* __restrict__ isCanon, uint32_t level, uint32_t* status)
 {
@@ -309,17 +314,17 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
     Child ch[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        ch[k] = loadChild(nodes + (size_t)i * 8, k, prevMap, prevInv);
+        ch[k] = loadChild(nodes + (size_t)i * 8, k, prevMap);
         cs.put(k, ch[k]);
     }
     uint64_t target[8], cur[8];
     if (c == i) {
-        identityCodes(ch, st, allowed, target);
+        identityCodes(ch, st, prevRep, target);
         uint64_t inv = 1; // identity
         for (uint32_t t = 1; t < 48; ++t) {
             if (!((allowed >> t) & 1))
                 continue;
-            transformedCodes(cs, t, st, allowed, cur);
+            transformedCodes(cs, t, st, prevRep, cur);
             bool eq = true;
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -334,13 +339,13 @@ __global__ void __launch_bounds__(kThreads) nodeResolveKernel(const uint32_t* __
         Child cc[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            cc[k] = loadChild(nodes + (size_t)c * 8, k, prevMap, prevInv);
-        identityCodes(cc, st, allowed, target);
+            cc[k] = loadChild(nodes + (size_t)c * 8, k, prevMap);
+        identityCodes(cc, st, prevRep, target);
         uint32_t found = 0xFF;
         for (uint32_t t = 0; t < 48; ++t) {
             if (!((allowed >> t) & 1))
                 continue;
-            transformedCodes(cs, t, st, allowed, cur);
+            transformedCodes(cs, t, st, prevRep, cur);
             bool eq = true;
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -571,6 +576,14 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
     };
     traceMark(0, 0);
     DevBuf<uint64_t> prevMap, prevInv;
+    DevBuf<uint8_t> prevRep; // coset representatives of the level below's kept nodes
+    auto buildRep = [&](uint32_t u) {
+        prevRep = DevBuf<uint8_t>((size_t)u * 48, s);
+        if (u) {
+            cosetRepKernel<<<gridFor((size_t)u * 48, 256), 256, 0, s>>>(prevInv.get(), u, ctx.tables, prevRep.get());
+            TDAG_LAUNCHED();
+        }
+    };
     DevBuf<uint32_t> prevHandleOffDev;
     auto uploadOffsets = [&](const std::vector<uint64_t>& off) {
         DevBuf<uint32_t> d(off.size(), s);
@@ -602,6 +615,7 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
             emitLeavesKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, in.leaves, out.leaves.get());
             TDAG_LAUNCHED();
         }
+        buildRep(u);
         if (stats) {
             stats->hierarchical[2].items = n;
             stats->hierarchical[2].unique = u;
@@ -617,14 +631,14 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
             prevHandleOffDev = uploadOffsets(out.handleOff[level - 1]);
         DevBuf<uint64_t> sig((size_t)n * sw, s), key(n, s);
         if (n) {
-            nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevInv.get(), ctx.tables, allowed, sig.get(), key.get(), gridOf,
+            nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevRep.get(), ctx.tables, allowed, sig.get(), key.get(), gridOf,
                 gridOf ? prevHandleOffDev.get() : nullptr);
             TDAG_LAUNCHED();
         }
         const uint64_t* pm = prevMap.get();
-        const uint64_t* pi = prevInv.get();
+        const uint8_t* pr = prevRep.get();
         auto resolve = [&](const uint32_t* slotOf, const uint32_t* minIdx, uint32_t* canonOf, uint8_t* tOf, uint64_t* invOf, uint32_t* isCanon) {
-            nodeResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, pm, pi, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, level, ctx.status);
+            nodeResolveKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, pm, pr, ctx.tables, allowed, slotOf, minIdx, canonOf, tOf, invOf, isCanon, level, ctx.status);
             TDAG_LAUNCHED();
         };
         DevBuf<uint64_t> map, inv;
@@ -645,6 +659,8 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         }
         prevMap = std::move(map);
         prevInv = std::move(inv);
+        if (level < in.rootLevel)
+            buildRep(u);
         if (stats) {
             stats->hierarchical[level].items = n;
             stats->hierarchical[level].unique = u;
