@@ -1473,8 +1473,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
     const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
-    // Source batches. Single grid: ranges of sorted positions growing eightfold (every batch costs a
-    // table rebuild, so a few large batches beat many small ones), starting at eight teams per SM
+    // Source batches. Single grid: ranges of sorted positions growing 8x (levels 2-3: 16x; every batch
+    // costs a table rebuild, so a few large batches beat many small ones), starting at eight teams per SM
     // (fixed, so that the schedule does not move with the probe kernel's occupancy). Batch: the same
     // fractions of every grid (1/512, 1/64, 1/8, 1), as a list of sorted positions per batch, with
     // each grid's own next-batch start for the pruning keys.
@@ -1483,9 +1483,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     std::vector<std::vector<unsigned long long>> minKeys; // per batch, per grid
     if (!batched) {
         const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, n / 256);
+        const uint64_t growth = R == 16 ? 8 : 16; // smaller grids probe faster, so their rebuilds weigh more
         while (bounds.back() < n) {
             const uint32_t b = bounds.back();
-            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, 8ull * b)));
+            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, growth * b)));
         }
     } else {
         constexpr int kBatches = 4; // fractions 1/512, 1/64, 1/8, 1: eightfold growth, as for a single grid
