@@ -9,10 +9,12 @@
 //      transform_dag.cpp:44-116, 417-441), run the matcher, keep the unique items (:208-221) and
 //      rewrite the parents' child pointers through the mapping (:224-233; the lower_bound lookup is
 //      a rank array here).
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -582,6 +584,8 @@ int tdag_ctx_destroy(tdag_ctx* ctx)
         cudaFree(c.status);
     if (c.hostStatus)
         cudaFreeHost(c.hostStatus);
+    if (c.stage)
+        cudaFreeHost(c.stage);
     if (c.stream)
         cudaStreamDestroy(c.stream);
     delete ctx;
@@ -595,6 +599,69 @@ int tdag_ctx_stream(tdag_ctx* ctx, void** out)
     *out = (void*)ctx->c.stream;
     return TDAG_OK;
 }
+
+namespace {
+// Copies device arrays into host (pageable) arrays through the context's pinned staging buffer. A
+// D2H copy into pinned memory runs at link speed; one straight into freshly allocated pageable pages
+// goes page by page through the driver and took ~20 ms for a 32 MB result. The host copies out of
+// the stage run on a few threads for large results.
+struct Download {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+
+void downloadStaged(tdag::Context& c, const std::vector<Download>& items)
+{
+    using namespace tdag;
+    size_t total = 0;
+    for (const auto& d : items)
+        total += (d.bytes + 255) & ~(size_t)255;
+    if (total == 0)
+        return;
+    if (total > c.stageBytes) {
+        if (c.stage)
+            TDAG_CUDA(cudaFreeHost(c.stage));
+        c.stage = nullptr;
+        c.stageBytes = 0;
+        const size_t want = total + total / 4;
+        TDAG_CUDA(cudaMallocHost(&c.stage, want));
+        c.stageBytes = want;
+    }
+    size_t off = 0;
+    for (const auto& d : items) {
+        if (d.bytes)
+            TDAG_CUDA(cudaMemcpyAsync(static_cast<char*>(c.stage) + off, d.src, d.bytes, cudaMemcpyDeviceToHost, c.stream));
+        off += (d.bytes + 255) & ~(size_t)255;
+    }
+    TDAG_CUDA(cudaStreamSynchronize(c.stream));
+    // host copies, split into chunks over up to 8 threads
+    struct Piece {
+        char* dst;
+        const char* src;
+        size_t bytes;
+    };
+    std::vector<Piece> pieces;
+    constexpr size_t kChunk = 4u << 20;
+    off = 0;
+    for (const auto& d : items) {
+        for (size_t o = 0; o < d.bytes; o += kChunk)
+            pieces.push_back({ static_cast<char*>(d.dst) + o, static_cast<const char*>(c.stage) + off + o, std::min(kChunk, d.bytes - o) });
+        off += (d.bytes + 255) & ~(size_t)255;
+    }
+    const unsigned workers = (unsigned)std::min<size_t>({ pieces.size(), (size_t)8, (size_t)std::max(1u, std::thread::hardware_concurrency()) });
+    auto work = [&](unsigned w) {
+        for (size_t i = w; i < pieces.size(); i += workers)
+            std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+    };
+    std::vector<std::thread> threads;
+    for (unsigned w = 1; w < workers; ++w)
+        threads.emplace_back(work, w);
+    work(0);
+    for (auto& t : threads)
+        t.join();
+}
+} // namespace
 
 int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
 {
@@ -631,6 +698,8 @@ int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg,
         Context& c = ctx->c;
         cudaStream_t s = c.stream;
         TDAG_CUDA(cudaSetDevice(c.device));
+        const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+        const auto t0 = std::chrono::steady_clock::now();
         Upload up;
         up.nodes.resize(in->root_level + 1);
         tdag_svdag_view dv = *in;
@@ -646,21 +715,28 @@ int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg,
             TDAG_CUDA(cudaMemcpyAsync(up.leaves.get(), in->leaves, in->leaf_count * 8, cudaMemcpyHostToDevice, s));
         dv.leaves = up.leaves.get();
         std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, false));
+        const auto t1 = std::chrono::steady_clock::now();
         DeviceResult dr = buildDevice(c, viewToDevice(&dv), *cfg, &r->stats);
+        const auto t2 = std::chrono::steady_clock::now();
+        std::vector<Download> dl;
         for (uint32_t l = 3; l <= in->root_level; ++l) {
             const size_t cnt = dr.levels[l].n / 8;
             r->node_counts[l] = cnt;
             r->nodes[l] = (uint64_t*)std::malloc(cnt ? cnt * 64 : 1);
             TDAG_CHECK(r->nodes[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
-            if (cnt)
-                TDAG_CUDA(cudaMemcpyAsync(r->nodes[l], dr.levels[l].get(), cnt * 64, cudaMemcpyDeviceToHost, s));
+            dl.push_back({ r->nodes[l], dr.levels[l].get(), cnt * 64 });
         }
         r->leaf_count = dr.leaves.n;
         r->leaves = (uint64_t*)std::malloc(dr.leaves.n ? dr.leaves.n * 8 : 1);
         TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
-        if (dr.leaves.n)
-            TDAG_CUDA(cudaMemcpyAsync(r->leaves, dr.leaves.get(), dr.leaves.n * 8, cudaMemcpyDeviceToHost, s));
-        TDAG_CUDA(cudaStreamSynchronize(s));
+        dl.push_back({ r->leaves, dr.leaves.get(), dr.leaves.n * 8 });
+        downloadStaged(c, dl);
+        if (trace) { // host-side phases: upload enqueue, build (to its return), download
+            const auto t3 = std::chrono::steady_clock::now();
+            auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+            std::fprintf(stderr, "[tdag] tdag_build host ms: upload %.3f build %.3f download %.3f (device total %.3f)\n", ms(t0, t1), ms(t1, t2), ms(t2, t3),
+                r->stats.total_ms);
+        }
         *out = r.release();
     });
 }
@@ -689,6 +765,7 @@ static int buildBatched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count
         std::memset(&st, 0, sizeof(st));
         DeviceResult dr = buildDevice(c, b.view, *cfg, &st);
         std::vector<std::unique_ptr<tdag_result>> res(count);
+        std::vector<Download> dl;
         for (uint32_t g = 0; g < count; ++g) {
             res[g].reset(newResult(in[g].resolution, in[g].root_level, !host));
             res[g]->stats = st;
@@ -712,10 +789,14 @@ static int buildBatched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count
                     res[g]->nodes[l] = dst;
                     res[g]->node_counts[l] = cnt;
                 }
-                if (bytes)
-                    TDAG_CUDA(cudaMemcpyAsync(dst, src + first * words, bytes, host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+                if (host)
+                    dl.push_back({ dst, src + first * words, bytes });
+                else if (bytes)
+                    TDAG_CUDA(cudaMemcpyAsync(dst, src + first * words, bytes, cudaMemcpyDeviceToDevice, s));
             }
         }
+        if (host)
+            downloadStaged(c, dl);
         TDAG_CUDA(cudaStreamSynchronize(s));
         for (uint32_t g = 0; g < count; ++g)
             out[g] = res[g].release();
@@ -755,20 +836,19 @@ int tdag_result_to_host(tdag_ctx* ctx, const tdag_result* d, tdag_result** out)
         std::unique_ptr<tdag_result> r(newResult(d->resolution, d->root_level, false));
         r->structure_type = d->structure_type;
         r->stats = d->stats;
+        std::vector<Download> dl;
         for (uint32_t l = 3; l <= d->root_level; ++l) {
             const size_t bytes = d->node_counts[l] * 64;
             r->node_counts[l] = d->node_counts[l];
             r->nodes[l] = (uint64_t*)std::malloc(bytes ? bytes : 1);
             TDAG_CHECK(r->nodes[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
-            if (bytes)
-                TDAG_CUDA(cudaMemcpyAsync(r->nodes[l], d->nodes[l], bytes, cudaMemcpyDeviceToHost, c.stream));
+            dl.push_back({ r->nodes[l], d->nodes[l], bytes });
         }
         r->leaf_count = d->leaf_count;
         r->leaves = (uint64_t*)std::malloc(d->leaf_count ? d->leaf_count * 8 : 1);
         TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
-        if (d->leaf_count)
-            TDAG_CUDA(cudaMemcpyAsync(r->leaves, d->leaves, d->leaf_count * 8, cudaMemcpyDeviceToHost, c.stream));
-        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+        dl.push_back({ r->leaves, d->leaves, d->leaf_count * 8 });
+        downloadStaged(c, dl);
         *out = r.release();
     });
 }

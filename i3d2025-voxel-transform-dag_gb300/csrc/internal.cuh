@@ -17,6 +17,8 @@ struct Context {
     tdag_tuning tuning {};
     int numSMs = 0;
     cudaEvent_t ev[8] {};
+    void* stage = nullptr; // pinned staging buffer of host-bound results (grown on demand)
+    size_t stageBytes = 0;
 
     // Synchronise the stream, read the device status word, throw on a recorded error.
     void checkStatus(const std::string& where);
