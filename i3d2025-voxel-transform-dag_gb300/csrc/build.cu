@@ -221,8 +221,14 @@ static DevBuf<uint32_t> uploadU32(const std::vector<uint64_t>& v, cudaStream_t s
     return d;
 }
 
+// Learned-proposal hook of a build (tdag_build_device_proposed): picks each level's searching sources.
+struct ProposalHook {
+    tdag_proposal_fn fn = nullptr;
+    void* user = nullptr;
+};
+
 template <int L>
-static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& out, const tdag_config& cfg, tdag_stats* stats)
+static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& out, const tdag_config& cfg, tdag_stats* stats, const ProposalHook& hook)
 {
     cudaStream_t s = ctx.stream;
     const uint64_t numItems = (L == 2) ? in.leafCount : in.nodeCounts[L];
@@ -266,7 +272,17 @@ static void translationLevel(Context& ctx, const DeviceSvdag& in, DeviceResult& 
         sg.offDev = offM.get();
     }
     tdag_level_stats* ls = stats ? &stats->translation[L] : nullptr;
-    MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls, &sg);
+    DevBuf<uint32_t> proposed;
+    uint32_t numProposed = 0;
+    if (hook.fn && m) {
+        TDAG_CHECK(in.numGrids == 1, TDAG_ERR_ARG, "proposal hooks apply to single-grid builds");
+        proposed = DevBuf<uint32_t>(m, s);
+        TDAG_CUDA(cudaStreamSynchronize(s)); // the hook reads the grids from its own stream
+        const int rc = hook.fn(hook.user, L, grids.get(), m, proposed.get(), &numProposed);
+        TDAG_CHECK(rc == 0, TDAG_ERR_ARG, "proposal function failed");
+        TDAG_CHECK(numProposed <= m, TDAG_ERR_ARG, "proposal function returned more sources than items");
+    }
+    MatchOutput mo = runMatcher(ctx, L, grids.get(), m, cfg, ls, &sg, hook.fn ? proposed.get() : nullptr, numProposed);
     grids.release();
     out.off[L] = mo.uniqueOff.empty() ? std::vector<uint64_t>(in.numGrids + 1, 0) : mo.uniqueOff;
     const uint32_t u = mo.numUnique;
@@ -306,7 +322,7 @@ static void validateInput(Context& ctx, const DeviceSvdag& in)
     ctx.checkStatus("input validation");
 }
 
-static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, tdag_stats* stats)
+static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, tdag_stats* stats, const ProposalHook& hook = ProposalHook {})
 {
     TDAG_CHECK(in.rootLevel >= 2 && in.rootLevel < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "root_level out of range");
     TDAG_CHECK(in.numGrids > 1 || in.resolution == (1u << in.rootLevel), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
@@ -343,11 +359,11 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
         h.midInv.release();
         for (int L = (int)cfg.max_translation_level; L >= 2; --L) {
             if (L == 4)
-                translationLevel<4>(ctx, in, out, cfg, stats);
+                translationLevel<4>(ctx, in, out, cfg, stats, hook);
             else if (L == 3)
-                translationLevel<3>(ctx, in, out, cfg, stats);
+                translationLevel<3>(ctx, in, out, cfg, stats, hook);
             else
-                translationLevel<2>(ctx, in, out, cfg, stats);
+                translationLevel<2>(ctx, in, out, cfg, stats, hook);
         }
     }
     TDAG_CUDA(cudaEventRecord(ctx.ev[4], s));
@@ -688,6 +704,30 @@ int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_confi
     });
 }
 
+int tdag_build_device_proposed(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_proposal_fn fn, void* user, tdag_result** out)
+{
+    if (!ctx || !cfg || !out || !fn)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        checkView(in);
+        Context& c = ctx->c;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, true));
+        DeviceResult dr = buildDevice(c, viewToDevice(in), *cfg, &r->stats, ProposalHook { fn, user });
+        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+        for (uint32_t l = 3; l <= in->root_level; ++l) {
+            r->node_counts[l] = dr.levels[l].n / 8;
+            r->nodes[l] = dr.levels[l].p;
+            dr.levels[l].p = nullptr;
+        }
+        r->leaf_count = dr.leaves.n;
+        r->leaves = dr.leaves.p;
+        dr.leaves.p = nullptr;
+        *out = r.release();
+    });
+}
+
 int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
 {
     if (!ctx || !cfg || !out)
@@ -898,6 +938,43 @@ int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* gr
         }
         TDAG_CUDA(cudaStreamSynchronize(s));
         *nUnique = mo.numUnique;
+        if (stats)
+            *stats = ls;
+    });
+}
+
+int tdag_device_copy(tdag_ctx* ctx, void* d_dst, const void* d_src, uint64_t bytes)
+{
+    if (!ctx || (bytes && (!d_dst || !d_src)))
+        return fail(TDAG_ERR_ARG, "null argument");
+    return guarded([&] {
+        Context& c = ctx->c;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        if (bytes)
+            TDAG_CUDA(cudaMemcpyAsync(d_dst, d_src, bytes, cudaMemcpyDeviceToDevice, c.stream));
+        TDAG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int tdag_find_duplicates_level_device(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n, const tdag_config* cfg, const uint32_t* d_sources,
+    uint32_t num_sources, uint64_t* d_out_mapping, uint32_t* d_out_unique, uint32_t* n_unique, tdag_level_stats* stats)
+{
+    if (!ctx || !cfg || !n_unique || (n && (!d_grids || !d_out_mapping || !d_out_unique)) || (num_sources && !d_sources))
+        return fail(TDAG_ERR_ARG, "null argument");
+    return guarded([&] {
+        TDAG_CHECK(level >= 2 && level <= 4, TDAG_ERR_ARG, "level must be 2..4");
+        Context& c = ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        tdag_level_stats ls {};
+        MatchOutput mo = runMatcher(c, level, d_grids, n, *cfg, &ls, nullptr, d_sources, d_sources ? num_sources : 0);
+        if (n) {
+            TDAG_CUDA(cudaMemcpyAsync(d_out_mapping, mo.mapping.get(), (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+            if (mo.numUnique)
+                TDAG_CUDA(cudaMemcpyAsync(d_out_unique, mo.uniques.get(), (size_t)mo.numUnique * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        *n_unique = mo.numUnique;
         if (stats)
             *stats = ls;
     });

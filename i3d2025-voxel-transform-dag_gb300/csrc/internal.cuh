@@ -86,9 +86,11 @@ void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s);
 HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, uint32_t midLevel, tdag_stats* stats);
 
 // findDuplicatesAmongFlattenedItems on n dense grids of level `level` (device pointer, n x W words).
-// seg (optional) splits the items into independent grids of a batch.
+// seg (optional) splits the items into independent grids of a batch. sources (optional, device, a
+// single grid only) restricts the searching sources to numSources item indices: every item is still
+// a target and its own candidate, but only the listed items probe (the learned-proposal mode).
 MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats,
-    const Segments* seg = nullptr);
+    const Segments* seg = nullptr, const uint32_t* sources = nullptr, uint32_t numSources = 0);
 
 // Segment helpers: per-item grid ids from offsets, per-grid counts of a grid-id list.
 void segmentIds(const uint32_t* offDev, uint32_t numGrids, uint64_t n, uint32_t* out, cudaStream_t s);

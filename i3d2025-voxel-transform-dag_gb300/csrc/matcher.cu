@@ -460,6 +460,33 @@ __global__ void __launch_bounds__(kPlaceThreads) runPlaceKernel(const uint64_t* 
     }
 }
 
+// rank[order[p]] = p: every item's position in popcount order.
+__global__ void sortedPositionKernel(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ rank)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n)
+        rank[order[p]] = p;
+}
+
+// The listed sources' sorted positions, as keys and values of an ascending sort; an index past the
+// level's items records an argument error (and sorts last).
+__global__ void gatherPositionsKernel(const uint32_t* __restrict__ sources, uint32_t m, const uint32_t* __restrict__ rank, uint32_t n,
+    uint64_t* __restrict__ key, uint32_t* __restrict__ val, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const uint32_t src = sources[i];
+    if (src >= n) {
+        setDeviceError(status, TDAG_ERR_ARG, 301);
+        key[i] = 0xFFFFFFFFull;
+        val[i] = 0;
+        return;
+    }
+    key[i] = rank[src];
+    val[i] = rank[src];
+}
+
 // Targets that a source at or after the next batch could still give a lower parent: live[t] = 1 when
 // parent[t] > the next batch's minimum key; *count = the live targets.
 __global__ void targetLiveKernel(const unsigned long long* __restrict__ parents, uint32_t n, unsigned long long minKeyNext, const uint32_t* __restrict__ gridOf,
@@ -1397,7 +1424,8 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
 }
 
 template <int L>
-MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg)
+MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg,
+    const uint32_t* sources, uint32_t numSources)
 {
     constexpr int R = 1 << L;
     constexpr int W = R * R * R / 64;
@@ -1410,6 +1438,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         return out;
     }
     TDAG_CHECK(n < (1u << 29), TDAG_ERR_ARG, "too many items for one matcher level");
+    TDAG_CHECK(!sources || !batched, TDAG_ERR_ARG, "a source subset applies to a single grid");
     const uint32_t* gridOf = batched ? seg->gridOf : nullptr;
     const uint32_t* segOff = batched ? seg->offDev : nullptr;
 
@@ -1436,6 +1465,25 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         while (batched && (1ull << (bits - 13)) < numGrids)
             bits += 8;
         radixSortPairs(key.get(), order.get(), n, 0, bits, s);
+    }
+
+    // learned-proposal mode: the sorted positions of the listed sources, ascending, as the work list
+    std::vector<uint32_t> subsetHost;
+    DevBuf<uint32_t> subsetDev;
+    if (sources) {
+        DevBuf<uint32_t> rank(n, s);
+        sortedPositionKernel<<<gridFor(n, 256), 256, 0, s>>>(order.get(), n, rank.get());
+        TDAG_LAUNCHED();
+        DevBuf<uint64_t> sk(std::max<uint32_t>(numSources, 1), s);
+        subsetDev = DevBuf<uint32_t>(std::max<uint32_t>(numSources, 1), s);
+        if (numSources) {
+            gatherPositionsKernel<<<gridFor(numSources, 256), 256, 0, s>>>(sources, numSources, rank.get(), n, sk.get(), subsetDev.get(), ctx.status);
+            TDAG_LAUNCHED();
+            radixSortPairs(sk.get(), subsetDev.get(), numSources, 0, 32, s);
+            subsetHost.resize(numSources);
+            TDAG_CUDA(cudaMemcpyAsync(subsetHost.data(), subsetDev.get(), (size_t)numSources * 4, cudaMemcpyDeviceToHost, s));
+        }
+        ctx.checkStatus("proposed sources");
     }
 
     // permuted corner views: 48 per item (8 when axis permutation is off: only the identity order)
@@ -1481,12 +1529,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     std::vector<uint32_t> bounds { 0 };
     std::vector<uint32_t> workList;
     std::vector<std::vector<unsigned long long>> minKeys; // per batch, per grid
+    // (the positions batched over: sorted positions, or indices into the subset's work list)
+    const uint32_t nSrc = sources ? numSources : n;
     if (!batched) {
-        const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, n / 256);
+        const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, nSrc / 256);
         const uint64_t growth = R == 16 ? 8 : 16; // smaller grids probe faster, so their rebuilds weigh more
-        while (bounds.back() < n) {
+        while (bounds.back() < nSrc) {
             const uint32_t b = bounds.back();
-            bounds.push_back((uint32_t)std::min<uint64_t>(n, std::max<uint64_t>((uint64_t)b + minBatch, growth * b)));
+            bounds.push_back((uint32_t)std::min<uint64_t>(nSrc, std::max<uint64_t>((uint64_t)b + minBatch, growth * b)));
         }
     } else {
         constexpr int kBatches = 4; // fractions 1/512, 1/64, 1/8, 1: eightfold growth, as for a single grid
@@ -1550,7 +1600,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             continue;
         if (bi > 0) {
             // drop targets whose parent no source at or after this batch can lower
-            const unsigned long long minKeyNext = encodeFixed64(b0, 0, 0, 1 - R, 1 - R, 1 - R, L);
+            const unsigned long long minKeyNext = encodeFixed64(sources ? subsetHost[b0] : b0, 0, 0, 1 - R, 1 - R, 1 - R, L);
             if (batched) {
                 TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
@@ -1574,7 +1624,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         ProbeParams pp {};
         pp.grids = grids;
         pp.order = order.get();
-        pp.workList = batched ? workListDev.get() : nullptr;
+        pp.workList = batched ? workListDev.get() : (sources ? subsetDev.get() : nullptr);
         pp.filter = table.filter.get();
         pp.filterShift = table.filterShift;
         pp.gridOf = gridOf;
@@ -1972,15 +2022,16 @@ unsigned char* noAllocScratchAddress(int device)
 
 } // namespace
 
-MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg)
+MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg,
+    const uint32_t* sources, uint32_t numSources)
 {
     switch (level) {
     case 2:
-        return runMatcherL<2>(ctx, grids, n, cfg, stats, seg);
+        return runMatcherL<2>(ctx, grids, n, cfg, stats, seg, sources, numSources);
     case 3:
-        return runMatcherL<3>(ctx, grids, n, cfg, stats, seg);
+        return runMatcherL<3>(ctx, grids, n, cfg, stats, seg, sources, numSources);
     case 4:
-        return runMatcherL<4>(ctx, grids, n, cfg, stats, seg);
+        return runMatcherL<4>(ctx, grids, n, cfg, stats, seg, sources, numSources);
     default:
         throw Error(TDAG_ERR_ARG, "translation matching supports levels 2..4");
     }

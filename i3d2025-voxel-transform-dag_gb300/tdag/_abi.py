@@ -86,8 +86,13 @@ EXPORTED = (
     "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
     "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
+    "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
 )
+
+# int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources, uint32_t* num_sources)
+PROPOSAL_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                               ctypes.POINTER(ctypes.c_uint32))
 
 _lib = None
 
@@ -129,6 +134,11 @@ def lib(path: str = None):
                                                          vp, vp, vp]
         L.tdag_result_to_host.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(ctypes.POINTER(Result))]
         L.tdag_l2_probe_peak.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+        L.tdag_find_duplicates_level_device.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.POINTER(Config), vp, ctypes.c_uint32,
+                                                        vp, vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(LevelStats)]
+        L.tdag_build_device_proposed.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), PROPOSAL_FN, vp,
+                                                 ctypes.POINTER(ctypes.POINTER(Result))]
+        L.tdag_device_copy.argtypes = [vp, vp, vp, ctypes.c_uint64]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

@@ -161,6 +161,30 @@ int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* gr
 int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n,
     const tdag_config* config, uint64_t* d_out_mapping, uint32_t* d_out_unique, uint32_t* d_n_unique);
 
+/* No counterpart in the reference: tdag_find_duplicates_level on DEVICE grids and outputs, with an
+ * optional subset of searching sources. d_sources == NULL: the exhaustive search (every item a
+ * source). Otherwise only the num_sources listed item indices (distinct, < n) probe; every item is
+ * still a target and every match is verified exactly, so the mapping is a valid one whose unique
+ * set can only be larger than the exhaustive search's. *n_unique is written on the host. */
+int tdag_find_duplicates_level_device(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n,
+    const tdag_config* config, const uint32_t* d_sources, uint32_t num_sources, uint64_t* d_out_mapping,
+    uint32_t* d_out_unique, uint32_t* n_unique, tdag_level_stats* stats);
+
+/* Learned-proposal extension (no counterpart in the reference). At every translation level the build
+ * calls fn with the level's n flattened items (d_grids: device, R^3/64 words each, bit x + R*y + R^2*z)
+ * before matching. fn writes up to n item indices into d_sources (device) -- the items allowed to
+ * search as sources -- sets *num_sources and returns 0; any other return value aborts the build with
+ * TDAG_ERR_ARG. fn must have finished its device writes when it returns. Only the listed items probe,
+ * every match is verified exactly, and the result is a valid TDAG with possibly more nodes than the
+ * exhaustive build. Single-grid builds only. */
+typedef int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources,
+    uint32_t* num_sources);
+int tdag_build_device_proposed(tdag_ctx* ctx, const tdag_svdag_view* in_device, const tdag_config* config,
+    tdag_proposal_fn fn, void* user, tdag_result** out);
+/* Device-to-device copy of `bytes` on the context's stream, complete on return: lets proposal
+ * functions written without CUDA bindings (ctypes) read d_grids and fill d_sources. */
+int tdag_device_copy(tdag_ctx* ctx, void* d_dst, const void* d_src, uint64_t bytes);
+
 /* constructTransformDAGHierarchical(inDag, config) (transform_dag.h:168-169;
  * tools/lib/src/voxel/transform_dag_hierarchical.cpp:304-529): symmetry + permutation only.
  * Host in, host out. */
