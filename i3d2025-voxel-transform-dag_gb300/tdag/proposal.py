@@ -211,7 +211,7 @@ def train(encoder: ProposalEncoder, sets: Sequence[Tuple[torch.Tensor, int, torc
         opt.zero_grad(set_to_none=True)
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(loss.item())
     return losses
 
 

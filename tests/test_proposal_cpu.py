@@ -89,7 +89,7 @@ def test_forward_matches_numpy_fp64():
     enc, words, x = _setup()
     params = [p.detach().numpy() for p in (enc.l1.weight, enc.l1.bias, enc.l2.weight, enc.l2.bias, enc.l3.weight, enc.l3.bias)]
     ref = np_forward(params, x.numpy(), 0.07)
-    got = float(_torch_loss(enc, x, 0.07))
+    got = _torch_loss(enc, x, 0.07).item()
     assert abs(got - ref) < 1e-10 * max(1.0, abs(ref))
     # the encoder's own forward (float32 on the CPU) agrees with the FP64 embedding to float32 precision
     e32 = P.ProposalEncoder()
