@@ -616,20 +616,15 @@ int tdag_ctx_stream(tdag_ctx* ctx, void** out)
     return TDAG_OK;
 }
 
-namespace {
+} // extern "C"
+
+namespace tdag {
 // Copies device arrays into host (pageable) arrays through the context's pinned staging buffer. A
 // D2H copy into pinned memory runs at link speed; one straight into freshly allocated pageable pages
 // goes page by page through the driver and took ~20 ms for a 32 MB result. The host copies out of
 // the stage run on a few threads for large results.
-struct Download {
-    void* dst;
-    const void* src;
-    size_t bytes;
-};
-
-void downloadStaged(tdag::Context& c, const std::vector<Download>& items)
+void downloadStaged(Context& c, const std::vector<Download>& items)
 {
-    using namespace tdag;
     size_t total = 0;
     for (const auto& d : items)
         total += (d.bytes + 255) & ~(size_t)255;
@@ -677,7 +672,9 @@ void downloadStaged(tdag::Context& c, const std::vector<Download>& items)
     for (auto& t : threads)
         t.join();
 }
-} // namespace
+} // namespace tdag
+
+extern "C" {
 
 int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)
 {

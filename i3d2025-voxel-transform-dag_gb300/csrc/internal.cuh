@@ -92,6 +92,15 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
 MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats,
     const Segments* seg = nullptr, const uint32_t* sources = nullptr, uint32_t numSources = 0);
 
+// Device -> host copies of several arrays through the context's pinned staging buffer; complete on
+// return (build.cu).
+struct Download {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+void downloadStaged(Context& c, const std::vector<Download>& items);
+
 // Segment helpers: per-item grid ids from offsets, per-grid counts of a grid-id list.
 void segmentIds(const uint32_t* offDev, uint32_t numGrids, uint64_t n, uint32_t* out, cudaStream_t s);
 std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx, uint64_t n, uint32_t numGrids, cudaStream_t s);

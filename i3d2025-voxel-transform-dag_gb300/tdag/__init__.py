@@ -94,6 +94,15 @@ class TransformDAGConfig:
         return cls(s, a, t, m)
 
 
+@dataclasses.dataclass
+class TransformEncodingConfig:
+    """TransformEncodingConfig (tools/svdag_encoding/src/transform_dag_encoding.h:180-182). The
+    svdag_encoding tool defaults both flags off (main.cpp:34); the renderer's files set both."""
+
+    pointer_tables: bool = False
+    huffman_code: bool = False
+
+
 # ------------------------------------------------------------------------------------------------
 # EditStructure
 # ------------------------------------------------------------------------------------------------
@@ -503,3 +512,53 @@ def construct_transform_dag_batched_device(dags: List["DeviceSvdag"], config: Tr
     st = _abi.Stats()
     _abi.check(lib().tdag_build_batched_device(ctx.handle, views, len(dags), ctypes.byref(_config_struct(config)), outs, ctypes.byref(st)))
     return [DeviceResult(outs[i]) for i in range(len(dags))], _abi.stats_to_dict(st, root)
+
+
+# ------------------------------------------------------------------------------------------------
+# .tdag16 encoding (include/tdag16.h)
+# ------------------------------------------------------------------------------------------------
+def _host_result_view(dag: EditStructure, keep: list) -> _abi.Result:
+    r = _abi.Result()
+    r.resolution = dag.resolution
+    r.root_level = dag.root_level
+    r.structure_type = dag.structure_type
+    r.on_device = 0
+    for lvl in range(3, dag.root_level + 1):
+        a = np.ascontiguousarray(dag.nodes_per_level[lvl], dtype=np.uint64)
+        keep.append(a)
+        r.nodes[lvl] = a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        r.node_counts[lvl] = a.shape[0]
+    sg = np.ascontiguousarray(dag.sub_grids, dtype=np.uint64)
+    keep.append(sg)
+    r.leaves = sg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    r.leaf_count = sg.shape[0]
+    return r
+
+
+def construct_transform_dag16(dag, dag_config: TransformDAGConfig = TransformDAGConfig(),
+                              encoding_config: TransformEncodingConfig = TransformEncodingConfig(),
+                              ctx: Optional[Context] = None, return_stats: bool = False):
+    """constructTransformDAG16(EditStructure<void, TransformPointer>, dagConfig, encodingConfig, stats)
+    (tools/svdag_encoding/src/transform_dag_encoding.cpp:240-497) followed by TransformDAG16::writeTo:
+    returns the .tdag16 file bytes (and, with return_stats, the per-level DAGEncodingStats).
+    ``dag`` is a host EditStructure of TransformPointers or a DeviceResult."""
+    ctx = ctx or default_context()
+    keep = []
+    if isinstance(dag, DeviceResult):
+        rp_in = dag._rp
+    else:
+        rp_in = ctypes.pointer(_host_result_view(dag, keep))
+    enc = _abi.EncodingConfig(int(encoding_config.pointer_tables), int(encoding_config.huffman_code))
+    op = ctypes.POINTER(_abi.Tdag16Result)()
+    _abi.check(lib().tdag_encode16(ctx.handle, rp_in, ctypes.byref(_config_struct(dag_config)), ctypes.byref(enc), ctypes.byref(op)))
+    try:
+        r = op.contents
+        data = ctypes.string_at(r.bytes, r.size)
+        stats = {
+            "encode_ms": r.encode_ms, "wall_ms": r.wall_ms, "kernel_launches": r.kernel_launches,
+            "levels": {l: {k: (list(getattr(r.levels[l], k)) if k in ("table_pointers", "direct_pointers") else getattr(r.levels[l], k))
+                           for k, _ in _abi.Tdag16LevelStats._fields_} for l in range(2, r.root_level + 1)},
+        }
+    finally:
+        lib().tdag16_result_free(op)
+    return (data, stats) if return_stats else data

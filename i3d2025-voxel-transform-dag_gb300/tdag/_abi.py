@@ -79,6 +79,22 @@ class Tuning(ctypes.Structure):
                 ("search_ctas_per_sm", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class EncodingConfig(ctypes.Structure):
+    _fields_ = [("pointer_tables", ctypes.c_int32), ("huffman_code", ctypes.c_int32)]
+
+
+class Tdag16LevelStats(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_uint64), ("memory_in_bytes", ctypes.c_uint64), ("table_size", ctypes.c_uint64),
+                ("unique_pointers", ctypes.c_uint64), ("table_pointers", ctypes.c_uint64 * 3),
+                ("direct_pointers", ctypes.c_uint64 * 3)]
+
+
+class Tdag16Result(ctypes.Structure):
+    _fields_ = [("bytes", ctypes.POINTER(ctypes.c_uint8)), ("size", ctypes.c_uint64), ("root_level", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("levels", Tdag16LevelStats * MAX_LEVELS), ("encode_ms", ctypes.c_float),
+                ("wall_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint64)]
+
+
 # Every symbol include/tdag.h declares (checked by the CPU test-suite).
 EXPORTED = (
     "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
@@ -88,6 +104,7 @@ EXPORTED = (
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
+    "tdag_encode16", "tdag16_result_free",  # include/tdag16.h
 )
 
 # int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources, uint32_t* num_sources)
@@ -139,6 +156,9 @@ def lib(path: str = None):
         L.tdag_build_device_proposed.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), PROPOSAL_FN, vp,
                                                  ctypes.POINTER(ctypes.POINTER(Result))]
         L.tdag_device_copy.argtypes = [vp, vp, vp, ctypes.c_uint64]
+        L.tdag_encode16.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(Config), ctypes.POINTER(EncodingConfig),
+                                    ctypes.POINTER(ctypes.POINTER(Tdag16Result))]
+        L.tdag16_result_free.argtypes = [ctypes.POINTER(Tdag16Result)]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

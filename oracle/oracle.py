@@ -20,8 +20,9 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++ -O3 -fopenmp)."""
+    sources = [os.path.join(_HERE, f) for f in ("tdag_oracle.cpp", "tdag16_oracle.cpp", "Makefile")]
     if force or not os.path.exists(_LIB_PATH) or (
-        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "tdag_oracle.cpp"))
+        os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(f) for f in sources)
     ):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
@@ -50,6 +51,13 @@ def lib():
         L.orc_encode_fixed64.restype = ctypes.c_uint64
         L.orc_decode_fixed64.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
         L.orc_decode_fixed64.restype = ctypes.c_uint64
+        L.orc16_last_error.restype = ctypes.c_char_p
+        L.orc16_huffman_lengths.argtypes = [u64p, ctypes.c_uint32, ctypes.c_uint32, u32p]
+        L.orc16_huffman_codes.argtypes = [u32p, ctypes.c_uint32, ctypes.c_int, u64p, u32p]
+        L.orc16_huffman_decode.argtypes = [u64p, u32p, ctypes.c_uint32, ctypes.c_uint32, u32p, u32p]
+        L.orc16_encode.argtypes = [u8p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, u8pp, u64p, u64p,
+                                   ctypes.c_uint32]
+        L.orc16_decode_dense.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -164,3 +172,67 @@ def encode_fixed64(tp: int, level: int) -> int:
 
 def decode_fixed64(e: int, level: int) -> int:
     return int(lib().orc_decode_fixed64(e, level))
+
+
+# ------------------------------------------------------------------------------------------------
+# .tdag16 (tdag16_oracle.cpp)
+# ------------------------------------------------------------------------------------------------
+TIE_CANONICAL = 0  # ties by ascending item index / ascending pointer value (the library's order)
+TIE_LIBSTDCXX = 1  # std::sort + std::unordered_map, as the reference behaves with libstdc++ (serial backend)
+LEVEL16_KEYS = ("num_nodes", "memory_in_bytes", "table_size", "unique_pointers", "table_u16", "table_u32",
+                "table_u48", "direct_u16", "direct_u32", "direct_u48")
+
+
+def _chk16(rc):
+    if rc != 0:
+        raise OracleError(lib().orc16_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def huffman_lengths(freq, max_len):
+    f = np.ascontiguousarray(freq, dtype=np.uint64)
+    out = np.zeros(len(f), np.uint32)
+    _chk16(lib().orc16_huffman_lengths(_p(f, ctypes.c_uint64), len(f), max_len, _p(out, ctypes.c_uint32)))
+    return [int(v) for v in out]
+
+
+def huffman_codes(lengths, lsb=False):
+    l = np.ascontiguousarray(lengths, dtype=np.uint32)
+    codes = np.zeros(len(l), np.uint64)
+    bits = np.zeros(len(l), np.uint32)
+    _chk16(lib().orc16_huffman_codes(_p(l, ctypes.c_uint32), len(l), int(lsb), _p(codes, ctypes.c_uint64),
+                                     _p(bits, ctypes.c_uint32)))
+    return [(int(c), int(b)) for c, b in zip(codes, bits)]
+
+
+def huffman_decode(codes, key):
+    c = np.array([x for x, _ in codes], np.uint64)
+    b = np.array([y for _, y in codes], np.uint32)
+    s, n = ctypes.c_uint32(), ctypes.c_uint32()
+    _chk16(lib().orc16_huffman_decode(_p(c, ctypes.c_uint64), _p(b, ctypes.c_uint32), len(c), key, ctypes.byref(s),
+                                      ctypes.byref(n)))
+    return int(s.value), int(n.value)
+
+
+def encode_tdag16(tdag: bytes, pointer_tables=False, huffman=False, tie=TIE_CANONICAL):
+    """constructTransformDAG16 on .tdag bytes -> (.tdag16 bytes, per-level stats dicts)."""
+    a, p = _u8(tdag)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    st = np.zeros((32, 10), np.uint64)
+    _chk16(lib().orc16_encode(p, len(tdag), int(pointer_tables), int(huffman), int(tie), ctypes.byref(out),
+                              ctypes.byref(n), _p(st, ctypes.c_uint64), 32))
+    data = _take(out, n)
+    root = int.from_bytes(tdag[-16:-12], "little")  # ..., resolution, rootLevel, structureType, config(8)
+    return data, [dict(zip(LEVEL16_KEYS, (int(v) for v in st[l]))) for l in range(root + 1)]
+
+
+def decode_tdag16(data: bytes, res: int) -> np.ndarray:
+    """Every voxel of a .tdag16, as dense[z, y, x]."""
+    a, p = _u8(data)
+    dense = np.zeros((res, res, res), dtype=np.uint8)
+    _chk16(lib().orc16_decode_dense(p, len(data), _p(dense, ctypes.c_uint8), res))
+    return dense

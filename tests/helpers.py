@@ -30,3 +30,34 @@ def dag_svo_bytes(oracle, dense):
 
 def structure_from_svo(tdag_mod, svo_bytes):
     return tdag_mod.EditStructure.from_svo_bytes(svo_bytes)
+
+
+def synthetic_tdag(n_leaves, refs_per_leaf, seed):
+    """A transform DAG whose level-3 nodes reference n_leaves distinct (leaf, transform) pointers
+    refs_per_leaf times each, in a random order, under an 8-ary tree up to a single root."""
+    import tdag
+    rng = np.random.default_rng(seed)
+    leaves = rng.integers(1, 2**63, size=n_leaves, dtype=np.uint64)
+    ptrs = []
+    for i in range(n_leaves):
+        t = rng.integers(-3, 4, size=3) * (rng.random() < 0.5)
+        ptrs.append(tdag.tp_create(i, tuple(bool(b) for b in rng.integers(0, 2, 3)), [(0, 1, 2), (1, 2, 0), (2, 1, 0)][i % 3],
+                                   tuple(int(v) for v in t)))
+    refs = np.repeat(np.array(ptrs, dtype=np.uint64), refs_per_leaf)
+    rng.shuffle(refs)
+    levels = [np.zeros((0, 8), np.uint64)] * 3
+    sentinel = tdag.tp_create(0xFFFFFFFF)
+    n3 = -(-len(refs) // 8)
+    l3 = np.full(n3 * 8, sentinel, dtype=np.uint64)
+    l3[: len(refs)] = refs
+    levels.append(l3.reshape(n3, 8))
+    count = n3
+    while count > 1:
+        up = -(-count // 8)
+        lv = np.full(up * 8, sentinel, dtype=np.uint64)
+        lv[:count] = [tdag.tp_create(i) for i in range(count)]
+        levels.append(lv.reshape(up, 8))
+        count = up
+    root = len(levels) - 1
+    s = tdag.EditStructure(levels, leaves, 1 << root, root, 0, "transform")
+    return tdag.write_tdag(s, tdag.TransformDAGConfig()), s

@@ -11,12 +11,12 @@ from conftest import REPO
 
 
 def header_functions():
-    """Every tdag_* function declared by the C headers (include/tdag.h, include/tdag_diag.h)."""
+    """Every tdag_* function declared by the C headers (include/tdag.h, tdag_diag.h, tdag16.h)."""
     names = set()
-    for h in ("tdag.h", "tdag_diag.h"):
+    for h in ("tdag.h", "tdag_diag.h", "tdag16.h"):
         src = open(os.path.join(REPO, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"\b(tdag_[a-z0-9_]+)\s*\(", src))
+        names |= set(re.findall(r"\b(tdag(?:16)?_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 

@@ -1,0 +1,81 @@
+"""GPU parity of the .tdag16 encoder (tdag_encode16) against the oracle's encoder, byte for byte.
+
+The oracle orders equal reference counts by ascending item index and ascending pointer value (its
+canonical tie order, the one the library implements); both are compared on every encoding variant
+(plain, Huffman, pointer tables, both), on transform DAGs built by the oracle and by the GPU, and on
+a synthetic DAG whose pointer table outgrows 16-bit indices.
+"""
+import numpy as np
+import pytest
+
+from helpers import blocky_grid, dag_svo_bytes, random_grid, synthetic_tdag
+
+pytestmark = pytest.mark.gpu
+
+ENCODINGS = [(False, False), (False, True), (True, False), (True, True)]
+
+
+def _gpu_encode(tdaglib, gpu_ctx, tdag_bytes, pt, hf):
+    s, cfg = tdaglib.read_tdag(tdag_bytes)
+    return tdaglib.construct_transform_dag16(s, cfg, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx, return_stats=True)
+
+
+CASES = [
+    ("blocky64", lambda g: blocky_grid(64, 3), dict()),
+    ("terrain64", lambda g: g.terrain(64, 1), dict()),
+    ("random32", lambda g: random_grid(32, 0.25, 7), dict()),
+    ("blocky128-sym", lambda g: blocky_grid(128, 5), dict(axis=False, translation=False)),
+    ("blocky64-plain", lambda g: blocky_grid(64, 6), dict(symmetry=False, axis=False, translation=False)),
+    ("terrain256", lambda g: g.terrain(256, 1), dict()),
+]
+
+
+@pytest.mark.parametrize("name,make,cfg", CASES, ids=[c[0] for c in CASES])
+def test_encode16_matches_oracle(oracle, tdaglib, gpu_ctx, name, make, cfg):
+    from oracle import generator
+    dense = make(generator)
+    t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense), **cfg)
+    for pt, hf in ENCODINGS:
+        ref, ref_stats = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
+        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf)
+        assert got == ref, (name, pt, hf)
+        for l in range(2, len(ref_stats)):
+            g, r = st["levels"][l], ref_stats[l]
+            assert (g["num_nodes"], g["memory_in_bytes"], g["table_size"]) == (r["num_nodes"], r["memory_in_bytes"], r["table_size"])
+            if l >= 3:
+                assert g["unique_pointers"] == r["unique_pointers"]
+                assert g["table_pointers"] == [r["table_u16"], r["table_u32"], r["table_u48"]]
+                assert g["direct_pointers"] == [r["direct_u16"], r["direct_u32"], r["direct_u48"]]
+        assert st["kernel_launches"] > 0
+
+
+def test_encode16_pointer_table_widening(oracle, tdaglib, gpu_ctx):
+    t, _ = synthetic_tdag(70000, 5, 1)
+    for pt, hf in [(True, True), (True, False)]:
+        ref, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
+        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf)
+        assert got == ref, (pt, hf)
+        assert st["levels"][3]["table_pointers"][0] == 65536
+
+
+def test_encode16_of_device_build(oracle, tdaglib, gpu_ctx):
+    """GPU build (device-resident result) -> GPU encode equals the oracle's encode of the oracle build."""
+    dense = blocky_grid(128, 8)
+    cfg = tdaglib.TransformDAGConfig()
+    t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense))
+    sv = tdaglib.svdag_from_dense(dense, ctx=gpu_ctx)
+    dev = tdaglib.construct_transform_dag_device(sv, cfg, ctx=gpu_ctx)
+    for pt, hf in ENCODINGS:
+        got = tdaglib.construct_transform_dag16(dev, cfg, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx)
+        ref, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
+        assert got == ref, (pt, hf)
+        assert np.array_equal(oracle.decode_tdag16(got, 128), dense)
+
+
+def test_encode16_rejects_dangling_child_pointers(tdaglib, gpu_ctx):
+    """A child index past the level below is reported (TDAG_ERR_CORRUPT) and its count is skipped."""
+    s, cfg = tdaglib.read_tdag(synthetic_tdag(64, 1, 2)[0])
+    s.nodes_per_level[3][0, 0] = tdaglib.tp_create(64)  # 64 leaves: valid indices are 0..63
+    with pytest.raises(tdaglib.TDagError) as e:
+        tdaglib.construct_transform_dag16(s, cfg, tdaglib.TransformEncodingConfig(True, True), ctx=gpu_ctx)
+    assert e.value.code == 6
