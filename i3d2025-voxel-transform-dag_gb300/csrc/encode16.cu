@@ -46,60 +46,56 @@ struct PointerCode {
 // ------------------------------------------------------------------------------------------------
 // Host: length-limited Huffman code by package-merge (huffman.cpp:100-170; Moffat 2019, alg. 3).
 // Items of a level are kept in the reference's total order (frequency, leaves before packages,
-// leaves by symbol, packages by their members), the 2n-2 smallest of the top level are chosen, and
-// chosen packages select the 2k smallest of the level below. Code words are assigned canonically in
-// order of increasing length (huffman.cpp:78-98; std::sort, like the reference, so that the order
-// of equal lengths is the same) and bit-reversed for LSB-first decoding (huffman.cpp:172-182).
+// leaves by symbol, packages by their two members in that same order), the 2n-2 smallest of the top
+// level are chosen, and chosen packages select the 2k smallest of the level below. A package's
+// members are named by their positions in the sorted level below, so comparing members is comparing
+// positions. Code words are assigned canonically in order of increasing length (huffman.cpp:78-98;
+// std::sort, like the reference, so that the order of equal lengths is the same) and bit-reversed
+// for LSB-first decoding (huffman.cpp:172-182).
 // ------------------------------------------------------------------------------------------------
 struct Pm {
     uint64_t freq;
-    int32_t symbol; // -1: package of (a, b) in the level below
+    int32_t symbol; // -1: package of the items at positions (a, b) of the sorted level below
     int32_t a, b;
-    uint32_t level;
 };
-struct PmLevels {
-    std::vector<std::vector<Pm>> lv;
-    bool less(const Pm& x, const Pm& y) const
-    {
-        if (x.freq != y.freq)
-            return x.freq < y.freq;
-        const bool xl = x.symbol >= 0, yl = y.symbol >= 0;
-        if (xl != yl)
-            return xl;
-        if (xl)
-            return x.symbol < y.symbol;
-        const auto& below = lv[x.level - 1];
-        if (less(below[x.a], below[y.a]))
-            return true;
-        if (less(below[y.a], below[x.a]))
-            return false;
-        return less(below[x.b], below[y.b]);
-    }
-};
-std::vector<PointerCode> huffmanCodes(const std::vector<uint64_t>& freq)
+inline bool pmLess(const Pm& x, const Pm& y)
+{
+    if (x.freq != y.freq)
+        return x.freq < y.freq;
+    const bool xl = x.symbol >= 0, yl = y.symbol >= 0;
+    if (xl != yl)
+        return xl;
+    if (xl)
+        return x.symbol < y.symbol;
+    return x.a != y.a ? x.a < y.a : x.b < y.b;
+}
+std::vector<PointerCode> huffmanCodes(const std::vector<uint64_t>& freq, uint32_t maxCodeLen = kMaxCodeLen, bool lsbFirst = true)
 {
     const uint32_t n = (uint32_t)freq.size();
-    PmLevels pm;
-    pm.lv.resize(kMaxCodeLen);
+    TDAG_CHECK(n >= 1 && maxCodeLen >= 1 && maxCodeLen <= 32, TDAG_ERR_ARG, "Huffman code: empty alphabet or length limit outside 1..32");
+    struct {
+        std::vector<std::vector<Pm>> lv;
+    } pm;
+    pm.lv.resize(maxCodeLen);
     auto sortLevel = [&](uint32_t l) {
         auto& v = pm.lv[l];
-        std::sort(v.begin(), v.end(), [&](const Pm& x, const Pm& y) { return pm.less(x, y); });
+        std::sort(v.begin(), v.end(), pmLess);
     };
     for (uint32_t s = 0; s < n; ++s)
-        pm.lv[0].push_back({ freq[s], (int32_t)s, -1, -1, 0 });
+        pm.lv[0].push_back({ freq[s], (int32_t)s, -1, -1 });
     sortLevel(0);
-    for (uint32_t l = 1; l < kMaxCodeLen; ++l) {
+    for (uint32_t l = 1; l < maxCodeLen; ++l) {
         const auto& below = pm.lv[l - 1];
         auto& cur = pm.lv[l];
         for (size_t i = 0; i + 1 < below.size(); i += 2)
-            cur.push_back({ below[i].freq + below[i + 1].freq, -1, (int32_t)i, (int32_t)(i + 1), l });
+            cur.push_back({ below[i].freq + below[i + 1].freq, -1, (int32_t)i, (int32_t)(i + 1) });
         for (uint32_t s = 0; s < n; ++s)
-            cur.push_back({ freq[s], (int32_t)s, -1, -1, l });
+            cur.push_back({ freq[s], (int32_t)s, -1, -1 });
         sortLevel(l);
     }
     std::vector<uint32_t> len(n, 0);
     size_t take = 2 * (size_t)n - 2;
-    for (int l = (int)kMaxCodeLen - 1; l >= 0 && take > 0; --l) {
+    for (int l = (int)maxCodeLen - 1; l >= 0 && take > 0; --l) {
         const auto& items = pm.lv[l];
         TDAG_CHECK(take <= items.size(), TDAG_ERR_ARG, "Huffman code length limit too small");
         size_t packages = 0;
@@ -120,14 +116,14 @@ std::vector<PointerCode> huffmanCodes(const std::vector<uint64_t>& freq)
     std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return len[l] < len[r]; });
     const uint32_t maxLen = *std::max_element(len.begin(), len.end());
     std::vector<PointerCode> codes(n);
-    uint32_t next = 0;
+    uint64_t next = 0;
     for (uint32_t s : order) {
-        const uint32_t msb = next >> (maxLen - len[s]);
+        const uint64_t msb = next >> (maxLen - len[s]);
         uint64_t lsb = 0;
         for (uint32_t i = 0; i < len[s]; ++i)
-            lsb |= (uint64_t)((msb >> i) & 1) << (len[s] - 1 - i);
-        codes[s] = { lsb, len[s], 0 };
-        next += 1u << (maxLen - len[s]);
+            lsb |= ((msb >> i) & 1) << (len[s] - 1 - i);
+        codes[s] = { lsbFirst ? lsb : msb, len[s], 0 };
+        next += 1ull << (maxLen - len[s]);
     }
     return codes;
 }
@@ -789,6 +785,21 @@ extern "C" int tdag_encode16(tdag_ctx* ctx, const tdag_result* dag, const tdag_c
         encodeTdag16(c, *dag, *config, *encoding, *r);
         r->wall_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
         *out = r.release();
+    });
+}
+
+extern "C" int tdag16_huffman_code_table(const uint64_t* frequencies, uint32_t n, uint32_t max_code_length, int lsb_first,
+    uint64_t* out_codes, uint32_t* out_bits)
+{
+    using namespace tdag;
+    if (!frequencies || !out_codes || !out_bits)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        const auto codes = huffmanCodes(std::vector<uint64_t>(frequencies, frequencies + n), max_code_length, lsb_first != 0);
+        for (uint32_t i = 0; i < n; ++i) {
+            out_codes[i] = codes[i].code;
+            out_bits[i] = codes[i].bits;
+        }
     });
 }
 

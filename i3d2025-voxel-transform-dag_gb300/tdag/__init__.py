@@ -562,3 +562,57 @@ def construct_transform_dag16(dag, dag_config: TransformDAGConfig = TransformDAG
     finally:
         lib().tdag16_result_free(op)
     return (data, stats) if return_stats else data
+
+
+def create_length_limited_huffman_code_table(frequencies, max_code_length: int = 16, lsb_first: bool = False):
+    """createLengthLimitedHuffmanCodeTable (+ convertHuffmanToLSB when lsb_first) (huffman.cpp:165-182):
+    a list of (code, bits) per symbol. Host computation in libtdag.so."""
+    f = np.ascontiguousarray(frequencies, dtype=np.uint64)
+    codes = np.zeros(len(f), np.uint64)
+    bits = np.zeros(len(f), np.uint32)
+    _abi.check(lib().tdag16_huffman_code_table(f.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), len(f), int(max_code_length),
+                                               int(lsb_first), codes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                               bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+    return [(int(c), int(b)) for c, b in zip(codes, bits)]
+
+
+class Tdag16Device:
+    """A .tdag16 file resident in device memory (tdag16_upload), for voxel queries
+    (TransformDAG16::get) and the lossless check against its source SVDAG."""
+
+    def __init__(self, data: bytes, ctx: Optional[Context] = None):
+        self._ctx = ctx or default_context()
+        buf = np.frombuffer(data, dtype=np.uint8)
+        h = ctypes.c_void_p()
+        _abi.check(lib().tdag16_upload(self._ctx.handle, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), len(data), ctypes.byref(h)))
+        self._h = h
+
+    def get(self, xyz):
+        """Occupancy of n voxels: xyz is an (n, 3) integer array (host) or a CUDA uint32/int32 tensor."""
+        import torch
+        on_host = not (isinstance(xyz, torch.Tensor) and xyz.is_cuda)
+        t = torch.as_tensor(np.ascontiguousarray(xyz, dtype=np.uint32).view(np.int32)) if on_host else xyz
+        t = t.to(device="cuda", dtype=torch.int32).contiguous()
+        n = t.shape[0]
+        out = torch.empty(n, dtype=torch.uint8, device=t.device)
+        torch.cuda.synchronize()
+        _abi.check(lib().tdag16_get(self._ctx.handle, self._h, ctypes.c_void_p(t.data_ptr()), n, ctypes.c_void_p(out.data_ptr())))
+        return out.cpu().numpy() if on_host else out
+
+    def verify(self, source: "DeviceSvdag") -> dict:
+        """Lossless check against the device SVDAG the DAG was built from (tdag16_verify)."""
+        st = _abi.Tdag16VerifyStats()
+        v = source.view()
+        _abi.check(lib().tdag16_verify(self._ctx.handle, self._h, ctypes.byref(v), ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _abi.Tdag16VerifyStats._fields_ if k != "reserved"}
+
+    def free(self):
+        if getattr(self, "_h", None):
+            lib().tdag16_device_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -95,6 +95,12 @@ class Tdag16Result(ctypes.Structure):
                 ("wall_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint64)]
 
 
+class Tdag16VerifyStats(ctypes.Structure):
+    _fields_ = [("existence_mismatches", ctypes.c_uint64), ("voxel_mismatches", ctypes.c_uint64),
+                ("boxes_compared", ctypes.c_uint64), ("pairs_walked", ctypes.c_uint64), ("box_level", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
 # Every symbol include/tdag.h declares (checked by the CPU test-suite).
 EXPORTED = (
     "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
@@ -104,7 +110,8 @@ EXPORTED = (
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
-    "tdag_encode16", "tdag16_result_free",  # include/tdag16.h
+    "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
+    "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify",
 )
 
 # int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources, uint32_t* num_sources)
@@ -159,6 +166,12 @@ def lib(path: str = None):
         L.tdag_encode16.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(Config), ctypes.POINTER(EncodingConfig),
                                     ctypes.POINTER(ctypes.POINTER(Tdag16Result))]
         L.tdag16_result_free.argtypes = [ctypes.POINTER(Tdag16Result)]
+        L.tdag16_upload.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint64, ctypes.POINTER(vp)]
+        L.tdag16_device_free.argtypes = [vp]
+        L.tdag16_get.argtypes = [vp, vp, vp, ctypes.c_uint64, vp]
+        L.tdag16_verify.argtypes = [vp, vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Tdag16VerifyStats)]
+        L.tdag16_huffman_code_table.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

@@ -56,6 +56,45 @@ int tdag_encode16(tdag_ctx* ctx, const tdag_result* dag, const tdag_config* conf
     tdag16_result** out);
 int tdag16_result_free(tdag16_result* result);
 
+/* ------------------------------------------------------------------------------------------------
+ * Queries on an encoded .tdag16 resident in device memory.
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct tdag16_device tdag16_device; /* device copy of a .tdag16 file, library-owned */
+
+/* Parse .tdag16 bytes (host memory) into device arrays and Huffman decode tables. Every index
+ * later read from them is bounds-checked on the device (TDAG_ERR_CORRUPT). Free the handle with
+ * tdag16_device_free before destroying the context. Root levels 3..23. */
+int tdag16_upload(tdag_ctx* ctx, const uint8_t* bytes, uint64_t size, tdag16_device** out);
+int tdag16_device_free(tdag16_device* dev);
+
+/* TranslateTransformBaseDAG<TransformDAG16>::get (transform_dag_encoding.cpp:699-745) for n voxels:
+ * d_xyz = n x (x, y, z) uint32 and d_out = n uint8 (1 = solid), both device memory. Coordinates
+ * outside the grid answer 0. */
+int tdag16_get(tdag_ctx* ctx, const tdag16_device* dev, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
+
+/* Lossless check of a .tdag16 against the SVDAG it encodes (device view, e.g. tdag_svdag_get_view):
+ * the role of verifyComplexTransformDAG (transform_dag_encoding.h:81-117). Above box_level the two
+ * structures are walked together and every child present on one side only counts as an existence
+ * mismatch; at box_level (the highest level whose incoming pointers may carry a translation, else
+ * the leaf level) every voxel of each reached box is compared. Empty regions are covered as well.
+ * The encoding is lossless when both mismatch counts are 0. */
+typedef struct tdag16_verify_stats {
+    uint64_t existence_mismatches;
+    uint64_t voxel_mismatches;
+    uint64_t boxes_compared;
+    uint64_t pairs_walked; /* (source node, .tdag16 node) pairs walked above box_level */
+    uint32_t box_level;
+    uint32_t reserved;
+} tdag16_verify_stats;
+int tdag16_verify(tdag_ctx* ctx, const tdag16_device* dev, const tdag_svdag_view* source_device, tdag16_verify_stats* out);
+
+/* createLengthLimitedHuffmanCodeTable(frequencies, max_code_length) and, if lsb_first,
+ * convertHuffmanToLSB (tools/svdag_encoding/src/huffman.h:22-25; huffman.cpp:165-182): the code of
+ * every symbol (bit-reversed when lsb_first) and its length. The encoder uses it with the level's
+ * pointer-type histogram and max_code_length 16. Host computation; needs no device. */
+int tdag16_huffman_code_table(const uint64_t* frequencies, uint32_t n, uint32_t max_code_length, int lsb_first,
+    uint64_t* out_codes, uint32_t* out_bits);
+
 #ifdef __cplusplus
 }
 #endif

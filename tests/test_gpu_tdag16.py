@@ -79,3 +79,58 @@ def test_encode16_rejects_dangling_child_pointers(tdaglib, gpu_ctx):
     with pytest.raises(tdaglib.TDagError) as e:
         tdaglib.construct_transform_dag16(s, cfg, tdaglib.TransformEncodingConfig(True, True), ctx=gpu_ctx)
     assert e.value.code == 6
+
+
+# ---- queries on the encoded file (tdag16_upload / tdag16_get / tdag16_verify) ------------------
+@pytest.mark.parametrize("pt,hf", ENCODINGS)
+def test_get_matches_oracle_decoder(oracle, tdaglib, gpu_ctx, pt, hf):
+    """Every voxel of a 64^3 grid, plus coordinates outside the grid."""
+    dense = blocky_grid(64, 3)
+    t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense))
+    data, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
+    dev = tdaglib.Tdag16Device(data, ctx=gpu_ctx)
+    z, y, x = np.meshgrid(np.arange(64), np.arange(64), np.arange(64), indexing="ij")
+    xyz = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1).astype(np.uint32)
+    got = dev.get(xyz).reshape(64, 64, 64)
+    assert np.array_equal(got, oracle.decode_tdag16(data, 64))
+    assert np.array_equal(got, dense)
+    assert list(dev.get(np.array([[64, 0, 0], [0, 0, 1 << 20], [63, 63, 63]], np.uint32))) == [0, 0, int(dense[63, 63, 63])]
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(translation=False), dict(symmetry=False, axis=False, translation=False), dict(max_level=3)])
+def test_verify_accepts_lossless_encodings(tdaglib, gpu_ctx, cfg):
+    dense = blocky_grid(128, 11)
+    c = tdaglib.TransformDAGConfig(cfg.get("symmetry", True), cfg.get("axis", True), cfg.get("translation", True), cfg.get("max_level", 4))
+    sv = tdaglib.svdag_from_dense(dense, ctx=gpu_ctx)
+    dev = tdaglib.construct_transform_dag_device(sv, c, ctx=gpu_ctx)
+    for pt, hf in ENCODINGS:
+        data = tdaglib.construct_transform_dag16(dev, c, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx)
+        st = tdaglib.Tdag16Device(data, ctx=gpu_ctx).verify(sv)
+        assert st["existence_mismatches"] == 0 and st["voxel_mismatches"] == 0, (cfg, pt, hf, st)
+        assert st["boxes_compared"] > 0
+
+
+def test_verify_reports_a_changed_leaf(tdaglib, gpu_ctx):
+    """A .tdag16 whose leaf masks were altered (pointers untouched) fails the check."""
+    import struct
+    dense = blocky_grid(64, 12)
+    c = tdaglib.TransformDAGConfig()
+    sv = tdaglib.svdag_from_dense(dense, ctx=gpu_ctx)
+    data = tdaglib.construct_transform_dag16(tdaglib.construct_transform_dag_device(sv, c, ctx=gpu_ctx), c)
+    off = 10
+    (nl,) = struct.unpack_from("<Q", data, off)
+    off += 8
+    for _ in range(nl):
+        (n,) = struct.unpack_from("<Q", data, off)
+        off += 8 + 2 * n
+    (n_leaves,) = struct.unpack_from("<Q", data, off)
+    assert n_leaves > 0
+    bad = bytearray(data)
+    (mask,) = struct.unpack_from("<Q", data, off + 8)
+    assert mask != 0
+    # clear a solid voxel of leaf 0: every pointer to the leaf keeps its solid voxels inside its box,
+    # so the change is visible wherever the leaf is used
+    struct.pack_into("<Q", bad, off + 8, mask & (mask - 1))
+    st = tdaglib.Tdag16Device(bytes(bad), ctx=gpu_ctx).verify(sv)
+    assert st["voxel_mismatches"] > 0
+    assert tdaglib.Tdag16Device(data, ctx=gpu_ctx).verify(sv)["voxel_mismatches"] == 0

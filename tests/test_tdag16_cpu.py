@@ -137,3 +137,20 @@ def test_pointer_table_index_widens_past_65535_entries(oracle):
     assert lv3["table_u32"] == lv3["table_size"] - 65536 and lv3["table_u48"] == 0
     assert lv3["direct_u32"] > 0 and lv3["direct_u48"] == 0
     assert lv3["table_size"] + lv3["direct_u32"] == 70000
+
+
+# ---- the library's host Huffman builder (libtdag.so, no device needed) against the oracle --------
+def test_library_huffman_known_answer(tdaglib):
+    codes = tdaglib.create_length_limited_huffman_code_table([20, 17, 6, 3, 2, 2, 2, 1, 1, 1], 5)
+    assert [b for _, b in codes] == [2, 2, 3, 4, 4, 4, 4, 5, 5, 4]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_library_huffman_matches_oracle(oracle, tdaglib, seed):
+    """Pointer-type histograms: 384 / 48 / 8 symbols with many zeros and ties."""
+    rng = np.random.default_rng(seed)
+    n = [384, 384, 48, 8, 384, 64, 6, 1][seed]
+    freq = rng.integers(0, 4, size=n) * rng.integers(0, 2, size=n) * rng.integers(1, 50, size=n)
+    for lsb in (False, True):
+        want = oracle.huffman_codes(oracle.huffman_lengths(freq, 16), lsb=lsb)
+        assert tdaglib.create_length_limited_huffman_code_table(freq, 16, lsb_first=lsb) == want
