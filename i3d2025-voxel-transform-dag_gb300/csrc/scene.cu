@@ -12,6 +12,8 @@
 //  * toDAG: restates EditStructure::toDAG (structure.h:703-763): per level, bottom-up, every item maps
 //    to the first occurrence of its content; first occurrences keep their order.
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -113,21 +115,26 @@ constexpr int kBrick = 32;
 constexpr int kHalo = kBrick + 2;
 constexpr int kMaxList = 1024;
 
-// CTA per 32^3 brick. Writes the brick's 8^3 leaf masks into the Morton-indexed leaf array.
-__global__ void __launch_bounds__(256) sceneBrickKernel(const DevPrim* __restrict__ prims, uint32_t numPrims, uint32_t kind, uint32_t res, uint32_t seed,
-    uint32_t shell, uint32_t bricksPerAxis, uint64_t* __restrict__ leafArray, uint32_t* status)
+// CTA per 32^3 brick of a chunk of bricksPerAxis^3 bricks whose first brick is (obx, oby, obz).
+// Writes the brick's 8^3 leaf masks into the chunk's Morton-indexed leaf array. The primitives
+// tested are cand[0..numCand) when cand is given (the chunk's candidates), else all of them.
+__global__ void __launch_bounds__(256) sceneBrickKernel(const DevPrim* __restrict__ prims, uint32_t numPrims, const uint32_t* __restrict__ cand,
+    uint32_t numCand, uint32_t kind, uint32_t res, uint32_t seed, uint32_t shell, uint32_t bricksPerAxis, uint32_t obx, uint32_t oby, uint32_t obz,
+    uint64_t* __restrict__ leafArray, uint32_t* status)
 {
     __shared__ uint64_t rows[kHalo * kHalo]; // bit hx (0..33) of row (hy, hz) = voxel (bx0 - 1 + hx, ...)
     __shared__ uint32_t list[kMaxList];
     __shared__ uint32_t listCount;
     const uint32_t b = blockIdx.x;
     const int bx = (int)(b % bricksPerAxis), by = (int)((b / bricksPerAxis) % bricksPerAxis), bz = (int)(b / (bricksPerAxis * bricksPerAxis));
-    const int x0 = bx * kBrick - 1, y0 = by * kBrick - 1, z0 = bz * kBrick - 1; // halo origin
+    const int x0 = (int)(obx + bx) * kBrick - 1, y0 = (int)(oby + by) * kBrick - 1, z0 = (int)(obz + bz) * kBrick - 1; // halo origin
     if (threadIdx.x == 0)
         listCount = 0;
     __syncthreads();
     if (kind == TDAG_SCENE_PRIMITIVES) {
-        for (uint32_t i = threadIdx.x; i < numPrims; i += blockDim.x) {
+        const uint32_t scan = cand ? numCand : numPrims;
+        for (uint32_t c = threadIdx.x; c < scan; c += blockDim.x) {
+            const uint32_t i = cand ? cand[c] : c;
             const DevPrim& p = prims[i];
             bool hit = true;
             const int lo[3] = { x0, y0, z0 };
@@ -534,6 +541,310 @@ DevPrim toDevPrim(const tdag_primitive& p)
 
 } // namespace
 
+// ------------------------------------------------------------------------------------------------
+// Streamed scene build for grids whose leaf array does not fit (SURVEY config 4, 16384^3): the grid
+// is generated in chunks of chunkRes^3 voxels in Morton order of the chunks. Every chunk gets its own
+// SVO (levels 2..log2(chunkRes)), is deduplicated within itself (first occurrence), and its unique
+// items are merged level by level into global content tables that number items in order of first
+// appearance. The level sequences of the whole tree are the chunks' sequences concatenated in chunk
+// Morton order (the depth-first Morton traversal visits chunks in that order), so the global
+// numbering is exactly toDAG's first-occurrence numbering of the full tree. Levels above the chunks
+// are built from the chunks' root ids on the host (at most (res/chunkRes)^3 entries).
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+template <int W>
+__device__ __forceinline__ uint64_t contentFp(const uint64_t* k)
+{
+    uint64_t fp = 0x2545F4914F6CDD1Dull;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        fp = mix64(fp ^ k[w]);
+    return fp;
+}
+// Global id of every key that the table already holds, else kNotFound (bounded probing).
+constexpr uint32_t kNotFound = 0xFFFFFFFFu;
+template <int W>
+__global__ void globalFindKernel(const uint64_t* __restrict__ keys, uint32_t n, const uint64_t* __restrict__ slots, uint64_t capMask,
+    const uint64_t* __restrict__ items, uint32_t* __restrict__ outId, uint32_t* __restrict__ missing, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint64_t k[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        k[w] = keys[(uint64_t)i * W + w];
+    const uint64_t fp = contentFp<W>(k);
+    const uint32_t tag = (uint32_t)(fp >> 32);
+    uint64_t slot = fp & capMask;
+    for (uint64_t probe = 0; probe <= capMask; ++probe) {
+        const uint64_t cur = slots[slot];
+        if (cur == kEmptySlot) {
+            outId[i] = kNotFound;
+            missing[i] = 1;
+            return;
+        }
+        if ((uint32_t)(cur >> 32) == tag) {
+            const uint32_t id = (uint32_t)cur;
+            bool eq = true;
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+                eq &= items[(uint64_t)id * W + w] == k[w];
+            if (eq) {
+                outId[i] = id;
+                missing[i] = 0;
+                return;
+            }
+        }
+        slot = (slot + 1) & capMask;
+    }
+    setDeviceError(status, TDAG_ERR_TABLE_FULL, 410);
+    outId[i] = kNotFound;
+    missing[i] = 0;
+}
+// Append the missing keys as ids base + rank (rank = order among the missing ones) and insert them.
+template <int W>
+__global__ void globalAppendKernel(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ missing, const uint32_t* __restrict__ rank,
+    uint64_t base, uint64_t* __restrict__ items, uint64_t* __restrict__ slots, uint64_t capMask, uint32_t* __restrict__ outId, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !missing[i])
+        return;
+    const uint64_t id = base + rank[i];
+    uint64_t k[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        k[w] = keys[(uint64_t)i * W + w];
+        items[id * W + w] = k[w];
+    }
+    outId[i] = (uint32_t)id;
+    const uint64_t fp = contentFp<W>(k);
+    const uint64_t mine = (fp >> 32) << 32 | id;
+    uint64_t slot = fp & capMask;
+    for (uint64_t probe = 0; probe <= capMask; ++probe) {
+        if (atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine) == kEmptySlot)
+            return;
+        slot = (slot + 1) & capMask;
+    }
+    setDeviceError(status, TDAG_ERR_TABLE_FULL, 411);
+}
+template <int W>
+__global__ void globalRehashKernel(const uint64_t* __restrict__ items, uint64_t count, uint64_t* __restrict__ slots, uint64_t capMask, uint32_t* status)
+{
+    const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= count)
+        return;
+    uint64_t k[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        k[w] = items[id * W + w];
+    const uint64_t fp = contentFp<W>(k);
+    const uint64_t mine = (fp >> 32) << 32 | id;
+    uint64_t slot = fp & capMask;
+    for (uint64_t probe = 0; probe <= capMask; ++probe) {
+        if (atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine) == kEmptySlot)
+            return;
+        slot = (slot + 1) & capMask;
+    }
+    setDeviceError(status, TDAG_ERR_TABLE_FULL, 412);
+}
+__global__ void composeIdsKernel(const uint32_t* __restrict__ mapping, uint32_t n, const uint32_t* __restrict__ uniqueId, uint32_t* __restrict__ out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = uniqueId[mapping[i]];
+}
+
+struct GlobalLevel {
+    int words = 1;
+    DevBuf<uint64_t> items; // count x words
+    uint64_t count = 0;
+    DevBuf<uint64_t> slots;
+    uint64_t cap = 0;
+};
+
+void reserveGlobal(Context& ctx, GlobalLevel& g, uint64_t incoming)
+{
+    cudaStream_t s = ctx.stream;
+    const uint64_t need = g.count + incoming;
+    TDAG_CHECK(need < 0xFFFFFFF0ull, TDAG_ERR_ARG, "a level of the streamed scene exceeds 2^32 unique items");
+    if (need * g.words > g.items.n) {
+        const uint64_t n = std::max<uint64_t>(need * g.words, g.items.n * 2);
+        DevBuf<uint64_t> bigger(n, s);
+        if (g.count)
+            TDAG_CUDA(cudaMemcpyAsync(bigger.get(), g.items.get(), g.count * g.words * 8, cudaMemcpyDeviceToDevice, s));
+        g.items = std::move(bigger);
+    }
+    if (need * 2 > g.cap) {
+        g.cap = pow2AtLeast(need * 4 + 64);
+        g.slots = DevBuf<uint64_t>(g.cap, s);
+        fillU64(g.slots.get(), kEmptySlot, g.cap, s);
+        if (g.count) {
+            if (g.words == 1)
+                globalRehashKernel<1><<<gridFor(g.count, 256), 256, 0, s>>>(g.items.get(), g.count, g.slots.get(), g.cap - 1, ctx.status);
+            else
+                globalRehashKernel<4><<<gridFor(g.count, 256), 256, 0, s>>>(g.items.get(), g.count, g.slots.get(), g.cap - 1, ctx.status);
+            TDAG_LAUNCHED();
+        }
+    }
+}
+
+// Merge n items of one chunk level (keys: n x words, in tree order) into the global level; returns
+// every item's global id.
+DevBuf<uint32_t> mergeLevel(Context& ctx, GlobalLevel& g, const uint64_t* keys, uint32_t n)
+{
+    cudaStream_t s = ctx.stream;
+    DevBuf<uint32_t> mapping, firsts;
+    const uint32_t u = dedupLevel(ctx, keys, g.words, n, mapping, firsts); // first occurrence within the chunk
+    DevBuf<uint64_t> ukeys((size_t)u * g.words, s);
+    gatherU64Kernel<<<gridFor((size_t)u * g.words, 256), 256, 0, s>>>(keys, firsts.get(), u, g.words, ukeys.get());
+    TDAG_LAUNCHED();
+    reserveGlobal(ctx, g, u);
+    DevBuf<uint32_t> uid(u, s), missing(u, s), rank(u, s);
+    if (g.words == 1)
+        globalFindKernel<1><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, g.slots.get(), g.cap - 1, g.items.get(), uid.get(), missing.get(), ctx.status);
+    else
+        globalFindKernel<4><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, g.slots.get(), g.cap - 1, g.items.get(), uid.get(), missing.get(), ctx.status);
+    TDAG_LAUNCHED();
+    const uint64_t added = exclusiveScanU32Total(missing.get(), rank.get(), u, s);
+    if (g.words == 1)
+        globalAppendKernel<1><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, missing.get(), rank.get(), g.count, g.items.get(), g.slots.get(), g.cap - 1,
+            uid.get(), ctx.status);
+    else
+        globalAppendKernel<4><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, missing.get(), rank.get(), g.count, g.items.get(), g.slots.get(), g.cap - 1,
+            uid.get(), ctx.status);
+    TDAG_LAUNCHED();
+    g.count += added;
+    DevBuf<uint32_t> ids(n, s);
+    composeIdsKernel<<<gridFor(n, 256), 256, 0, s>>>(mapping.get(), n, uid.get(), ids.get());
+    TDAG_LAUNCHED();
+    return ids;
+}
+
+inline uint32_t log2u(uint32_t v) { return (uint32_t)(31 - __builtin_clz(v)); }
+
+} // namespace
+
+std::unique_ptr<SvdagOwned> sceneSvdagStreamed(Context& ctx, const tdag_scene& sc, uint32_t chunkRes)
+{
+    cudaStream_t s = ctx.stream;
+    const uint32_t res = sc.resolution, root = log2u(res), lc = log2u(chunkRes);
+    TDAG_CHECK(chunkRes >= 64 && chunkRes <= 2048 && (chunkRes & (chunkRes - 1)) == 0 && chunkRes <= res, TDAG_ERR_ARG,
+        "chunk resolution must be a power of two in [64, min(2048, resolution)]");
+    const uint32_t cpa = res / chunkRes;
+    const uint64_t numChunks = (uint64_t)cpa * cpa * cpa;
+    auto prims = scenePrimitives(sc);
+    std::vector<DevPrim> dp(prims.size());
+    for (size_t i = 0; i < prims.size(); ++i)
+        dp[i] = toDevPrim(prims[i]);
+    DevBuf<DevPrim> dprims(std::max<size_t>(1, dp.size()), s);
+    if (!dp.empty())
+        TDAG_CUDA(cudaMemcpyAsync(dprims.get(), dp.data(), dp.size() * sizeof(DevPrim), cudaMemcpyHostToDevice, s));
+    // candidates per chunk (Morton index): primitives whose box, grown by the 1-voxel shell halo, meets it
+    std::vector<std::vector<uint32_t>> perChunk(numChunks);
+    if (sc.kind == TDAG_SCENE_PRIMITIVES)
+        for (uint32_t i = 0; i < dp.size(); ++i) {
+            int lo[3], hi[3];
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::max(0, (dp[i].lo[k] - 1) / (int)chunkRes);
+                hi[k] = std::min((int)cpa - 1, (dp[i].lo[k] + dp[i].ext[k]) / (int)chunkRes);
+            }
+            for (int z = lo[2]; z <= hi[2]; ++z)
+                for (int y = lo[1]; y <= hi[1]; ++y)
+                    for (int x = lo[0]; x <= hi[0]; ++x)
+                        perChunk[morton3((uint32_t)x, (uint32_t)y, (uint32_t)z)].push_back(i);
+        }
+    std::vector<uint32_t> candOff(numChunks + 1, 0), candIds;
+    for (uint64_t m = 0; m < numChunks; ++m) {
+        candOff[m + 1] = candOff[m] + (uint32_t)perChunk[m].size();
+        candIds.insert(candIds.end(), perChunk[m].begin(), perChunk[m].end());
+    }
+    DevBuf<uint32_t> dcand(std::max<size_t>(1, candIds.size()), s);
+    if (!candIds.empty())
+        TDAG_CUDA(cudaMemcpyAsync(dcand.get(), candIds.data(), candIds.size() * 4, cudaMemcpyHostToDevice, s));
+
+    std::vector<GlobalLevel> glv(lc + 1);
+    for (uint32_t l = 2; l <= lc; ++l)
+        glv[l].words = l == 2 ? 1 : 4;
+    std::vector<uint32_t> chunkRoot(numChunks, kEmpty32);
+    uint64_t voxels = 0;
+    const uint32_t bpa = chunkRes / kBrick;
+    const uint64_t cells = (uint64_t)(chunkRes / 4) * (chunkRes / 4) * (chunkRes / 4);
+    for (uint64_t m = 0; m < numChunks; ++m) {
+        const uint32_t nc = candOff[m + 1] - candOff[m];
+        if (sc.kind == TDAG_SCENE_PRIMITIVES && nc == 0)
+            continue; // nothing reaches this chunk: empty
+        const uint32_t cx = compact1by2((uint32_t)m), cy = compact1by2((uint32_t)(m >> 1)), cz = compact1by2((uint32_t)(m >> 2));
+        DevBuf<uint64_t> leafArray(cells, s);
+        sceneBrickKernel<<<(unsigned)((uint64_t)bpa * bpa * bpa), 256, 0, s>>>(dprims.get(), (uint32_t)dp.size(),
+            sc.kind == TDAG_SCENE_PRIMITIVES ? dcand.get() + candOff[m] : nullptr, nc, sc.kind, res, sc.seed, sc.shell, bpa, cx * bpa, cy * bpa, cz * bpa,
+            leafArray.get(), ctx.status);
+        TDAG_LAUNCHED();
+        ctx.checkStatus("scene generation (chunk)");
+        SvdagOwned tree;
+        buildTree(ctx, leafArray, cells, chunkRes, tree);
+        voxels += tree.voxelCount;
+        if (tree.leaves.n == 0)
+            continue;
+        DevBuf<uint32_t> prevIds = mergeLevel(ctx, glv[2], tree.leaves.get(), (uint32_t)tree.leaves.n);
+        for (uint32_t l = 3; l <= lc; ++l) {
+            const uint32_t n = (uint32_t)(tree.nodes[l].n / 8);
+            DevBuf<uint64_t> keys((size_t)n * 4, s);
+            remapChildrenKernel<<<gridFor((size_t)n * 4, 256), 256, 0, s>>>(tree.nodes[l].get(), (uint64_t)n * 8, prevIds.get(), keys.get());
+            TDAG_LAUNCHED();
+            tree.nodes[l].release();
+            prevIds = mergeLevel(ctx, glv[l], keys.get(), n);
+        }
+        TDAG_CUDA(cudaMemcpyAsync(&chunkRoot[m], prevIds.get(), 4, cudaMemcpyDeviceToHost, s));
+        ctx.checkStatus("scene merge (chunk)");
+    }
+
+    auto out = std::make_unique<SvdagOwned>();
+    out->resolution = res;
+    out->rootLevel = root;
+    out->structureType = 1;
+    out->voxelCount = voxels;
+    out->nodes.resize(root + 1);
+    out->leaves = DevBuf<uint64_t>(glv[2].count, s);
+    if (glv[2].count)
+        TDAG_CUDA(cudaMemcpyAsync(out->leaves.get(), glv[2].items.get(), glv[2].count * 8, cudaMemcpyDeviceToDevice, s));
+    for (uint32_t l = 3; l <= lc; ++l) {
+        out->nodes[l] = DevBuf<uint32_t>(glv[l].count * 8, s);
+        if (glv[l].count)
+            TDAG_CUDA(cudaMemcpyAsync(out->nodes[l].get(), glv[l].items.get(), glv[l].count * 32, cudaMemcpyDeviceToDevice, s));
+    }
+    // levels above the chunks: dense Morton arrays of ids, deduplicated by first occurrence
+    std::vector<uint32_t> cur = chunkRoot;
+    for (uint32_t l = lc + 1; l <= root; ++l) {
+        std::vector<uint32_t> next(cur.size() / 8, kEmpty32), nodes;
+        std::map<std::array<uint32_t, 8>, uint32_t> seen;
+        for (size_t p = 0; p < next.size(); ++p) {
+            std::array<uint32_t, 8> c;
+            bool any = false;
+            for (int k = 0; k < 8; ++k) {
+                c[k] = cur[8 * p + k];
+                any |= c[k] != kEmpty32;
+            }
+            if (!any)
+                continue;
+            auto it = seen.find(c);
+            if (it == seen.end()) {
+                it = seen.emplace(c, (uint32_t)(nodes.size() / 8)).first;
+                nodes.insert(nodes.end(), c.begin(), c.end());
+            }
+            next[p] = it->second;
+        }
+        out->nodes[l] = DevBuf<uint32_t>(nodes.size(), s);
+        if (!nodes.empty())
+            TDAG_CUDA(cudaMemcpyAsync(out->nodes[l].get(), nodes.data(), nodes.size() * 4, cudaMemcpyHostToDevice, s));
+        TDAG_CUDA(cudaStreamSynchronize(s)); // `nodes` is reused by the next level
+        cur = std::move(next);
+    }
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    return out;
+}
+
 std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool toDag)
 {
     TDAG_CHECK(sc.kind == TDAG_SCENE_TERRAIN || sc.kind == TDAG_SCENE_PRIMITIVES, TDAG_ERR_ARG, "unknown scene kind");
@@ -542,6 +853,11 @@ std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool 
     cudaStream_t s = ctx.stream;
     const uint32_t res = sc.resolution;
     const uint64_t cells = (uint64_t)(res / 4) * (res / 4) * (res / 4);
+    const uint32_t chunk = sc.chunk_resolution ? sc.chunk_resolution : (res > 4096 ? 2048u : 0u);
+    if (chunk) {
+        TDAG_CHECK(toDag, TDAG_ERR_ARG, "a streamed scene build always deduplicates (to_dag = 1)");
+        return sceneSvdagStreamed(ctx, sc, chunk);
+    }
     TDAG_CHECK(cells < (1ull << 32), TDAG_ERR_ARG, "scene too large for the single-pass generator");
     auto prims = scenePrimitives(sc);
     std::vector<DevPrim> dp(prims.size());
@@ -553,7 +869,8 @@ std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool 
     DevBuf<uint64_t> leafArray(cells, s);
     const uint32_t bpa = res / kBrick;
     const uint64_t bricks = (uint64_t)bpa * bpa * bpa;
-    sceneBrickKernel<<<(unsigned)bricks, 256, 0, s>>>(dprims.get(), (uint32_t)dp.size(), sc.kind, res, sc.seed, sc.shell, bpa, leafArray.get(), ctx.status);
+    sceneBrickKernel<<<(unsigned)bricks, 256, 0, s>>>(dprims.get(), (uint32_t)dp.size(), nullptr, 0, sc.kind, res, sc.seed, sc.shell, bpa, 0, 0, 0,
+        leafArray.get(), ctx.status);
     TDAG_LAUNCHED();
     ctx.checkStatus("scene generation");
     auto out = std::make_unique<SvdagOwned>();

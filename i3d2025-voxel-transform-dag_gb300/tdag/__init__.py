@@ -356,11 +356,13 @@ class SceneSpec:
     num_primitives: int = 4000
     copy_percent: int = 30
     shell: bool = True
+    chunk_resolution: int = 0  # 0: automatic (chunked above 4096^3); else generated in chunks of this size
 
     def to_c(self) -> _abi.Scene:
         c = _abi.Scene()
         c.kind, c.resolution, c.seed = self.kind, self.resolution, self.seed
         c.num_primitives, c.copy_percent, c.shell = self.num_primitives, self.copy_percent, int(self.shell)
+        c.chunk_resolution = self.chunk_resolution
         return c
 
 

@@ -65,7 +65,7 @@ class Result(ctypes.Structure):
 class Scene(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("resolution", ctypes.c_uint32), ("seed", ctypes.c_uint32),
                 ("num_primitives", ctypes.c_uint32), ("copy_percent", ctypes.c_uint32), ("shell", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("chunk_resolution", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class Primitive(ctypes.Structure):

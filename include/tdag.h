@@ -206,7 +206,10 @@ typedef struct tdag_scene {
     uint32_t num_primitives; /* TDAG_SCENE_PRIMITIVES */
     uint32_t copy_percent; /* percent of primitives placed as mirrored / permuted / translated copies */
     uint32_t shell; /* 1: keep only the 1-voxel surface shell (6-neighbourhood) */
-    uint32_t reserved[2];
+    uint32_t chunk_resolution; /* 0: automatic (streamed in 2048^3 chunks above 4096^3). Otherwise the
+                                  grid is generated and deduplicated chunk by chunk (power of two in
+                                  64..2048); the resulting SVDAG is the same. */
+    uint32_t reserved;
 } tdag_scene;
 
 /* One primitive of a TDAG_SCENE_PRIMITIVES scene. A world voxel v is inside when

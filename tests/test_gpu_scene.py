@@ -66,3 +66,16 @@ def test_scene_build_end_to_end_matches_oracle(oracle, tdaglib, gpu_ctx):
     cfg = tdaglib.TransformDAGConfig()
     got = tdaglib.write_tdag(tdaglib.construct_transform_dag(host, cfg, ctx=gpu_ctx), cfg)
     assert got == ref
+
+
+@pytest.mark.parametrize("res,chunk,n,seed,kind", [(256, 64, 200, 3, "primitives"), (512, 128, 600, 8, "primitives"), (256, 128, 50, 4, "primitives"),
+                                                   (128, 64, 0, 2, "terrain")])
+def test_chunked_scene_equals_single_pass(tdaglib, gpu_ctx, res, chunk, n, seed, kind):
+    """The chunked generator (chunk SVOs merged into global first-occurrence tables) builds the same
+    SVDAG as the single-pass generator: same items, same order, same voxel count."""
+    k = tdaglib.SCENE_PRIMITIVES if kind == "primitives" else tdaglib.SCENE_TERRAIN
+    base = dict(kind=k, resolution=res, seed=seed, num_primitives=n, shell=kind == "primitives")
+    one = tdaglib.scene_svdag(tdaglib.SceneSpec(**base), to_dag=True, ctx=gpu_ctx)
+    many = tdaglib.scene_svdag(tdaglib.SceneSpec(**base, chunk_resolution=chunk), to_dag=True, ctx=gpu_ctx)
+    _assert_same(many.to_host(), one.to_host())
+    assert many.voxel_count == one.voxel_count
