@@ -153,6 +153,46 @@ __global__ void __launch_bounds__(256) sceneBrickKernel(const DevPrim* __restric
                 setDeviceError(status, TDAG_ERR_ALLOC, 400);
             return;
         }
+        // A brick whose whole halo box lies inside one box or ball primitive (and inside the grid) is
+        // solid throughout: its shell is empty, its solid leaves are full.
+        __shared__ int covered;
+        if (threadIdx.x == 0)
+            covered = 0;
+        __syncthreads();
+        const bool inGrid = x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + kHalo <= (int)res && y0 + kHalo <= (int)res && z0 + kHalo <= (int)res;
+        if (inGrid)
+            for (uint32_t li = threadIdx.x; li < listCount; li += blockDim.x) {
+                const DevPrim& p = prims[list[li]];
+                const int lo[3] = { x0, y0, z0 };
+                bool in = false;
+                if (p.type == 0) {
+                    in = true;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        in &= p.lo[k] <= lo[k] && lo[k] + kHalo <= p.lo[k] + p.ext[k];
+                } else if (p.type == 1) {
+                    in = true; // a ball is convex: all 8 corners inside -> the box inside
+                    for (int c = 0; c < 8 && in; ++c) {
+                        int64_t d2 = 0;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const int64_t d = (int64_t)(lo[k] + (((c >> k) & 1) ? kHalo - 1 : 0)) - (p.lo[k] + p.radius);
+                            d2 += d * d;
+                        }
+                        in = d2 <= (int64_t)p.radius * p.radius;
+                    }
+                }
+                if (in)
+                    covered = 1;
+            }
+        __syncthreads();
+        if (covered) {
+            for (int l = threadIdx.x; l < 512; l += blockDim.x) {
+                const uint32_t gx = bx * 8 + (l & 7), gy = by * 8 + ((l >> 3) & 7), gz = bz * 8 + (l >> 6);
+                leafArray[(uint64_t)part1by2(gx) | ((uint64_t)part1by2(gy) << 1) | ((uint64_t)part1by2(gz) << 2)] = shell ? 0ull : ~0ull;
+            }
+            return;
+        }
     }
     const uint32_t nList = listCount;
     // ---- inside rows with halo

@@ -79,3 +79,40 @@ def test_chunked_scene_equals_single_pass(tdaglib, gpu_ctx, res, chunk, n, seed,
     many = tdaglib.scene_svdag(tdaglib.SceneSpec(**base, chunk_resolution=chunk), to_dag=True, ctx=gpu_ctx)
     _assert_same(many.to_host(), one.to_host())
     assert many.voxel_count == one.voxel_count
+
+
+def _covered_bricks(res, prims):
+    """32^3 bricks whose 34^3 halo box lies inside one box or ball primitive and inside the grid."""
+    from oracle.generator import PERMS
+    n = 0
+    for bz in range(res // 32):
+        for by in range(res // 32):
+            for bx in range(res // 32):
+                lo = [bx * 32 - 1, by * 32 - 1, bz * 32 - 1]
+                if min(lo) < 0 or max(lo) + 34 > res:
+                    continue
+                for p in prims:
+                    ext = [p["size"][PERMS[p["xform"] & 7][k]] for k in range(3)]
+                    if p["type"] == 0 and all(p["offset"][k] <= lo[k] and lo[k] + 34 <= p["offset"][k] + ext[k] for k in range(3)):
+                        n += 1
+                        break
+                    if p["type"] == 1:
+                        r = p["radius"]
+                        c = [p["offset"][k] + r for k in range(3)]
+                        if all(sum((lo[k] + (33 if (m >> k) & 1 else 0) - c[k]) ** 2 for k in range(3)) <= r * r for m in range(8)):
+                            n += 1
+                            break
+    return n
+
+
+@pytest.mark.parametrize("shell", [True, False])
+def test_scene_with_solid_bricks_matches_cpu_generator(oracle, tdaglib, gpu_ctx, shell):
+    """Large primitives: bricks entirely inside one primitive take the generator's solid-brick exit."""
+    from oracle import generator
+    spec = tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=512, seed=21, num_primitives=60, copy_percent=30, shell=shell)
+    prims = tdaglib.scene_primitives(spec)
+    assert _covered_bricks(512, prims) > 0
+    dense = generator.primitives_scene(512, prims, shell=shell)
+    got = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx)
+    _assert_same(got.to_host(), _svo_struct(tdaglib, oracle, dense, True))
+    assert got.voxel_count == int(dense.sum())
