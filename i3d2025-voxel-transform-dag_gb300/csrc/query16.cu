@@ -200,6 +200,144 @@ __global__ void getKernel(D16 d, const uint32_t* __restrict__ xyz, uint64_t n, u
     out[i] = r;
 }
 
+// ---- ray queries ------------------------------------------------------------------------------
+// Voxel probe for the traversal: solid, or an empty world-aligned box containing the voxel. Above the
+// translation levels pointers only mirror and permute, which keeps child boxes aligned, so a missing
+// child is an empty aligned box of the child's size. Once a translated pointer has been followed (a
+// box of 2^maxTranslationLevel voxels or less) the empty box is the voxel itself.
+__device__ bool probeVoxel(const D16& d, const int w[3], int emptyLo[3], int& emptySize, uint32_t* status)
+{
+    int v[3] = { w[0], w[1], w[2] };
+    uint64_t at = 0;
+    bool aligned = true;
+    for (uint32_t level = d.root; level > 2; --level) {
+        const int half = 1 << (level - 1);
+        const uint32_t ci = (v[0] >= half ? 1u : 0u) | (v[1] >= half ? 2u : 0u) | (v[2] >= half ? 4u : 0u);
+        Ptr16 p;
+        const bool has = decodeChild(d, level, at, ci, p, status);
+        bool inside = has;
+        if (has) {
+            for (int k = 0; k < 3; ++k)
+                v[k] &= half - 1;
+            if (p.t[0] | p.t[1] | p.t[2])
+                aligned = false;
+            inside = applyPointer(p, half, v);
+        }
+        if (!inside) {
+            emptySize = aligned ? half : 1;
+            for (int k = 0; k < 3; ++k)
+                emptyLo[k] = w[k] & ~(emptySize - 1);
+            return false;
+        }
+        at = p.index;
+    }
+    if (at >= d.leafCount) {
+        setDeviceError(status, TDAG_ERR_CORRUPT, 45);
+        emptySize = 1;
+        for (int k = 0; k < 3; ++k)
+            emptyLo[k] = w[k];
+        return false;
+    }
+    if ((d.leaves[at] >> morton3((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2])) & 1)
+        return true;
+    emptySize = 1;
+    for (int k = 0; k < 3; ++k)
+        emptyLo[k] = w[k];
+    return false;
+}
+
+// First solid voxel along each ray (restart traversal, double precision). The ray enters the grid
+// box [0, res)^3, and from each empty box it moves to the neighbouring cell across the face it
+// leaves through (ties: the lowest axis); t is the entry parameter of the hit voxel.
+__global__ void raycastKernel(D16 d, const tdag16_ray* __restrict__ rays, uint64_t n, tdag16_hit* __restrict__ hits, uint32_t maxSteps, uint32_t* status)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const tdag16_ray r = rays[i];
+    tdag16_hit h {};
+    h.t = r.tmax;
+    const double R = (double)d.resolution;
+    double o[3], dir[3], inv[3];
+    for (int k = 0; k < 3; ++k) {
+        o[k] = r.origin[k];
+        dir[k] = r.direction[k];
+        inv[k] = dir[k] != 0.0 ? 1.0 / dir[k] : 0.0;
+    }
+    // entry into the grid box
+    double t0 = r.tmin, t1 = r.tmax;
+    int entryAxis = -1;
+    for (int k = 0; k < 3; ++k) {
+        if (dir[k] == 0.0) {
+            if (o[k] < 0.0 || o[k] >= R)
+                t0 = t1 + 1.0;
+            continue;
+        }
+        double a = (0.0 - o[k]) * inv[k], b = (R - o[k]) * inv[k];
+        if (a > b) {
+            const double tmp = a;
+            a = b;
+            b = tmp;
+        }
+        if (a > t0) {
+            t0 = a;
+            entryAxis = k;
+        }
+        if (b < t1)
+            t1 = b;
+    }
+    if (d.nodeLen[d.root] == 0 || !(t0 < t1)) {
+        hits[i] = h;
+        return;
+    }
+    int c[3];
+    for (int k = 0; k < 3; ++k) {
+        double x = o[k] + t0 * dir[k];
+        int ck = (int)floor(x);
+        if (k == entryAxis)
+            ck = dir[k] > 0 ? 0 : (int)d.resolution - 1;
+        c[k] = min(max(ck, 0), (int)d.resolution - 1);
+    }
+    double t = t0;
+    uint32_t steps = 0;
+    for (; steps < maxSteps; ++steps) {
+        int lo[3], size;
+        if (probeVoxel(d, c, lo, size, status)) {
+            h.hit = 1;
+            h.t = (float)t;
+            h.voxel[0] = (uint32_t)c[0];
+            h.voxel[1] = (uint32_t)c[1];
+            h.voxel[2] = (uint32_t)c[2];
+            break;
+        }
+        // leave the empty box
+        double tk[3];
+        for (int k = 0; k < 3; ++k)
+            tk[k] = dir[k] > 0.0 ? ((double)(lo[k] + size) - o[k]) * inv[k] : dir[k] < 0.0 ? ((double)lo[k] - o[k]) * inv[k] : 1e300;
+        int ax = 0;
+        if (tk[1] < tk[ax])
+            ax = 1;
+        if (tk[2] < tk[ax])
+            ax = 2;
+        const double tn = tk[ax] > t ? tk[ax] : t;
+        if (tn >= t1)
+            break;
+        for (int k = 0; k < 3; ++k) {
+            if (k == ax) {
+                c[k] = dir[k] > 0.0 ? lo[k] + size : lo[k] - 1;
+            } else {
+                const int ck = (int)floor(o[k] + tn * dir[k]);
+                c[k] = min(max(ck, lo[k]), lo[k] + size - 1);
+            }
+        }
+        if (c[ax] < 0 || c[ax] >= (int)d.resolution)
+            break;
+        t = tn;
+    }
+    h.steps = steps;
+    hits[i] = h;
+}
+
 // ---- lossless check ---------------------------------------------------------------------------
 // A pair: a source node and the .tdag16 state covering the same box. map = (mirror | perm << 3)
 // maps box-local world coordinates w into the frame the pending pointer applies to:
@@ -501,6 +639,16 @@ void tdag16Get(Context& c, const Tdag16Device& h, const uint32_t* dXyz, uint64_t
     c.checkStatus("tdag16_get");
 }
 
+void tdag16Raycast(Context& c, const Tdag16Device& h, const tdag16_ray* dRays, uint64_t n, tdag16_hit* dHits)
+{
+    if (n) {
+        const uint32_t maxSteps = 8u * h.d.resolution + 64u; // each step leaves a box; a ray crosses at most 3 * res voxels
+        raycastKernel<<<gridFor(n, 128), 128, 0, c.stream>>>(h.d, dRays, n, dHits, maxSteps, c.status);
+        TDAG_LAUNCHED();
+    }
+    c.checkStatus("tdag16_raycast");
+}
+
 void tdag16Verify(Context& c, const Tdag16Device& h, const tdag_svdag_view& in, tdag16_verify_stats& out)
 {
     cudaStream_t s = c.stream;
@@ -595,6 +743,18 @@ extern "C" int tdag16_get(tdag_ctx* ctx, const tdag16_device* dev, const uint32_
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
         tdag16Get(c, *dev->h, d_xyz, n, d_out);
+    });
+}
+
+extern "C" int tdag16_raycast(tdag_ctx* ctx, const tdag16_device* dev, const tdag16_ray* d_rays, uint64_t n, tdag16_hit* d_hits)
+{
+    using namespace tdag;
+    if (!ctx || !dev || (n && (!d_rays || !d_hits)))
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        tdag16Raycast(c, *dev->h, d_rays, n, d_hits);
     });
 }
 

@@ -601,6 +601,19 @@ class Tdag16Device:
         _abi.check(lib().tdag16_get(self._ctx.handle, self._h, ctypes.c_void_p(t.data_ptr()), n, ctypes.c_void_p(out.data_ptr())))
         return out.cpu().numpy() if on_host else out
 
+    def raycast(self, rays):
+        """First solid voxel per ray: rays is an (n, 8) float32 array (origin xyz, direction xyz, tmin,
+        tmax) on the host or a CUDA tensor. Returns (t, voxel (n, 3), hit, steps) as numpy arrays."""
+        import torch
+        r = rays if (isinstance(rays, torch.Tensor) and rays.is_cuda) else torch.as_tensor(np.ascontiguousarray(rays, dtype=np.float32))
+        r = r.to(device="cuda", dtype=torch.float32).contiguous()
+        n = r.shape[0]
+        out = torch.empty((n, 6), dtype=torch.int32, device=r.device)  # tdag16_hit: t, voxel[3], hit, steps
+        torch.cuda.synchronize()
+        _abi.check(lib().tdag16_raycast(self._ctx.handle, self._h, ctypes.c_void_p(r.data_ptr()), n, ctypes.c_void_p(out.data_ptr())))
+        o = out.cpu().numpy()
+        return o[:, 0].copy().view(np.float32), o[:, 1:4].astype(np.uint32), o[:, 4].astype(np.uint8), o[:, 5].astype(np.uint32)
+
     def verify(self, source: "DeviceSvdag") -> dict:
         """Lossless check against the device SVDAG the DAG was built from (tdag16_verify)."""
         st = _abi.Tdag16VerifyStats()

@@ -111,7 +111,7 @@ EXPORTED = (
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
     "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
-    "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify",
+    "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify", "tdag16_raycast",
 )
 
 # int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources, uint32_t* num_sources)
@@ -169,6 +169,7 @@ def lib(path: str = None):
         L.tdag16_upload.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint64, ctypes.POINTER(vp)]
         L.tdag16_device_free.argtypes = [vp]
         L.tdag16_get.argtypes = [vp, vp, vp, ctypes.c_uint64, vp]
+        L.tdag16_raycast.argtypes = [vp, vp, vp, ctypes.c_uint64, vp]
         L.tdag16_verify.argtypes = [vp, vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Tdag16VerifyStats)]
         L.tdag16_huffman_code_table.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)]

@@ -72,6 +72,25 @@ int tdag16_device_free(tdag16_device* dev);
  * outside the grid answer 0. */
 int tdag16_get(tdag_ctx* ctx, const tdag16_device* dev, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
 
+/* First solid voxel along rays (the CUDA part of the renderer's transform-DAG traversal,
+ * renderer/src/dags/transform_dag/transform_dag.cu:5-41, as a batch query). Rays are in voxel units of
+ * the grid [0, resolution)^3; d_rays and d_hits are device arrays of n entries. hit.t is the ray
+ * parameter where the ray enters the hit voxel (t = tmax and hit = 0 for a miss); steps counts the
+ * empty boxes crossed. Empty space is skipped in aligned boxes above the translation levels and
+ * voxel by voxel inside translated boxes. Computed in double precision. */
+typedef struct tdag16_ray {
+    float origin[3];
+    float direction[3];
+    float tmin, tmax;
+} tdag16_ray;
+typedef struct tdag16_hit {
+    float t;
+    uint32_t voxel[3];
+    uint32_t hit;
+    uint32_t steps;
+} tdag16_hit;
+int tdag16_raycast(tdag_ctx* ctx, const tdag16_device* dev, const tdag16_ray* d_rays, uint64_t n, tdag16_hit* d_hits);
+
 /* Lossless check of a .tdag16 against the SVDAG it encodes (device view, e.g. tdag_svdag_get_view):
  * the role of verifyComplexTransformDAG (transform_dag_encoding.h:81-117). Above box_level the two
  * structures are walked together and every child present on one side only counts as an existence

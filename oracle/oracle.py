@@ -58,6 +58,8 @@ def lib():
         L.orc16_encode.argtypes = [u8p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, u8pp, u64p, u64p,
                                    ctypes.c_uint32]
         L.orc16_decode_dense.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
+        L.orc16_raycast.argtypes = [u8p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64,
+                                    ctypes.POINTER(ctypes.c_float), u32p, u8p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -236,3 +238,17 @@ def decode_tdag16(data: bytes, res: int) -> np.ndarray:
     dense = np.zeros((res, res, res), dtype=np.uint8)
     _chk16(lib().orc16_decode_dense(p, len(data), _p(dense, ctypes.c_uint8), res))
     return dense
+
+
+def raycast_tdag16(data: bytes, rays: np.ndarray):
+    """First solid voxel per ray (n x 8 float32: origin, direction, tmin, tmax) by voxel DDA over the
+    decoder, double precision -> (t float32 [n], voxel uint32 [n, 3], hit uint8 [n])."""
+    a, p = _u8(data)
+    r = np.ascontiguousarray(rays, dtype=np.float32)
+    n = r.shape[0]
+    t = np.zeros(n, np.float32)
+    vox = np.zeros((n, 3), np.uint32)
+    hit = np.zeros(n, np.uint8)
+    _chk16(lib().orc16_raycast(p, len(data), _p(r, ctypes.c_float), n, _p(t, ctypes.c_float), _p(vox, ctypes.c_uint32),
+                               _p(hit, ctypes.c_uint8)))
+    return t, vox, hit

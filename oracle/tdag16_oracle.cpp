@@ -19,6 +19,7 @@
 // with stable radix sorts; the library's encoder is bit-exact with this mode.
 
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <bit>
 #include <cstdint>
@@ -735,6 +736,77 @@ struct Decoder {
     }
 };
 
+// First solid voxel along a ray by voxel-by-voxel DDA (Amanatides and Woo 1987) over Decoder::get, in
+// double precision. Entry into [0, res)^3 by slabs; the crossing parameter of each cell face is
+// recomputed from the cell index, and ties go to the lowest axis. t is where the ray enters the hit voxel.
+struct RayHit {
+    bool hit = false;
+    double t = 0;
+    uint32_t voxel[3] = { 0, 0, 0 };
+};
+static RayHit castRay(const Decoder& dec, uint32_t res, const double o[3], const double dir[3], double tmin, double tmax)
+{
+    RayHit h;
+    h.t = tmax;
+    const double R = res;
+    double inv[3];
+    for (int k = 0; k < 3; ++k)
+        inv[k] = dir[k] != 0.0 ? 1.0 / dir[k] : 0.0;
+    double t0 = tmin, t1 = tmax;
+    int entryAxis = -1;
+    for (int k = 0; k < 3; ++k) {
+        if (dir[k] == 0.0) {
+            if (o[k] < 0.0 || o[k] >= R)
+                t0 = t1 + 1.0;
+            continue;
+        }
+        double a = (0.0 - o[k]) * inv[k], b = (R - o[k]) * inv[k];
+        if (a > b)
+            std::swap(a, b);
+        if (a > t0) {
+            t0 = a;
+            entryAxis = k;
+        }
+        if (b < t1)
+            t1 = b;
+    }
+    if (dec.t.nodes[dec.t.rootLevel].empty() || !(t0 < t1))
+        return h;
+    int c[3];
+    for (int k = 0; k < 3; ++k) {
+        int ck = (int)std::floor(o[k] + t0 * dir[k]);
+        if (k == entryAxis)
+            ck = dir[k] > 0 ? 0 : (int)res - 1;
+        c[k] = std::min(std::max(ck, 0), (int)res - 1);
+    }
+    double t = t0;
+    for (uint64_t steps = 0; steps < 8ull * res + 64; ++steps) {
+        if (dec.get((uint32_t)c[0], (uint32_t)c[1], (uint32_t)c[2])) {
+            h.hit = true;
+            h.t = t;
+            for (int k = 0; k < 3; ++k)
+                h.voxel[k] = (uint32_t)c[k];
+            return h;
+        }
+        double tk[3];
+        for (int k = 0; k < 3; ++k)
+            tk[k] = dir[k] > 0.0 ? ((double)(c[k] + 1) - o[k]) * inv[k] : dir[k] < 0.0 ? ((double)c[k] - o[k]) * inv[k] : 1e300;
+        int ax = 0;
+        if (tk[1] < tk[ax])
+            ax = 1;
+        if (tk[2] < tk[ax])
+            ax = 2;
+        const double tn = std::max(tk[ax], t);
+        if (tn >= t1)
+            return h;
+        c[ax] += dir[ax] > 0.0 ? 1 : -1;
+        if (c[ax] < 0 || c[ax] >= (int)res)
+            return h;
+        t = tn;
+    }
+    return h;
+}
+
 } // namespace orc16
 
 // ================================================================================================
@@ -819,6 +891,37 @@ int orc16_encode(const uint8_t* tdag, uint64_t len, int pointerTables, int huffm
                     s.direct[0], s.direct[1], s.direct[2] };
                 std::memcpy(levelStats + 10 * l, row, sizeof(row));
             }
+        return 0;
+    } catch (const std::exception& e) {
+        return fail16(e);
+    }
+}
+
+// rays: n x 8 floats (origin xyz, direction xyz, tmin, tmax). outT: entry parameter of the hit voxel
+// (tmax on a miss), outVoxel: n x 3, outHit: n.
+int orc16_raycast(const uint8_t* buf, uint64_t len, const float* rays, uint64_t n, float* outT, uint32_t* outVoxel, uint8_t* outHit)
+{
+    try {
+        const auto t = orc16::deserialize(buf, len);
+        const orc16::Decoder d(t);
+        std::string err;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < (int64_t)n; ++i) {
+            try {
+                const float* r = rays + 8 * i;
+                const double o[3] = { r[0], r[1], r[2] }, dir[3] = { r[3], r[4], r[5] };
+                const auto h = orc16::castRay(d, t.resolution, o, dir, r[6], r[7]);
+                outT[i] = (float)h.t;
+                outHit[i] = h.hit ? 1 : 0;
+                for (int k = 0; k < 3; ++k)
+                    outVoxel[3 * i + k] = h.voxel[k];
+            } catch (const std::exception& e) {
+#pragma omp critical
+                err = e.what();
+            }
+        }
+        if (!err.empty())
+            throw std::runtime_error(err);
         return 0;
     } catch (const std::exception& e) {
         return fail16(e);

@@ -134,3 +134,38 @@ def test_verify_reports_a_changed_leaf(tdaglib, gpu_ctx):
     st = tdaglib.Tdag16Device(bytes(bad), ctx=gpu_ctx).verify(sv)
     assert st["voxel_mismatches"] > 0
     assert tdaglib.Tdag16Device(data, ctx=gpu_ctx).verify(sv)["voxel_mismatches"] == 0
+
+
+def _rays(res, n, seed):
+    """Rays from around and inside the grid towards random points, some axis-aligned, some cut short."""
+    rng = np.random.default_rng(seed)
+    org = rng.uniform(-0.3 * res, 1.3 * res, (n, 3))
+    org[: n // 8] = rng.uniform(0.01, res - 0.01, (n // 8, 3))  # starting inside
+    tgt = rng.uniform(0, res, (n, 3))
+    d = tgt - org
+    axis = rng.integers(0, 3, n // 8)
+    d[n // 8: n // 4] = 0.0
+    d[np.arange(n // 8, n // 4), axis] = rng.choice([-1.0, 1.0], n // 8)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tmax = np.full(n, 4.0 * res)
+    tmax[n // 4: n // 4 + n // 16] = rng.uniform(0, res, n // 16)
+    return np.concatenate([org, d, np.zeros((n, 1)), tmax[:, None]], axis=1).astype(np.float32)
+
+
+@pytest.mark.parametrize("pt,hf", [(False, False), (True, True)])
+@pytest.mark.parametrize("maker", ["blocky", "terrain"])
+def test_raycast_matches_oracle_dda(oracle, tdaglib, gpu_ctx, maker, pt, hf):
+    """First hit of 4096 rays: the GPU's box-skipping traversal against a voxel-by-voxel DDA over the
+    oracle's decoder (both double precision, same tie rule)."""
+    from oracle import generator
+    dense = blocky_grid(128, 5) if maker == "blocky" else generator.terrain(128, 3)
+    t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense))
+    data, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
+    rays = _rays(128, 4096, 7)
+    t_ref, v_ref, h_ref = oracle.raycast_tdag16(data, rays)
+    t_got, v_got, h_got, steps = tdaglib.Tdag16Device(data, ctx=gpu_ctx).raycast(rays)
+    assert np.array_equal(h_got, h_ref)
+    assert np.array_equal(v_got[h_ref == 1], v_ref[h_ref == 1])
+    assert np.allclose(t_got, t_ref, rtol=0, atol=1e-3)
+    assert 0.2 < h_ref.mean() < 0.95  # both hits and misses are exercised
+    assert all(dense[z, y, x] for x, y, z in v_got[h_got == 1])
