@@ -978,3 +978,308 @@ int tdag_find_duplicates_level_device(tdag_ctx* ctx, uint32_t level, const uint6
 }
 
 } // extern "C"
+
+// ================================================================================================
+// constructStaticTransformDAG (transform_dag.cpp:242-390): StaticStructure<void, uint32_t> in,
+// StaticStructure<void, TransformPointer> out. A packed level is a word stream: per node a header
+// (child mask) and one word per present child, child words being word offsets into the level below
+// (leaf indices at level 3). The levels are unpacked on the device (node starts found top-down from
+// the parents' child words, then checked to tile each level), built like the EditStructure path
+// except that the hierarchical pass hashes child word offsets (transform_dag_hierarchical.cpp:531-743),
+// and packed again with 64-bit words.
+// ================================================================================================
+namespace tdag {
+namespace {
+
+__global__ void staticChildCountKernel(const uint32_t* __restrict__ words, uint64_t wordCount, const uint32_t* __restrict__ starts, uint32_t n,
+    uint32_t* __restrict__ counts, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t s = starts[i];
+    uint32_t c = 0;
+    if (s < wordCount && (words[s] >> 8) == 0 && s + 1 + (uint64_t)__popc(words[s]) <= wordCount)
+        c = __popc(words[s]);
+    else
+        setDeviceError(status, TDAG_ERR_CORRUPT, 60);
+    counts[i] = c;
+}
+__global__ void staticChildWordsKernel(const uint32_t* __restrict__ words, const uint32_t* __restrict__ starts, uint32_t n, const uint32_t* __restrict__ base,
+    const uint32_t* __restrict__ counts, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t s = starts[i];
+    for (uint32_t j = 0; j < counts[i]; ++j) {
+        keys[base[i] + j] = words[s + 1 + j];
+        vals[base[i] + j] = 0;
+    }
+}
+__global__ void distinctFlagsKernel(const uint64_t* __restrict__ keys, uint32_t m, uint32_t* __restrict__ flags)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m)
+        flags[j] = (j == 0 || keys[j] != keys[j - 1]) ? 1u : 0u;
+}
+__global__ void distinctGatherKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ idx, uint32_t u, uint32_t* __restrict__ out)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < u)
+        out[j] = (uint32_t)keys[idx[j]];
+}
+// The starts found from the parents must tile the level: node j ends where node j + 1 starts.
+__global__ void staticTileCheckKernel(const uint32_t* __restrict__ words, uint64_t wordCount, const uint32_t* __restrict__ starts, uint32_t n, uint32_t* status)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n)
+        return;
+    const uint32_t s = starts[j];
+    bool ok = s < wordCount && (j > 0 || s == 0);
+    if (ok) {
+        const uint32_t h = words[s];
+        const uint64_t end = (uint64_t)s + 1 + __popc(h);
+        ok = (h >> 8) == 0 && end == (j + 1 < n ? (uint64_t)starts[j + 1] : wordCount);
+    }
+    if (!ok)
+        setDeviceError(status, TDAG_ERR_CORRUPT, 61);
+}
+// Packed node -> EditNode<uint32_t> (children as indices into the level below).
+__global__ void staticUnpackKernel(const uint32_t* __restrict__ words, const uint32_t* __restrict__ starts, uint32_t n, const uint32_t* __restrict__ childStarts,
+    uint32_t childCount, bool leavesBelow, uint32_t* __restrict__ nodes, uint32_t* status)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t s = starts[i];
+    const uint32_t mask = words[s];
+    uint32_t w = s + 1;
+    for (uint32_t k = 0; k < 8; ++k) {
+        uint32_t out = kEmpty32;
+        if ((mask >> k) & 1) {
+            const uint32_t v = words[w++];
+            if (leavesBelow) {
+                out = v;
+                if (v >= childCount)
+                    setDeviceError(status, TDAG_ERR_CORRUPT, 62);
+            } else {
+                uint32_t lo = 0, hi = childCount; // first start >= v
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (childStarts[mid] < v)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                if (lo < childCount && childStarts[lo] == v)
+                    out = lo;
+                else
+                    setDeviceError(status, TDAG_ERR_CORRUPT, 63);
+            }
+        }
+        nodes[(size_t)i * 8 + k] = out;
+    }
+}
+__global__ void packSizeKernel(const uint64_t* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ sizes)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t w = 1;
+    for (int k = 0; k < 8; ++k)
+        w += nodes[(size_t)i * 8 + k] != tpSentinel() ? 1u : 0u;
+    sizes[i] = w;
+}
+__global__ void packKernel(const uint64_t* __restrict__ nodes, uint32_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ childOff,
+    uint64_t* __restrict__ words)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint64_t at = off[i];
+    const uint64_t head = at++;
+    uint64_t mask = 0;
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t c = nodes[(size_t)i * 8 + k];
+        if (c == tpSentinel())
+            continue;
+        mask |= 1ull << k;
+        words[at++] = childOff ? tpWithPtr(c, childOff[tpPtr(c)]) : c;
+    }
+    words[head] = mask;
+}
+
+} // namespace
+
+struct StaticOut {
+    std::vector<DevBuf<uint64_t>> words;
+    std::vector<uint64_t> wordCounts;
+    DevBuf<uint64_t> leaves;
+    uint64_t leafCount = 0;
+};
+
+StaticOut buildStatic(Context& c, const tdag_static_view& in, const tdag_config& cfg, tdag_stats* stats)
+{
+    cudaStream_t s = c.stream;
+    const uint32_t root = in.root_level;
+    TDAG_CHECK(root >= 3 && root < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "root_level out of range");
+    TDAG_CHECK(in.resolution == (1u << root), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
+    TDAG_CHECK(in.leaf_count < (1ull << 31), TDAG_ERR_ARG, "too many leaves");
+    // upload the packed levels
+    std::vector<DevBuf<uint32_t>> words(root + 1);
+    for (uint32_t l = 3; l <= root; ++l) {
+        TDAG_CHECK(in.word_counts[l] < 0xFFFFFFFFull, TDAG_ERR_ARG, "a packed level exceeds 2^32 words");
+        TDAG_CHECK(in.word_counts[l] == 0 || in.words[l] != nullptr, TDAG_ERR_ARG, "null word array with non-zero count");
+        words[l] = DevBuf<uint32_t>(std::max<uint64_t>(in.word_counts[l], 1), s);
+        if (in.word_counts[l])
+            TDAG_CUDA(cudaMemcpyAsync(words[l].get(), in.words[l], in.word_counts[l] * 4, cudaMemcpyHostToDevice, s));
+    }
+    DevBuf<uint64_t> leaves(std::max<uint64_t>(in.leaf_count, 1), s);
+    if (in.leaf_count)
+        TDAG_CUDA(cudaMemcpyAsync(leaves.get(), in.leaves, in.leaf_count * 8, cudaMemcpyHostToDevice, s));
+    // node starts, top-down: the root level holds one node at word 0; every other level's starts are
+    // the distinct child words of the level above
+    std::vector<DevBuf<uint32_t>> starts(root + 1);
+    std::vector<uint32_t> count(root + 1, 0);
+    count[root] = in.word_counts[root] ? 1 : 0;
+    starts[root] = DevBuf<uint32_t>(1, s);
+    TDAG_CUDA(cudaMemsetAsync(starts[root].get(), 0, 4, s));
+    for (uint32_t l = root; l >= 3; --l) {
+        const uint32_t n = count[l];
+        if (n) {
+            staticTileCheckKernel<<<gridFor(n, 256), 256, 0, s>>>(words[l].get(), in.word_counts[l], starts[l].get(), n, c.status);
+            TDAG_LAUNCHED();
+        } else {
+            TDAG_CHECK(in.word_counts[l] == 0, TDAG_ERR_CORRUPT, "a packed level holds words no parent references");
+        }
+        c.checkStatus("static input: node starts");
+        if (l == 3)
+            break;
+        DevBuf<uint32_t> cnt(std::max<uint32_t>(n, 1), s), base(std::max<uint32_t>(n, 1), s);
+        uint32_t m = 0;
+        if (n) {
+            staticChildCountKernel<<<gridFor(n, 256), 256, 0, s>>>(words[l].get(), in.word_counts[l], starts[l].get(), n, cnt.get(), c.status);
+            TDAG_LAUNCHED();
+            m = (uint32_t)exclusiveScanU32Total(cnt.get(), base.get(), n, s);
+        }
+        DevBuf<uint64_t> keys(std::max<uint32_t>(m, 1), s);
+        DevBuf<uint32_t> vals(std::max<uint32_t>(m, 1), s), flags(std::max<uint32_t>(m, 1), s), idx(std::max<uint32_t>(m, 1), s);
+        uint32_t u = 0;
+        if (m) {
+            staticChildWordsKernel<<<gridFor(n, 256), 256, 0, s>>>(words[l].get(), starts[l].get(), n, base.get(), cnt.get(), keys.get(), vals.get());
+            TDAG_LAUNCHED();
+            radixSortPairs(keys.get(), vals.get(), m, 0, 32, s);
+            distinctFlagsKernel<<<gridFor(m, 256), 256, 0, s>>>(keys.get(), m, flags.get());
+            TDAG_LAUNCHED();
+            u = compactFlags(flags.get(), idx.get(), m, s);
+        }
+        starts[l - 1] = DevBuf<uint32_t>(std::max<uint32_t>(u, 1), s);
+        if (u) {
+            distinctGatherKernel<<<gridFor(u, 256), 256, 0, s>>>(keys.get(), idx.get(), u, starts[l - 1].get());
+            TDAG_LAUNCHED();
+        }
+        count[l - 1] = u;
+    }
+    // unpack into EditNode<uint32_t> levels
+    std::vector<DevBuf<uint32_t>> nodes(root + 1);
+    DeviceSvdag dv;
+    dv.resolution = in.resolution;
+    dv.rootLevel = root;
+    dv.staticOffsets = true;
+    for (uint32_t l = 3; l <= root; ++l) {
+        nodes[l] = DevBuf<uint32_t>(std::max<uint64_t>((uint64_t)count[l] * 8, 1), s);
+        if (count[l]) {
+            staticUnpackKernel<<<gridFor(count[l], 256), 256, 0, s>>>(words[l].get(), starts[l].get(), count[l], l == 3 ? nullptr : starts[l - 1].get(),
+                l == 3 ? (uint32_t)in.leaf_count : count[l - 1], l == 3, nodes[l].get(), c.status);
+            TDAG_LAUNCHED();
+        }
+        dv.nodes[l] = nodes[l].get();
+        dv.nodeCounts[l] = count[l];
+    }
+    dv.leaves = leaves.get();
+    dv.leafCount = in.leaf_count;
+    c.checkStatus("static input: unpack");
+    words.clear();
+    starts.clear();
+    DeviceResult dr = buildDevice(c, dv, cfg, stats);
+    // pack with 64-bit words: child TransformPointers point at word offsets (level 3: leaf indices)
+    StaticOut out;
+    out.words.resize(root + 1);
+    out.wordCounts.assign(root + 1, 0);
+    DevBuf<uint32_t> prevOff;
+    for (uint32_t l = 3; l <= root; ++l) {
+        const uint32_t n = (uint32_t)(dr.levels[l].n / 8);
+        DevBuf<uint32_t> sizes(std::max<uint32_t>(n, 1), s), off(std::max<uint32_t>(n, 1), s);
+        uint64_t total = 0;
+        if (n) {
+            packSizeKernel<<<gridFor(n, 256), 256, 0, s>>>(dr.levels[l].get(), n, sizes.get());
+            TDAG_LAUNCHED();
+            total = exclusiveScanU32Total(sizes.get(), off.get(), n, s);
+        }
+        out.words[l] = DevBuf<uint64_t>(std::max<uint64_t>(total, 1), s);
+        out.wordCounts[l] = total;
+        if (n) {
+            packKernel<<<gridFor(n, 256), 256, 0, s>>>(dr.levels[l].get(), n, off.get(), l == 3 ? nullptr : prevOff.get(), out.words[l].get());
+            TDAG_LAUNCHED();
+        }
+        prevOff = std::move(off);
+    }
+    out.leafCount = dr.leaves.n;
+    out.leaves = std::move(dr.leaves);
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    return out;
+}
+
+} // namespace tdag
+
+extern "C" {
+
+int tdag_static_result_free(tdag_static_result* r);
+
+int tdag_build_static(tdag_ctx* ctx, const tdag_static_view* in, const tdag_config* cfg, tdag_static_result** out)
+{
+    if (!ctx || !in || !cfg || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        Context& c = ctx->c;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        std::unique_ptr<tdag_static_result, int (*)(tdag_static_result*)> r(new tdag_static_result, tdag_static_result_free);
+        std::memset(r.get(), 0, sizeof(tdag_static_result));
+        r->resolution = in->resolution;
+        r->root_level = in->root_level;
+        r->structure_type = 0;
+        StaticOut so = buildStatic(c, *in, *cfg, &r->stats);
+        std::vector<Download> dl;
+        for (uint32_t l = 3; l <= in->root_level; ++l) {
+            r->word_counts[l] = so.wordCounts[l];
+            if (so.wordCounts[l]) {
+                r->words[l] = static_cast<uint64_t*>(std::malloc(so.wordCounts[l] * 8));
+                TDAG_CHECK(r->words[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
+                dl.push_back({ r->words[l], so.words[l].get(), so.wordCounts[l] * 8 });
+            }
+        }
+        r->leaf_count = so.leafCount;
+        if (so.leafCount) {
+            r->leaves = static_cast<uint64_t*>(std::malloc(so.leafCount * 8));
+            TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
+            dl.push_back({ r->leaves, so.leaves.get(), so.leafCount * 8 });
+        }
+        downloadStaged(c, dl);
+        *out = r.release();
+    });
+}
+
+int tdag_static_result_free(tdag_static_result* r)
+{
+    if (!r)
+        return TDAG_OK;
+    for (uint32_t l = 0; l < TDAG_MAX_LEVELS; ++l)
+        std::free(r->words[l]);
+    std::free(r->leaves);
+    delete r;
+    return TDAG_OK;
+}
+
+} // extern "C"

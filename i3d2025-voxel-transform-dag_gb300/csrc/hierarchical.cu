@@ -254,9 +254,11 @@ __device__ __forceinline__ bool lexLess(const uint64_t a[8], const uint64_t b[8]
     return false;
 }
 
+// prevValue (optional, static input): the value hashed for a child handle h is prevValue[h], the
+// word offset of that node in its packed level (transform_dag_hierarchical.cpp:597-606, 696-703).
 __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __restrict__ nodes, uint32_t n, const uint64_t* __restrict__ prevMap,
     const uint8_t* __restrict__ prevRep, const TransformTables* __restrict__ tables, uint64_t allowed, uint64_t* __restrict__ sig, uint64_t* __restrict__ key,
-    const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff)
+    const uint32_t* __restrict__ gridOf, const uint32_t* __restrict__ prevHandleOff, const uint32_t* __restrict__ prevValue)
 {
     __shared__ SmemTables st;
     __shared__ ChildSlots cs;
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) nodeSigKernel(const uint32_t* __rest
     for (int k = 0; k < 8; ++k) {
         ch[k] = loadChild(node, k, prevMap);
         cs.put(k, ch[k]);
-        p[k] = ch[k].h == kEmpty32 ? (uint64_t)kEmpty32 : (uint64_t)(ch[k].h - hbase);
+        p[k] = ch[k].h == kEmpty32 ? (uint64_t)kEmpty32 : prevValue ? (uint64_t)prevValue[ch[k].h] : (uint64_t)(ch[k].h - hbase);
     }
     key[i] = sortedPtrHash(p);
     uint64_t best[8], cur[8];
@@ -541,6 +543,20 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     return u;
 }
 
+namespace {
+// Words of a packed node: one header plus one per present child (8 TransformPointers per node in).
+__global__ void packedSizeKernel(const uint64_t* __restrict__ nodes, uint32_t n, uint32_t* __restrict__ sizes)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t w = 1;
+    for (int k = 0; k < 8; ++k)
+        w += nodes[(size_t)i * 8 + k] != tpSentinel() ? 1u : 0u;
+    sizes[i] = w;
+}
+} // namespace
+
 HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, uint32_t midLevel, tdag_stats* stats)
 {
     cudaStream_t s = ctx.stream;
@@ -622,6 +638,7 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         }
         traceMark(n, u);
     }
+    DevBuf<uint32_t> prevWordOff; // static input: word offsets of the previous level's emitted nodes
     for (uint32_t level = 3; level <= in.rootLevel; ++level) {
         const uint32_t n = (uint32_t)in.nodeCounts[level];
         const uint32_t* nodes = in.nodes[level];
@@ -632,7 +649,7 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         DevBuf<uint64_t> sig((size_t)n * sw, s), key(n, s);
         if (n) {
             nodeSigKernel<<<gridFor(n, kThreads), kThreads, 0, s>>>(nodes, n, prevMap.get(), prevRep.get(), ctx.tables, allowed, sig.get(), key.get(), gridOf,
-                gridOf ? prevHandleOffDev.get() : nullptr);
+                gridOf ? prevHandleOffDev.get() : nullptr, (in.staticOffsets && level >= 4) ? prevWordOff.get() : nullptr);
             TDAG_LAUNCHED();
         }
         const uint64_t* pm = prevMap.get();
@@ -661,6 +678,17 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         prevInv = std::move(inv);
         if (level < in.rootLevel)
             buildRep(u);
+        if (in.staticOffsets && level < in.rootLevel) {
+            // word offsets of this level's emitted nodes when packed (header + one word per child)
+            DevBuf<uint32_t> sizes(std::max<uint32_t>(u, 1), s);
+            prevWordOff = DevBuf<uint32_t>(std::max<uint32_t>(u, 1), s);
+            if (u) {
+                packedSizeKernel<<<gridFor(u, 256), 256, 0, s>>>(lvl.get(), u, sizes.get());
+                TDAG_LAUNCHED();
+                const uint64_t words = exclusiveScanU32Total(sizes.get(), prevWordOff.get(), u, s);
+                TDAG_CHECK(words < 0xFFFFFFFFull, TDAG_ERR_ARG, "a packed level exceeds 2^32 words");
+            }
+        }
         if (stats) {
             stats->hierarchical[level].items = n;
             stats->hierarchical[level].unique = u;

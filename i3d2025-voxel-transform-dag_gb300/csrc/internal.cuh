@@ -38,6 +38,9 @@ struct DeviceSvdag {
     uint32_t numGrids = 1;
     std::vector<uint64_t> segOff[TDAG_MAX_LEVELS];
     const uint32_t* gridOf[TDAG_MAX_LEVELS] {};
+    // StaticStructure input (constructStaticTransformDAG): the hierarchical pass groups nodes by a
+    // hash of their children's word offsets in the packed levels instead of their indices.
+    bool staticOffsets = false;
 };
 
 // Grid segmentation of a list of items (host offsets + device per-item grid ids and offsets).

@@ -631,3 +631,126 @@ class Tdag16Device:
             self.free()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------------------
+# StaticStructure (structure.h:298-320, 765-798, 859-895) and constructStaticTransformDAG
+# ------------------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class StaticStructure:
+    """StaticStructure<void, Child>: ``words[l]`` is level l's packed word stream (uint32 for
+    ``child_type="u32"``, uint64 TransformPointers for ``"transform"``): per node a header word (child
+    mask) and one word per present child, the child's word offset in level l-1 (leaf index at level 3)."""
+
+    words: List[np.ndarray]
+    sub_grids: np.ndarray
+    resolution: int
+    root_level: int
+    structure_type: int = 0
+    child_type: str = "u32"
+
+    @property
+    def word_dtype(self):
+        return np.uint32 if self.child_type == "u32" else np.uint64
+
+    @classmethod
+    def from_edit(cls, e: EditStructure) -> "StaticStructure":
+        """StaticStructure(const EditStructure&) (structure.h:765-798)."""
+        is_tp = e.child_type == "transform"
+        dt = np.uint64 if is_tp else np.uint32
+        empty = np.uint64(tp_create(0xFFFFFFFF)) if is_tp else np.uint32(0xFFFFFFFF)
+        ptr_mask = np.uint64((1 << 37) - 1)
+        prev = np.arange(len(e.sub_grids), dtype=np.uint64)
+        words = [np.zeros(0, dt) for _ in range(len(e.nodes_per_level))]
+        for lvl in range(3, e.root_level + 1):
+            nodes = np.asarray(e.nodes_per_level[lvl], dtype=dt).reshape(-1, 8)
+            present = nodes != empty
+            sizes = 1 + present.sum(axis=1)
+            starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+            w = np.zeros(int(sizes.sum()), dt)
+            w[starts.astype(np.int64)] = (present.astype(dt) << np.arange(8, dtype=dt)).sum(axis=1).astype(dt)
+            rank = np.cumsum(present, axis=1) - 1
+            r, k = np.nonzero(present)
+            pos = (starts[r] + 1 + rank[r, k].astype(np.uint64)).astype(np.int64)
+            c = nodes[r, k]
+            if is_tp:
+                w[pos] = (c & ~ptr_mask) | prev[(c & ptr_mask).astype(np.int64)]
+            else:
+                w[pos] = prev[c.astype(np.int64)].astype(dt)
+            words[lvl] = w
+            prev = starts
+        return cls(words, np.asarray(e.sub_grids, np.uint64).copy(), e.resolution, e.root_level, e.structure_type, e.child_type)
+
+    def to_bytes(self) -> bytes:
+        """StaticStructure::writeTo (structure.h:887-895)."""
+        out = [struct.pack("<Q", len(self.words))]
+        for w in self.words:
+            a = np.ascontiguousarray(w, dtype=self.word_dtype)
+            out.append(struct.pack("<Q", a.shape[0]))
+            out.append(a.tobytes())
+        sg = np.ascontiguousarray(self.sub_grids, dtype=np.uint64)
+        out.append(struct.pack("<Q", sg.shape[0]))
+        out.append(sg.tobytes())
+        out.append(struct.pack("<III", self.resolution, self.root_level, self.structure_type))
+        return b"".join(out)
+
+    @classmethod
+    def from_bytes(cls, buf: bytes, child_type: str = "u32") -> "StaticStructure":
+        dt = np.uint32 if child_type == "u32" else np.uint64
+        off = 0
+
+        def take(n):
+            nonlocal off
+            if off + n > len(buf):
+                raise TDagError(_abi.TDAG_ERR_CORRUPT, "truncated static structure")
+            b = buf[off: off + n]
+            off += n
+            return b
+
+        (nl,) = struct.unpack("<Q", take(8))
+        if nl > 64:
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "corrupt level count")
+        words = []
+        for _ in range(nl):
+            (cnt,) = struct.unpack("<Q", take(8))
+            words.append(np.frombuffer(take(cnt * np.dtype(dt).itemsize), dtype=dt).copy())
+        (cnt,) = struct.unpack("<Q", take(8))
+        sg = np.frombuffer(take(cnt * 8), dtype=np.uint64).copy()
+        res, root, st = struct.unpack("<III", take(12))
+        if root + 1 != nl or off != len(buf):
+            raise TDagError(_abi.TDAG_ERR_CORRUPT, "malformed static structure")
+        return cls(words, sg, res, root, st, child_type)
+
+
+def construct_static_transform_dag(in_dag: StaticStructure, config: TransformDAGConfig = TransformDAGConfig(),
+                                   ctx: Optional[Context] = None, return_stats: bool = False):
+    """constructStaticTransformDAG (transform_dag.h:163; transform_dag.cpp:242-390): returns a
+    StaticStructure of TransformPointers."""
+    assert in_dag.child_type == "u32"
+    ctx = ctx or default_context()
+    v = _abi.StaticView()
+    v.resolution, v.root_level, v.structure_type = in_dag.resolution, in_dag.root_level, in_dag.structure_type
+    keep = []
+    for lvl in range(3, in_dag.root_level + 1):
+        a = np.ascontiguousarray(in_dag.words[lvl], dtype=np.uint32)
+        keep.append(a)
+        v.words[lvl] = a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        v.word_counts[lvl] = a.shape[0]
+    sg = np.ascontiguousarray(in_dag.sub_grids, dtype=np.uint64)
+    keep.append(sg)
+    v.leaves = sg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    v.leaf_count = sg.shape[0]
+    rp = ctypes.POINTER(_abi.StaticResult)()
+    _abi.check(lib().tdag_build_static(ctx.handle, ctypes.byref(v), ctypes.byref(_config_struct(config)), ctypes.byref(rp)))
+    try:
+        r = rp.contents
+        words = []
+        for lvl in range(r.root_level + 1):
+            cnt = r.word_counts[lvl]
+            words.append(np.ctypeslib.as_array(r.words[lvl], shape=(cnt,)).copy() if (lvl >= 3 and cnt) else np.zeros(0, np.uint64))
+        leaves = np.ctypeslib.as_array(r.leaves, shape=(r.leaf_count,)).copy() if r.leaf_count else np.zeros(0, np.uint64)
+        out = StaticStructure(words, leaves, r.resolution, r.root_level, r.structure_type, "transform")
+        stats = _abi.stats_to_dict(r.stats, r.root_level)
+    finally:
+        lib().tdag_static_result_free(rp)
+    return (out, stats) if return_stats else out

@@ -62,6 +62,23 @@ class Result(ctypes.Structure):
                 ("stats", Stats)]
 
 
+class StaticView(ctypes.Structure):
+    _fields_ = [("resolution", ctypes.c_uint32), ("root_level", ctypes.c_uint32),
+                ("structure_type", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("words", ctypes.POINTER(ctypes.c_uint32) * MAX_LEVELS),
+                ("word_counts", ctypes.c_uint64 * MAX_LEVELS),
+                ("leaves", ctypes.POINTER(ctypes.c_uint64)), ("leaf_count", ctypes.c_uint64)]
+
+
+class StaticResult(ctypes.Structure):
+    _fields_ = [("resolution", ctypes.c_uint32), ("root_level", ctypes.c_uint32),
+                ("structure_type", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("words", ctypes.POINTER(ctypes.c_uint64) * MAX_LEVELS),
+                ("word_counts", ctypes.c_uint64 * MAX_LEVELS),
+                ("leaves", ctypes.POINTER(ctypes.c_uint64)), ("leaf_count", ctypes.c_uint64),
+                ("stats", Stats)]
+
+
 class Scene(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("resolution", ctypes.c_uint32), ("seed", ctypes.c_uint32),
                 ("num_primitives", ctypes.c_uint32), ("copy_percent", ctypes.c_uint32), ("shell", ctypes.c_uint32),
@@ -109,6 +126,7 @@ EXPORTED = (
     "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
+    "tdag_build_static", "tdag_static_result_free",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
     "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
     "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify", "tdag16_raycast",
@@ -163,6 +181,8 @@ def lib(path: str = None):
         L.tdag_build_device_proposed.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), PROPOSAL_FN, vp,
                                                  ctypes.POINTER(ctypes.POINTER(Result))]
         L.tdag_device_copy.argtypes = [vp, vp, vp, ctypes.c_uint64]
+        L.tdag_build_static.argtypes = [vp, ctypes.POINTER(StaticView), ctypes.POINTER(Config), ctypes.POINTER(ctypes.POINTER(StaticResult))]
+        L.tdag_static_result_free.argtypes = [ctypes.POINTER(StaticResult)]
         L.tdag_encode16.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(Config), ctypes.POINTER(EncodingConfig),
                                     ctypes.POINTER(ctypes.POINTER(Tdag16Result))]
         L.tdag16_result_free.argtypes = [ctypes.POINTER(Tdag16Result)]

@@ -190,6 +190,44 @@ int tdag_device_copy(tdag_ctx* ctx, void* d_dst, const void* d_src, uint64_t byt
  * Host in, host out. */
 int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in_host, const tdag_config* config, tdag_result** out);
 
+/* StaticStructure (tools/lib/include/voxcom/voxel/structure.h:298-320, 765-798): the memory-lean
+ * packed layout. Per level a word stream; every node is a header word (child mask, bit i = child i)
+ * followed by one word per present child in child order, each the word offset of the child in the
+ * level below (level 3: the leaf index). Input words are uint32_t (StaticStructure<void, uint32_t>),
+ * output words uint64_t (StaticStructure<void, TransformPointer>: headers and TransformPointers). */
+typedef struct tdag_static_view {
+    uint32_t resolution;
+    uint32_t root_level;
+    uint32_t structure_type;
+    uint32_t reserved;
+    const uint32_t* words[TDAG_MAX_LEVELS]; /* host memory, levels 3..root_level */
+    uint64_t word_counts[TDAG_MAX_LEVELS];
+    const uint64_t* leaves;
+    uint64_t leaf_count;
+} tdag_static_view;
+
+typedef struct tdag_static_result {
+    uint32_t resolution;
+    uint32_t root_level;
+    uint32_t structure_type;
+    uint32_t reserved;
+    uint64_t* words[TDAG_MAX_LEVELS]; /* host memory owned by the library */
+    uint64_t word_counts[TDAG_MAX_LEVELS];
+    uint64_t* leaves;
+    uint64_t leaf_count;
+    tdag_stats stats;
+} tdag_static_result;
+
+/* constructStaticTransformDAG(StaticStructure<void, uint32_t>&&, config)
+ * (tools/lib/include/voxcom/voxel/transform_dag.h:163; tools/lib/src/voxel/transform_dag.cpp:242-390).
+ * The same construction as tdag_build, except that its hierarchical pass groups nodes by a hash of
+ * their children's word offsets (transform_dag_hierarchical.cpp:531-743), which orders the levels
+ * above the translation levels differently. Every node of a packed level must be referenced by the
+ * level above (true of SVDAGs); a level holding unreferenced words is rejected (TDAG_ERR_CORRUPT).
+ * Release the result with tdag_static_result_free. */
+int tdag_build_static(tdag_ctx* ctx, const tdag_static_view* in_host, const tdag_config* config, tdag_static_result** out);
+int tdag_static_result_free(tdag_static_result* result);
+
 /* ------------------------------------------------------------------------------------------------
  * Input side of the path: procedural scenes, SVO construction and toDAG on the device.
  * (EditStructure(VoxelGrid), structure.h:423-429, 658-701; EditStructure::toDAG, structure.h:703-763.)

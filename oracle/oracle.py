@@ -60,6 +60,10 @@ def lib():
         L.orc16_decode_dense.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
         L.orc16_raycast.argtypes = [u8p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64,
                                     ctypes.POINTER(ctypes.c_float), u32p, u8p]
+        L.orc_to_static.argtypes = [u8p, ctypes.c_uint64, u8pp, u64p]
+        L.orc_construct_static_tdag.argtypes = [u8p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                                                u8pp, u64p]
+        L.orc_static_tdag_decode.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -252,3 +256,32 @@ def raycast_tdag16(data: bytes, rays: np.ndarray):
     _chk16(lib().orc16_raycast(p, len(data), _p(r, ctypes.c_float), n, _p(t, ctypes.c_float), _p(vox, ctypes.c_uint32),
                                _p(hit, ctypes.c_uint8)))
     return t, vox, hit
+
+
+# ------------------------------------------------------------------------------------------------
+# StaticStructure path (constructStaticTransformDAG)
+# ------------------------------------------------------------------------------------------------
+def to_static(svo: bytes) -> bytes:
+    """StaticStructure<void, uint32_t>(EditStructure) of an .svo, as StaticStructure::writeTo bytes."""
+    a, p = _u8(svo)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    _chk(lib().orc_to_static(p, len(svo), ctypes.byref(out), ctypes.byref(n)))
+    return _take(out, n)
+
+
+def construct_static_tdag(static_bytes: bytes, symmetry=True, axis=True, translation=True, max_level=4) -> bytes:
+    """constructStaticTransformDAG -> StaticStructure<void, TransformPointer>::writeTo bytes."""
+    a, p = _u8(static_bytes)
+    out = ctypes.POINTER(ctypes.c_uint8)()
+    n = ctypes.c_uint64()
+    _chk(lib().orc_construct_static_tdag(p, len(static_bytes), int(symmetry), int(axis), int(translation), int(max_level),
+                                         ctypes.byref(out), ctypes.byref(n)))
+    return _take(out, n)
+
+
+def static_tdag_decode(static_tdag: bytes, res: int) -> np.ndarray:
+    a, p = _u8(static_tdag)
+    dense = np.zeros((res, res, res), dtype=np.uint8)
+    _chk(lib().orc_static_tdag_decode(p, len(static_tdag), dense.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), res))
+    return dense

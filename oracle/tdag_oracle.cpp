@@ -489,7 +489,10 @@ struct HierResult {
 
 // processLevel (:359-448): group by hash of sorted child ptrs, canonical search in (hash, index) order.
 // outHandles receives, for each emitted (canonical) node, its input index in emission order.
-static void processLevel(const std::vector<TNode>& nodes, std::vector<Tagged>& mapping, std::vector<uint32_t>& emitted, const Config& cfg)
+// ptrValue (optional): the value hashed for a child pointer ptr, ptrValue[ptr] (the static variant
+// hashes the child's word offset in its packed level, transform_dag_hierarchical.cpp:597-606, 696-703).
+static void processLevel(const std::vector<TNode>& nodes, std::vector<Tagged>& mapping, std::vector<uint32_t>& emitted, const Config& cfg,
+    const std::vector<uint64_t>* ptrValue = nullptr)
 {
     const size_t n = nodes.size();
     mapping.assign(n, Tagged {});
@@ -500,8 +503,10 @@ static void processLevel(const std::vector<TNode>& nodes, std::vector<Tagged>& m
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
         std::array<uint64_t, 8> p;
-        for (int k = 0; k < 8; ++k)
-            p[k] = nodes[i].c[k].ptr;
+        for (int k = 0; k < 8; ++k) {
+            const uint64_t c = nodes[i].c[k].ptr;
+            p[k] = (ptrValue && c != 0xFFFFFFFFull) ? (*ptrValue)[c] : c;
+        }
         std::sort(p.begin(), p.end());
         uint64_t seed = 0;
         for (uint64_t v : p)
@@ -572,7 +577,11 @@ static void processLevel(const std::vector<TNode>& nodes, std::vector<Tagged>& m
     }
 }
 
-static HierResult constructHierarchical(const Structure32& in, uint32_t midLevel, const Config& cfg)
+// staticOffsets: the StaticStructure variant (constructStaticTransformDAGHierarchical,
+// transform_dag_hierarchical.cpp:531-743). It makes the same decisions, but a child pointer's value is
+// the word offset of the child in its packed level (header + one word per child), so the grouping hash,
+// and with it the emission order, differs from levels 4 up.
+static HierResult constructHierarchical(const Structure32& in, uint32_t midLevel, const Config& cfg, bool staticOffsets = false)
 {
     HierResult res;
     StructureTP& out = res.out;
@@ -609,6 +618,7 @@ static HierResult constructHierarchical(const Structure32& in, uint32_t midLevel
             storeMid(out.leaves.size(), mapping);
     }
     out.nodes.resize(in.nodes.size());
+    std::vector<uint64_t> prevOffsets; // word offsets of the previous level's emitted nodes (static variant)
     for (uint32_t level = 3; level <= in.rootLevel; ++level) {
         const auto& inNodes = in.nodes[level];
         std::vector<TNode> nodes(inNodes.size());
@@ -618,7 +628,7 @@ static HierResult constructHierarchical(const Structure32& in, uint32_t midLevel
                 nodes[i].c[k] = (inNodes[i][k] == kEmpty32) ? taggedSentinel() : mapping[inNodes[i][k]];
         std::vector<uint32_t> emitted;
         std::vector<Tagged> newMapping;
-        processLevel(nodes, newMapping, emitted, cfg);
+        processLevel(nodes, newMapping, emitted, cfg, (staticOffsets && level >= 4) ? &prevOffsets : nullptr);
         auto& outNodes = out.nodes[level];
         outNodes.resize(emitted.size());
         for (size_t i = 0; i < emitted.size(); ++i)
@@ -626,6 +636,16 @@ static HierResult constructHierarchical(const Structure32& in, uint32_t midLevel
                 const Tagged& c = nodes[emitted[i]].c[k];
                 outNodes[i][k] = tp::createT(c.ptr, c.t);
             }
+        if (staticOffsets) {
+            prevOffsets.assign(outNodes.size(), 0);
+            uint64_t off = 0;
+            for (size_t i = 0; i < outNodes.size(); ++i) {
+                prevOffsets[i] = off;
+                off += 1;
+                for (uint64_t c : outNodes[i])
+                    off += c != tp::sentinel() ? 1 : 0;
+            }
+        }
         mapping = std::move(newMapping);
         if (level == midLevel)
             storeMid(outNodes.size(), mapping);
@@ -978,11 +998,13 @@ static void translationLevel(const Structure32& in, StructureTP& out, const Conf
 }
 
 // A6: constructTransformDAG (transform_dag.cpp:138-240).
-static StructureTP constructTransformDAG(const Structure32& in, const Config& cfg, MatchStats& st, std::vector<uint64_t>* levelTimes = nullptr)
+static StructureTP constructTransformDAG(const Structure32& in, const Config& cfg, MatchStats& st, std::vector<uint64_t>* levelTimes = nullptr,
+    bool staticOffsets = false)
 {
-    check(in.structureType == 1, "input structure must be a DAG");
+    if (!staticOffsets) // the static variant does not check (transform_dag.cpp:244)
+        check(in.structureType == 1, "input structure must be a DAG");
     const double t0 = omp_get_wtime();
-    HierResult h = constructHierarchical(in, cfg.maxTranslationLevel + 1, cfg);
+    HierResult h = constructHierarchical(in, cfg.maxTranslationLevel + 1, cfg, staticOffsets);
     const double t1 = omp_get_wtime();
     if (levelTimes)
         levelTimes->push_back((uint64_t)((t1 - t0) * 1e9));
@@ -1052,6 +1074,126 @@ static bool tdagGet(const StructureTP& s, uint32_t x, uint32_t y, uint32_t z)
             v[k] = u[k] % half;
         ptr = child;
     }
+}
+
+// ------------------------------------------------------------------------------------------------
+// StaticStructure (structure.h:298-320, 765-798, 859-895): per level a packed word stream, each node a
+// header word (child mask, bit i = child i) followed by one word per present child in child order;
+// child words are word offsets into the level below (level 3: leaf indices). Words are uint32_t for
+// EditNode<uint32_t> inputs and the 64-bit TransformPointer for transform DAGs.
+// ------------------------------------------------------------------------------------------------
+template <typename W>
+struct StaticS {
+    std::vector<std::vector<W>> words;
+    std::vector<uint64_t> leaves;
+    uint32_t resolution = 0, rootLevel = 0, structureType = 0;
+};
+template <typename W, typename C>
+static StaticS<W> toStatic(const Structure<C>& s, C empty) // StaticStructure(const EditStructure&) (:765-798)
+{
+    StaticS<W> out;
+    out.resolution = s.resolution;
+    out.rootLevel = s.rootLevel;
+    out.structureType = s.structureType;
+    out.leaves = s.leaves;
+    out.words.resize(s.nodes.size());
+    std::vector<uint64_t> prev(s.leaves.size());
+    std::iota(prev.begin(), prev.end(), 0ull);
+    for (uint32_t level = 3; level <= s.rootLevel; ++level) {
+        std::vector<uint64_t> cur(s.nodes[level].size());
+        auto& w = out.words[level];
+        for (size_t i = 0; i < s.nodes[level].size(); ++i) {
+            cur[i] = w.size();
+            const size_t head = w.size();
+            w.push_back(0);
+            for (uint32_t k = 0; k < 8; ++k) {
+                const C c = s.nodes[level][i][k];
+                if (c == empty)
+                    continue;
+                if constexpr (sizeof(C) == 8)
+                    w.push_back((W)((c & ~tp::kPtrMask) | (prev[tp::ptr(c)] & tp::kPtrMask)));
+                else
+                    w.push_back((W)prev[c]);
+                w[head] |= (W)1 << k;
+            }
+        }
+        prev = std::move(cur);
+    }
+    return out;
+}
+// The inverse: node starts by a sequential walk (getLevelNodeStarts, :859-876), offsets -> indices.
+template <typename W, typename C>
+static Structure<C> fromStatic(const StaticS<W>& s, C empty)
+{
+    Structure<C> out;
+    out.resolution = s.resolution;
+    out.rootLevel = s.rootLevel;
+    out.structureType = s.structureType;
+    out.leaves = s.leaves;
+    out.nodes.resize(s.words.size());
+    std::unordered_map<uint64_t, uint64_t> prev; // child word offset -> index (level 3: identity)
+    for (uint32_t level = 3; level <= s.rootLevel; ++level) {
+        const auto& w = s.words[level];
+        std::unordered_map<uint64_t, uint64_t> cur;
+        for (size_t at = 0; at < w.size();) {
+            const uint32_t mask = (uint32_t)w[at] & 0xFF;
+            check(((uint64_t)w[at] >> 8) == 0 || sizeof(W) == 8, "static header word has bits above the child mask");
+            cur[at] = out.nodes[level].size();
+            std::array<C, 8> node;
+            node.fill(empty);
+            size_t c = at + 1;
+            for (uint32_t k = 0; k < 8; ++k) {
+                if (!((mask >> k) & 1))
+                    continue;
+                check(c < w.size(), "static node runs past its level");
+                const uint64_t v = w[c++];
+                const uint64_t off = sizeof(C) == 8 ? tp::ptr(v) : v;
+                uint64_t idx = off;
+                if (level > 3) {
+                    auto it = prev.find(off);
+                    check(it != prev.end(), "static child pointer is not a node start");
+                    idx = it->second;
+                } else {
+                    check(idx < s.leaves.size(), "static leaf pointer out of range");
+                }
+                if constexpr (sizeof(C) == 8)
+                    node[k] = (C)((v & ~tp::kPtrMask) | (idx & tp::kPtrMask));
+                else
+                    node[k] = (C)idx;
+            }
+            out.nodes[level].push_back(node);
+            at = c;
+        }
+        prev = std::move(cur);
+    }
+    return out;
+}
+template <typename W>
+static void writeStatic(Writer& wr, const StaticS<W>& s) // StaticStructure::writeTo (:888-895)
+{
+    wr.pod<uint64_t>(s.words.size());
+    for (const auto& l : s.words)
+        wr.vec(l);
+    wr.vec(s.leaves);
+    wr.pod(s.resolution);
+    wr.pod(s.rootLevel);
+    wr.pod(s.structureType);
+}
+template <typename W>
+static StaticS<W> readStatic(Reader& r)
+{
+    StaticS<W> s;
+    const uint64_t nl = r.pod<uint64_t>();
+    check(nl >= 4 && nl <= 32, "corrupt static level count");
+    s.words.resize(nl);
+    for (auto& l : s.words)
+        l = r.vec<W>();
+    s.leaves = r.vec<uint64_t>();
+    s.resolution = r.pod<uint32_t>();
+    s.rootLevel = r.pod<uint32_t>();
+    s.structureType = r.pod<uint32_t>();
+    check(s.rootLevel + 1 == nl, "rootLevel does not match level count");
+    return s;
 }
 
 } // namespace orc
@@ -1224,6 +1366,58 @@ int orc_tdag_decode(const uint8_t* tdag, uint64_t len, uint8_t* dense, uint32_t 
     try {
         orc::Reader r { tdag, len };
         auto s = orc::readStructure<uint64_t>(r);
+        orc::check(s.resolution == res, "resolution mismatch");
+#pragma omp parallel for schedule(static)
+        for (int64_t z = 0; z < (int64_t)res; ++z)
+            for (uint32_t y = 0; y < res; ++y)
+                for (uint32_t x = 0; x < res; ++x)
+                    dense[(size_t)x + (size_t)res * y + (size_t)res * res * z] = orc::tdagGet(s, x, y, (uint32_t)z) ? 1 : 0;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// .svo (EditStructure<void, uint32_t>) -> StaticStructure<void, uint32_t>::writeTo bytes.
+int orc_to_static(const uint8_t* svo, uint64_t len, uint8_t** out, uint64_t* outLen)
+{
+    try {
+        const auto s = readSvo(svo, len);
+        orc::Writer w;
+        orc::writeStatic(w, orc::toStatic<uint32_t, uint32_t>(s, orc::kEmpty32));
+        *out = dupBuf(w.buf, outLen);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// constructStaticTransformDAG (transform_dag.cpp:242-390) on StaticStructure<void, uint32_t> bytes:
+// the same construction as orc_construct_tdag with the static variant's grouping hash, returned as
+// StaticStructure<void, TransformPointer>::writeTo bytes.
+int orc_construct_static_tdag(const uint8_t* in, uint64_t len, int sym, int axis, int trans, uint32_t maxL, uint8_t** out, uint64_t* outLen)
+{
+    try {
+        orc::Reader r { in, len };
+        const auto st32 = orc::readStatic<uint32_t>(r);
+        const auto edit = orc::fromStatic<uint32_t, uint32_t>(st32, orc::kEmpty32);
+        orc::MatchStats ms;
+        const auto res = orc::constructTransformDAG(edit, mkCfg(sym, axis, trans, maxL), ms, nullptr, true);
+        orc::Writer w;
+        orc::writeStatic(w, orc::toStatic<uint64_t, uint64_t>(res, orc::tp::sentinel()));
+        *out = dupBuf(w.buf, outLen);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// Every voxel of a StaticStructure<void, TransformPointer> (dense[x + res*y + res*res*z]).
+int orc_static_tdag_decode(const uint8_t* in, uint64_t len, uint8_t* dense, uint32_t res)
+{
+    try {
+        orc::Reader r { in, len };
+        const auto s = orc::fromStatic<uint64_t, uint64_t>(orc::readStatic<uint64_t>(r), orc::tp::sentinel());
         orc::check(s.resolution == res, "resolution mismatch");
 #pragma omp parallel for schedule(static)
         for (int64_t z = 0; z < (int64_t)res; ++z)
