@@ -1388,7 +1388,16 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
     while ((1ull << log2Cap) < cap)
         ++log2Cap;
     t.homeShift = 64 - log2Cap;
-    const uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key ? ctx.tuning.filter_bits_per_key : 32u;
+    // Filter density: 32 bits per key unless the filter would then exceed 64 MB; past that it no longer
+    // stays in L2 (126 MB over two dies, shared with the batch's grids and records), every probe
+    // becomes a DRAM access, and halving the density (down to 8 bits per key) costs less in extra
+    // false-positive lookups than it saves (8192^3 grid: 337 -> 273 ms per build).
+    uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key;
+    if (!bitsPerKey) {
+        bitsPerKey = 32;
+        while (bitsPerKey > 8 && pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey)) > (1ull << 29))
+            bitsPerKey /= 2;
+    }
     const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey));
     uint32_t log2F = 0;
     while ((1ull << log2F) < filterBits)
