@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--resolution", type=int, default=2048)
     ap.add_argument("--primitives", type=int, default=4000)
+    ap.add_argument("--scene", default="primitives", choices=["primitives", "terrain"],
+                    help="primitives: the primitive-union shell (configs 1, 3, 4); terrain: solid fBm terrain (config 0, 256^3)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -111,7 +113,7 @@ def run_proposal(args, world, rank, local, pg):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del sets
-    spec = tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+    spec = scene_spec(args)
     g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
     voxels = g.voxel_count
 
@@ -222,13 +224,24 @@ def run_batch(args, world, rank, local, pg):
         print(json.dumps(out), flush=True)
 
 
+def scene_spec(args):
+    import tdag
+    if getattr(args, "scene", "primitives") == "terrain":
+        return tdag.SceneSpec(kind=tdag.SCENE_TERRAIN, resolution=args.resolution, seed=args.seed, shell=False)
+    return tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+
+
 def workload_config(args, voxels=None):
+    if getattr(args, "scene", "primitives") == "terrain":
+        what = f"{args.resolution}^3 solid fBm terrain (5 octaves, base frequency 1/64, seed {args.seed})"
+    else:
+        what = (f"{args.resolution}^3 primitive-union shell ({args.primitives} primitives, 30% transformed copies, "
+                f"seed {args.seed})")
     cfg = {
-        "workload": f"single-grid exhaustive TDAG build, {args.resolution}^3 primitive-union shell "
-                    f"({args.primitives} primitives, 30% transformed copies, seed {args.seed}), "
-                    f"symmetry+axis permutation+translation, maxTranslationLevel 4",
+        "workload": f"single-grid exhaustive TDAG build, {what}, symmetry+axis permutation+translation, maxTranslationLevel 4",
         "resolution": args.resolution,
-        "primitives": args.primitives,
+        "scene": getattr(args, "scene", "primitives"),
+        "primitives": args.primitives if getattr(args, "scene", "primitives") == "primitives" else 0,
         "seed": args.seed,
         "l2": "flushed between timed steps (256 MiB device write)",
     }
@@ -464,16 +477,18 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(level: int):
-    """DRAM bytes (read + write) of the level's probe launches from an ncu capture, if recorded."""
+def load_traffic(level: int, args):
+    """DRAM bytes (read + write) of the level's probe launches in one build of this workload, from an
+    ncu capture of the same workload if one is recorded (else None)."""
     p = os.path.join(REPO, "profiles", "probe_traffic.json")
     if not os.path.exists(p):
         return None
+    key = f"{getattr(args, 'scene', 'primitives')}/{args.resolution}/{args.primitives}/{args.seed}"
     try:
         with open(p) as f:
             d = json.load(f)
-        return d.get(str(level))
-    except (OSError, ValueError):
+        return d.get("workloads", {}).get(key, {}).get(str(level))
+    except (OSError, ValueError, AttributeError):
         return None
 
 
@@ -486,7 +501,7 @@ def run_reference(args, world, rank, pg):
         return
     import tdag
     ctx = tdag.default_context()
-    spec = tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+    spec = scene_spec(args)
     g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
     host = g.to_host()
     g.free()
@@ -523,7 +538,7 @@ def run_ours(args, world, rank, local, pg):
     dev = local if torch.cuda.is_available() else 0
     torch.cuda.set_device(dev)
     ctx = tdag.Context(dev)
-    spec = tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
+    spec = scene_spec(args)
     g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
     voxels = g.voxel_count
     cfg = tdag.TransformDAGConfig()
@@ -660,7 +675,7 @@ def run_ours(args, world, rank, local, pg):
     build_s = dev_ms / args.steps / 1e3
     roof = {"bound": "hbm", "kernel": f"probeKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-            "traffic": load_traffic(dom), "algorithmic_bytes": alg, "device_ms": ms,
+            "traffic": load_traffic(dom, args), "algorithmic_bytes": alg, "device_ms": ms,
             "model": "survey algorithmic bytes of the search: M*G + P*16 (M source items, G grid bytes, P non-empty probes)",
             "dram_only": {"algorithmic_bytes": dram_alg, "achieved": dram_alg / (ms / 1e3) / 1e9 if ms > 0 else None,
                           "note": "grids in + line orientations and survivor records out; the filter stays in L2"},
