@@ -619,6 +619,47 @@ int tdag_ctx_stream(tdag_ctx* ctx, void** out)
 } // extern "C"
 
 namespace tdag {
+void requireDeviceAccessible(Context& c, const void* p, const char* what)
+{
+    if (!p)
+        return;
+    cudaPointerAttributes a {};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(TDAG_ERR_ARG, std::string(what) + ": not a pointer the device can use");
+    }
+    bool ok = false;
+    switch (a.type) {
+    case cudaMemoryTypeDevice:
+        ok = a.device == c.device;
+        break;
+    case cudaMemoryTypeManaged:
+        ok = true;
+        break;
+    case cudaMemoryTypeHost:
+        ok = a.devicePointer == p;
+        break;
+    default: // unregistered (pageable) host memory
+        if (c.pageableAccess < 0) {
+            int v = 0;
+            TDAG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, c.device));
+            c.pageableAccess = v;
+        }
+        ok = c.pageableAccess == 1;
+        break;
+    }
+    TDAG_CHECK(ok, TDAG_ERR_ARG, std::string(what) + ": expected memory the context's device can read (a device pointer)");
+}
+
+void requireDeviceView(Context& c, const tdag_svdag_view& v)
+{
+    for (uint32_t l = 3; l <= v.root_level && l < TDAG_MAX_LEVELS; ++l)
+        if (v.node_counts[l])
+            requireDeviceAccessible(c, v.nodes[l], "tdag_svdag_view.nodes");
+    if (v.leaf_count)
+        requireDeviceAccessible(c, v.leaves, "tdag_svdag_view.leaves");
+}
+
 // Copies device arrays into host (pageable) arrays through the context's pinned staging buffer. A
 // D2H copy into pinned memory runs at link speed; one straight into freshly allocated pageable pages
 // goes page by page through the driver and took ~20 ms for a 32 MB result. The host copies out of
@@ -685,6 +726,7 @@ int tdag_build_device(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_confi
         checkView(in);
         Context& c = ctx->c;
         TDAG_CUDA(cudaSetDevice(c.device));
+        requireDeviceView(c, *in);
         std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, true));
         DeviceResult dr = buildDevice(c, viewToDevice(in), *cfg, &r->stats);
         // hand ownership of the device buffers to the result (freed by tdag_result_free)
@@ -710,6 +752,7 @@ int tdag_build_device_proposed(tdag_ctx* ctx, const tdag_svdag_view* in, const t
         checkView(in);
         Context& c = ctx->c;
         TDAG_CUDA(cudaSetDevice(c.device));
+        requireDeviceView(c, *in);
         std::unique_ptr<tdag_result> r(newResult(in->resolution, in->root_level, true));
         DeviceResult dr = buildDevice(c, viewToDevice(in), *cfg, &r->stats, ProposalHook { fn, user });
         TDAG_CUDA(cudaStreamSynchronize(c.stream));
@@ -796,6 +839,9 @@ static int buildBatched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count
         Context& c = ctx->c;
         cudaStream_t s = c.stream;
         TDAG_CUDA(cudaSetDevice(c.device));
+        if (!host)
+            for (uint32_t g = 0; g < count; ++g)
+                requireDeviceView(c, in[g]);
         BatchInput b;
         concatBatch(c, in, count, host, b);
         tdag_stats st;
@@ -947,8 +993,11 @@ int tdag_device_copy(tdag_ctx* ctx, void* d_dst, const void* d_src, uint64_t byt
     return guarded([&] {
         Context& c = ctx->c;
         TDAG_CUDA(cudaSetDevice(c.device));
-        if (bytes)
+        if (bytes) {
+            requireDeviceAccessible(c, d_dst, "d_dst");
+            requireDeviceAccessible(c, d_src, "d_src");
             TDAG_CUDA(cudaMemcpyAsync(d_dst, d_src, bytes, cudaMemcpyDeviceToDevice, c.stream));
+        }
         TDAG_CUDA(cudaStreamSynchronize(c.stream));
     });
 }
@@ -963,6 +1012,13 @@ int tdag_find_duplicates_level_device(tdag_ctx* ctx, uint32_t level, const uint6
         Context& c = ctx->c;
         cudaStream_t s = c.stream;
         TDAG_CUDA(cudaSetDevice(c.device));
+        if (n) {
+            requireDeviceAccessible(c, d_grids, "d_grids");
+            requireDeviceAccessible(c, d_out_mapping, "d_out_mapping");
+            requireDeviceAccessible(c, d_out_unique, "d_out_unique");
+        }
+        if (num_sources)
+            requireDeviceAccessible(c, d_sources, "d_sources");
         tdag_level_stats ls {};
         MatchOutput mo = runMatcher(c, level, d_grids, n, *cfg, &ls, nullptr, d_sources, d_sources ? num_sources : 0);
         if (n) {

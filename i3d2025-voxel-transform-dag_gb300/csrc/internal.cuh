@@ -19,6 +19,7 @@ struct Context {
     cudaEvent_t ev[8] {};
     void* stage = nullptr; // pinned staging buffer of host-bound results (grown on demand)
     size_t stageBytes = 0;
+    int pageableAccess = -1; // cudaDevAttrPageableMemoryAccess of the device (-1: not queried yet)
 
     // Synchronise the stream, read the device status word, throw on a recorded error.
     void checkStatus(const std::string& where);
@@ -94,6 +95,12 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
 // a target and its own candidate, but only the listed items probe (the learned-proposal mode).
 MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats,
     const Segments* seg = nullptr, const uint32_t* sources = nullptr, uint32_t numSources = 0);
+
+// Throws TDAG_ERR_ARG unless the context's device can dereference p: device memory of that device,
+// managed memory, mapped pinned host memory, or pageable host memory on systems where the GPU reads
+// it directly (cudaDevAttrPageableMemoryAccess). Null passes (callers check counts). (build.cu)
+void requireDeviceAccessible(Context& c, const void* p, const char* what);
+void requireDeviceView(Context& c, const tdag_svdag_view& v);
 
 // Device -> host copies of several arrays through the context's pinned staging buffer; complete on
 // return (build.cu).

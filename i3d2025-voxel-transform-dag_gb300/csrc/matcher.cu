@@ -2067,6 +2067,12 @@ extern "C" int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level,
         TDAG_CHECK(n <= kNoAllocMaxItems, TDAG_ERR_ARG, "tdag_find_duplicates_level_noalloc accepts at most 4096 items per call");
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
+        requireDeviceAccessible(c, d_n_unique, "d_n_unique");
+        if (n) {
+            requireDeviceAccessible(c, d_grids, "d_grids");
+            requireDeviceAccessible(c, d_out_mapping, "d_out_mapping");
+            requireDeviceAccessible(c, d_out_unique, "d_out_unique");
+        }
         if (n == 0) {
             TDAG_CUDA(cudaMemsetAsync(d_n_unique, 0, 4, c.stream));
             TDAG_CUDA(cudaStreamSynchronize(c.stream));

@@ -742,6 +742,10 @@ extern "C" int tdag16_get(tdag_ctx* ctx, const tdag16_device* dev, const uint32_
     return guardedCall([&] {
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
+        if (n) {
+            requireDeviceAccessible(c, d_xyz, "d_xyz");
+            requireDeviceAccessible(c, d_out, "d_out");
+        }
         tdag16Get(c, *dev->h, d_xyz, n, d_out);
     });
 }
@@ -754,6 +758,10 @@ extern "C" int tdag16_raycast(tdag_ctx* ctx, const tdag16_device* dev, const tda
     return guardedCall([&] {
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
+        if (n) {
+            requireDeviceAccessible(c, d_rays, "d_rays");
+            requireDeviceAccessible(c, d_hits, "d_hits");
+        }
         tdag16Raycast(c, *dev->h, d_rays, n, d_hits);
     });
 }
@@ -766,6 +774,7 @@ extern "C" int tdag16_verify(tdag_ctx* ctx, const tdag16_device* dev, const tdag
     return guardedCall([&] {
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
+        requireDeviceView(c, *source_device);
         *out = tdag16_verify_stats {};
         tdag16Verify(c, *dev->h, *source_device, *out);
     });

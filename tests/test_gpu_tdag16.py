@@ -169,3 +169,20 @@ def test_raycast_matches_oracle_dda(oracle, tdaglib, gpu_ctx, maker, pt, hf):
     assert np.allclose(t_got, t_ref, rtol=0, atol=1e-3)
     assert 0.2 < h_ref.mean() < 0.95  # both hits and misses are exercised
     assert all(dense[z, y, x] for x, y, z in v_got[h_got == 1])
+
+
+def test_device_entry_points_check_their_pointers(oracle, tdaglib, gpu_ctx):
+    """tdag16_get with host (numpy) arrays: refused with TDAG_ERR_ARG where the GPU cannot read
+    pageable memory, answered correctly where it can (cudaDevAttrPageableMemoryAccess, e.g. Grace)."""
+    import ctypes
+    dense = blocky_grid(64, 3)
+    t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense))
+    data, _ = oracle.encode_tdag16(t)
+    dev = tdaglib.Tdag16Device(data, ctx=gpu_ctx)
+    xyz = np.array([[1, 2, 3], [40, 41, 42], [63, 0, 17]], np.uint32)
+    out = np.full(3, 7, np.uint8)
+    rc = tdaglib.lib().tdag16_get(gpu_ctx.handle, dev._h, ctypes.c_void_p(xyz.ctypes.data), 3, ctypes.c_void_p(out.ctypes.data))
+    if rc == 0:
+        assert list(out) == [int(dense[z, y, x]) for x, y, z in xyz]
+    else:
+        assert rc == 1 and b"device" in tdaglib.lib().tdag_last_error_message()
