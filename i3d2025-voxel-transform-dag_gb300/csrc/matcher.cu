@@ -509,6 +509,22 @@ __global__ void entryLiveKernel(const uint32_t* __restrict__ pays, size_t m, con
         flags[e] = live[pays[e] >> 6];
 }
 
+// Membership filter over the keys of the flagged entries only: a pruning round that keeps the table
+// refreshes just the filter. A key is inserted by the first flagged entry of each flagged stretch
+// (repeats are harmless: insertion is idempotent).
+__global__ void liveFilterKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ flags, size_t m, uint32_t* __restrict__ filter,
+    uint32_t filterShift)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m || !flags[e])
+        return;
+    const uint64_t k = keys[e];
+    if (e > 0 && flags[e - 1] && keys[e - 1] == k)
+        return;
+    const uint32_t x = filterFold(k);
+    atomicOr(&filter[filterWordIndex(x, filterShift)], filterBits(x));
+}
+
 // Stable compaction of the flagged entries to their exclusive-scan offsets (keeps the key order).
 __global__ void compactEntriesKernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pays, const uint32_t* __restrict__ flags,
     const uint32_t* __restrict__ offs, size_t m, uint64_t* __restrict__ keysOut, uint32_t* __restrict__ paysOut)
@@ -1623,12 +1639,23 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             const uint64_t live = exclusiveScanU32Total(flags.get(), liveIdx.get(), mCur, s);
             if (live == 0)
                 break;
-            compactEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, flags.get(), liveIdx.get(), mCur, spareKeys, sparePays);
-            TDAG_LAUNCHED();
-            std::swap(curKeys, spareKeys);
-            std::swap(curPays, sparePays);
-            mCur = live;
-            buildRunTable(ctx, curKeys, curPays, mCur, table);
+            if (2 * live >= mCur && mCur <= (1ull << 25)) {
+                // Most entries live in a table of up to 2^25 entries: keep it and refresh only the
+                // filter from the live keys. Dead entries left in a run cost a parent read in the
+                // lookup, where their key (no smaller than minKeyNext) already fails the `key < parent`
+                // test. Larger tables are compacted and rebuilt: there the dead entries' lookup work
+                // outweighs a rebuild (2048^3: 67.7 -> 64.8 ms kept; 16384^3: 874 -> 1000 ms kept).
+                TDAG_CUDA(cudaMemsetAsync(table.filter.get(), 0, table.filter.bytes(), s));
+                liveFilterKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, flags.get(), mCur, table.filter.get(), table.filterShift);
+                TDAG_LAUNCHED();
+            } else {
+                compactEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, flags.get(), liveIdx.get(), mCur, spareKeys, sparePays);
+                TDAG_LAUNCHED();
+                std::swap(curKeys, spareKeys);
+                std::swap(curPays, sparePays);
+                mCur = live;
+                buildRunTable(ctx, curKeys, curPays, mCur, table);
+            }
         }
         ProbeParams pp {};
         pp.grids = grids;
