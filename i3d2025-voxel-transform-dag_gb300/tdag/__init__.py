@@ -543,9 +543,14 @@ def construct_transform_dag16(dag, dag_config: TransformDAGConfig = TransformDAG
     """constructTransformDAG16(EditStructure<void, TransformPointer>, dagConfig, encodingConfig, stats)
     (tools/svdag_encoding/src/transform_dag_encoding.cpp:240-497) followed by TransformDAG16::writeTo:
     returns the .tdag16 file bytes (and, with return_stats, the per-level DAGEncodingStats).
-    ``dag`` is a host EditStructure of TransformPointers or a DeviceResult."""
+    ``dag`` is a host EditStructure of TransformPointers, a DeviceResult, or a StaticStructure of
+    TransformPointers (constructTransformDAG16(StaticStructure<void, TransformPointer>, ...),
+    transform_dag_encoding.cpp:519-697, which makes the same decisions on the unpacked structure; only
+    its statistics are indexed by child level there)."""
     ctx = ctx or default_context()
     keep = []
+    if isinstance(dag, StaticStructure):
+        dag = dag.to_edit()
     if isinstance(dag, DeviceResult):
         rp_in = dag._rp
     else:
@@ -680,6 +685,40 @@ class StaticStructure:
             words[lvl] = w
             prev = starts
         return cls(words, np.asarray(e.sub_grids, np.uint64).copy(), e.resolution, e.root_level, e.structure_type, e.child_type)
+
+    def to_edit(self) -> EditStructure:
+        """The same structure with fixed 8-child nodes: node starts by a sequential walk of each level
+        (getLevelNodeStarts, structure.h:859-876), child word offsets turned into node indices."""
+        is_tp = self.child_type == "transform"
+        dt = np.uint64 if is_tp else np.uint32
+        empty = tp_create(0xFFFFFFFF) if is_tp else 0xFFFFFFFF
+        ptr_mask = (1 << 37) - 1
+        levels = [np.zeros((0, 8), dt) for _ in range(len(self.words))]
+        prev_index = None  # word offset -> node index of the level below (level 3: leaf indices)
+        for lvl in range(3, self.root_level + 1):
+            w = [int(v) for v in np.asarray(self.words[lvl])]
+            nodes, index, at = [], {}, 0
+            while at < len(w):
+                mask = w[at] & 0xFF
+                index[at] = len(nodes)
+                row, c = [empty] * 8, at + 1
+                for k in range(8):
+                    if (mask >> k) & 1:
+                        if c >= len(w):
+                            raise TDagError(_abi.TDAG_ERR_CORRUPT, "static node runs past its level")
+                        v = w[c]
+                        off = (v & ptr_mask) if is_tp else v
+                        idx = off if lvl == 3 else prev_index.get(off)
+                        if idx is None:
+                            raise TDagError(_abi.TDAG_ERR_CORRUPT, "static child pointer is not a node start")
+                        row[k] = ((v & ~ptr_mask) | idx) if is_tp else idx
+                        c += 1
+                nodes.append(row)
+                at = c
+            levels[lvl] = np.array(nodes, dtype=dt).reshape(-1, 8)
+            prev_index = index
+        return EditStructure(levels, np.asarray(self.sub_grids, np.uint64).copy(), self.resolution, self.root_level,
+                             self.structure_type, self.child_type)
 
     def to_bytes(self) -> bytes:
         """StaticStructure::writeTo (structure.h:887-895)."""

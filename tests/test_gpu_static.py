@@ -35,3 +35,17 @@ def test_static_build_rejects_unreferenced_words(tdaglib, gpu_ctx, oracle):
     with pytest.raises(tdaglib.TDagError) as e:
         tdaglib.construct_static_transform_dag(st, ctx=gpu_ctx)
     assert e.value.code == 6
+
+
+def test_static_tdag_encodes_to_tdag16(oracle, tdaglib, gpu_ctx):
+    """constructTransformDAG16 of a static transform DAG: the encoder on the unpacked structure, equal
+    to the oracle's encoding of it and lossless."""
+    dense = blocky_grid(128, 9)
+    st_bytes = oracle.construct_static_tdag(oracle.to_static(dag_svo_bytes(oracle, dense)))
+    st = tdaglib.StaticStructure.from_bytes(st_bytes, "transform")
+    cfg = tdaglib.TransformDAGConfig()
+    for pt, hf in [(False, False), (True, True)]:
+        got = tdaglib.construct_transform_dag16(st, cfg, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx)
+        want, _ = oracle.encode_tdag16(tdaglib.write_tdag(st.to_edit(), cfg), pointer_tables=pt, huffman=hf)
+        assert got == want
+        assert np.array_equal(oracle.decode_tdag16(got, 128), dense)

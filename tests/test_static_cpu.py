@@ -39,3 +39,16 @@ def test_static_tdag_is_lossless_and_agrees_below_the_boundary(oracle, name, mak
         assert got.words[l].shape == packed_edit.words[l].shape
         if l <= top:
             assert np.array_equal(got.words[l], packed_edit.words[l]), l
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_static_unpacks_to_the_same_structure(oracle, name, make):
+    """StaticStructure -> EditStructure: the inverse of the packing, for u32 inputs and for the static
+    transform DAG (which then equals the oracle's own unpacking, byte for byte)."""
+    import tdag
+    svo = dag_svo_bytes(oracle, make())
+    edit = tdag.EditStructure.from_svo_bytes(svo)
+    back = tdag.StaticStructure.from_bytes(oracle.to_static(svo)).to_edit()
+    assert back.to_bytes() == edit.to_bytes()
+    st = tdag.StaticStructure.from_bytes(oracle.construct_static_tdag(oracle.to_static(svo)), "transform")
+    assert tdag.StaticStructure.from_edit(st.to_edit()).to_bytes() == st.to_bytes()
