@@ -320,6 +320,101 @@ __global__ void __launch_bounds__(kSortThreads) radixScatterKernel(const uint64_
         valsOut[out] = sv[i];
     }
 }
+// The whole sort of at most one tile (n <= 4096) in one block: every pass ranks the items exactly
+// as radixScatterKernel does (warp-major, then round, then lane: stable) and moves them between two
+// shared-memory buffers; one launch replaces three per pass for the small upper-level arrays.
+constexpr size_t kSmallSortSmem = (size_t)kSortTile * (8 + 4) * 2 + (size_t)kSortWarps * 256 * 4;
+
+__global__ void __launch_bounds__(kSortThreads) radixSortSmallKernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t n,
+    uint32_t beginBit, uint32_t endBit)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t* const k0 = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* const k1 = k0 + kSortTile;
+    uint32_t* const v0 = reinterpret_cast<uint32_t*>(k1 + kSortTile);
+    uint32_t* const v1 = v0 + kSortTile;
+    uint32_t (*warpBase)[256] = reinterpret_cast<uint32_t (*)[256]>(v1 + kSortTile);
+    __shared__ uint32_t warpTotals[kSortWarps];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t ltMask = (1u << lane) - 1u;
+    for (uint32_t i = threadIdx.x; i < n; i += kSortThreads) {
+        k0[i] = keys[i];
+        v0[i] = vals[i];
+    }
+    int cur = 0;
+    for (uint32_t shift = beginBit; shift < endBit; shift += 8) {
+        const uint64_t* const kin = cur ? k1 : k0;
+        const uint32_t* const vin = cur ? v1 : v0;
+        uint64_t* const kout = cur ? k0 : k1;
+        uint32_t* const vout = cur ? v0 : v1;
+        for (int d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads)
+            (&warpBase[0][0])[d] = 0;
+        __syncthreads();
+        const uint32_t warpItems = warp * (32 * kSortRounds);
+        for (int r = 0; r < kSortRounds; ++r) {
+            const uint32_t i = warpItems + r * 32 + lane;
+            const bool valid = i < n;
+            const uint32_t digit = valid ? (uint32_t)(kin[i] >> shift) & 0xFF : 256u;
+            const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+            if (valid && (peers & ltMask) == 0)
+                warpBase[warp][digit] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        {
+            const uint32_t d = threadIdx.x; // 256 threads == 256 digits
+            uint32_t cnt = 0;
+            for (int w = 0; w < kSortWarps; ++w)
+                cnt += warpBase[w][d];
+            uint32_t incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o)
+                    incl += t;
+            }
+            if (lane == 31)
+                warpTotals[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w)
+                before += warpTotals[w];
+            uint32_t run = before + incl - cnt;
+            for (int w = 0; w < kSortWarps; ++w) {
+                const uint32_t c = warpBase[w][d];
+                warpBase[w][d] = run;
+                run += c;
+            }
+        }
+        __syncthreads();
+        for (int r = 0; r < kSortRounds; ++r) {
+            const uint32_t i = warpItems + r * 32 + lane;
+            const bool valid = i < n;
+            const uint32_t digit = valid ? (uint32_t)(kin[i] >> shift) & 0xFF : 256u;
+            const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+            uint32_t pos = 0;
+            if (valid)
+                pos = warpBase[warp][digit] + __popc(peers & ltMask);
+            __syncwarp();
+            if (valid && (peers & ltMask) == 0)
+                warpBase[warp][digit] += __popc(peers);
+            __syncwarp();
+            if (valid) {
+                kout[pos] = kin[i];
+                vout[pos] = vin[i];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    const uint64_t* const kfin = cur ? k1 : k0;
+    const uint32_t* const vfin = cur ? v1 : v0;
+    for (uint32_t i = threadIdx.x; i < n; i += kSortThreads) {
+        keys[i] = kfin[i];
+        vals[i] = vfin[i];
+    }
+}
 } // namespace
 
 void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s)
@@ -328,13 +423,19 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
         return;
     TDAG_CHECK(n < (1ull << 32), TDAG_ERR_ARG, "radix sort size exceeds 2^32");
     const uint32_t numTiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
-    static bool smemSet[64] = {}; // the shared-memory limit is set once per device
+    static bool smemSet[64] = {}; // the shared-memory limits are set once per device
     int dev = 0;
     TDAG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64 || !smemSet[dev]) {
         TDAG_CUDA(cudaFuncSetAttribute(radixScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
+        TDAG_CUDA(cudaFuncSetAttribute(radixSortSmallKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSortSmem));
         if (dev >= 0 && dev < 64)
             smemSet[dev] = true;
+    }
+    if (n <= (size_t)kSortTile) {
+        radixSortSmallKernel<<<1, kSortThreads, kSmallSortSmem, s>>>(keys, vals, (uint32_t)n, beginBit, endBit);
+        TDAG_LAUNCHED();
+        return;
     }
     DevBuf<uint64_t> k2(n, s);
     DevBuf<uint32_t> v2(n, s);
