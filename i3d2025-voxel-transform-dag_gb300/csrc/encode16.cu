@@ -77,21 +77,23 @@ std::vector<PointerCode> huffmanCodes(const std::vector<uint64_t>& freq, uint32_
         std::vector<std::vector<Pm>> lv;
     } pm;
     pm.lv.resize(maxCodeLen);
-    auto sortLevel = [&](uint32_t l) {
-        auto& v = pm.lv[l];
-        std::sort(v.begin(), v.end(), pmLess);
-    };
+    // The leaves, sorted once, start every level. The packages of a level pair up consecutive items of
+    // the sorted level below, so they are already in order (non-decreasing sums, increasing positions),
+    // and each level is the merge of the two sorted lists in the same total order.
+    std::vector<Pm> leaves(n);
     for (uint32_t s = 0; s < n; ++s)
-        pm.lv[0].push_back({ freq[s], (int32_t)s, -1, -1 });
-    sortLevel(0);
+        leaves[s] = { freq[s], (int32_t)s, -1, -1 };
+    std::sort(leaves.begin(), leaves.end(), pmLess);
+    pm.lv[0] = leaves;
+    std::vector<Pm> packs;
     for (uint32_t l = 1; l < maxCodeLen; ++l) {
         const auto& below = pm.lv[l - 1];
-        auto& cur = pm.lv[l];
+        packs.clear();
         for (size_t i = 0; i + 1 < below.size(); i += 2)
-            cur.push_back({ below[i].freq + below[i + 1].freq, -1, (int32_t)i, (int32_t)(i + 1) });
-        for (uint32_t s = 0; s < n; ++s)
-            cur.push_back({ freq[s], (int32_t)s, -1, -1 });
-        sortLevel(l);
+            packs.push_back({ below[i].freq + below[i + 1].freq, -1, (int32_t)i, (int32_t)(i + 1) });
+        auto& cur = pm.lv[l];
+        cur.resize(packs.size() + leaves.size());
+        std::merge(leaves.begin(), leaves.end(), packs.begin(), packs.end(), cur.begin(), pmLess);
     }
     std::vector<uint32_t> len(n, 0);
     size_t take = 2 * (size_t)n - 2;
