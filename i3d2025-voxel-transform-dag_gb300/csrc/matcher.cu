@@ -1445,7 +1445,8 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
     t.entries = pays;
     t.numEntries = m;
     t.distinct = runs;
-    ctx.checkStatus("corner-view table");
+    // no device-side error can arise while placing runs; the level's final status check covers the
+    // launches, and the probe can be queued behind the placement without a host round trip
 }
 
 template <int L>
