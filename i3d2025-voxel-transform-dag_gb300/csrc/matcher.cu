@@ -1594,6 +1594,19 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     mark("table");
     const uint64_t entriesInitial = table.numEntries;
     float searchMs = 0, probeMs = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> batchEv;
+    struct EventPairs {
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& v;
+        ~EventPairs()
+        {
+            for (auto& e : v) {
+                if (e.first)
+                    cudaEventDestroy(e.first);
+                if (e.second)
+                    cudaEventDestroy(e.second);
+            }
+        }
+    } batchEvGuard { batchEv };
     DevBuf<uint32_t> flags(m, s), liveIdx(m, s);
     DevBuf<uint64_t> k2(m, s);
     DevBuf<uint32_t> p2(m, s);
@@ -1683,7 +1696,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         lp.allowPerm = cfg.axis_permutation ? 1 : 0;
         lp.allowTrans = cfg.translation ? 1 : 0;
         lp.counters = counters.get();
-        TDAG_CUDA(cudaEventRecord(ctx.ev[0], s));
+        // batch timing events, read once the level has finished (no round trip per batch)
+        batchEv.emplace_back();
+        TDAG_CUDA(cudaEventCreate(&batchEv.back().first));
+        TDAG_CUDA(cudaEventCreate(&batchEv.back().second));
+        TDAG_CUDA(cudaEventRecord(batchEv.back().first, s));
         // Probe ranges of the batch sized so that their records fit; a range whose records overflow
         // the buffer is probed again after the buffer grew to the exact count (or, past the memory
         // limit, as two halves).
@@ -1751,12 +1768,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             }
             pos += cs;
         }
-        TDAG_CUDA(cudaEventRecord(ctx.ev[1], s));
-        TDAG_CUDA(cudaEventSynchronize(ctx.ev[1]));
-        float ms = 0;
-        TDAG_CUDA(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[1]));
-        searchMs += ms;
+        TDAG_CUDA(cudaEventRecord(batchEv.back().second, s));
         if (trace) {
+            TDAG_CUDA(cudaEventSynchronize(batchEv.back().second));
+            float ms = 0;
+            TDAG_CUDA(cudaEventElapsedTime(&ms, batchEv.back().first, batchEv.back().second));
             unsigned long long c[8];
             TDAG_CUDA(cudaMemcpy(c, counters.get(), 64, cudaMemcpyDeviceToHost));
             std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f (probe %.3f lookup %.3f records %llu) | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu\n",
@@ -1789,6 +1805,12 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_LAUNCHED();
     out.uniqueOff = batched ? countPerGrid(gridOf, out.uniques.get(), out.numUnique, numGrids, s) : std::vector<uint64_t> { 0, out.numUnique };
 
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    for (auto& e : batchEv) {
+        float ms = 0;
+        TDAG_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+        searchMs += ms;
+    }
     if (stats) {
         unsigned long long c[8];
         TDAG_CUDA(cudaMemcpyAsync(c, counters.get(), 64, cudaMemcpyDeviceToHost, s));
