@@ -574,36 +574,63 @@ struct SearchShape {
 
 __device__ __forceinline__ int smemStride(int a, int SY, int SZ) { return a == 0 ? 1 : (a == 1 ? SY : SZ); }
 
-// Exact verification: target == translate(mirror(permute(source, P), S), T) (find_translation.cpp:857-862),
-// row by row. lines[a][u_lo + R u_hi] holds the source's voxels along axis a (bit j = coordinate j).
+// One row of the exact verification target == translate(mirror(permute(source, P), S), T)
+// (find_translation.cpp:857-862): the target's row along x at (w1, w2) against the source line that
+// the transform moves there. L = lines[a0]; lines[a][u_lo + R u_hi] holds the source's voxels along
+// axis a (bit j = coordinate j).
+template <int R>
+__device__ __forceinline__ bool verifyRow(const uint64_t* __restrict__ tgrid, const uint16_t* L, int lo, int hi, int a1, uint32_t S, int T0, int T1, int T2, int w1,
+    int w2)
+{
+    constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
+    const uint32_t bitOff = (uint32_t)(R * (w1 + R * w2));
+    const uint32_t trow = (uint32_t)(tgrid[bitOff >> 6] >> (bitOff & 63)) & rowMask;
+    int y1 = w1 - T1, y2 = w2 - T2;
+    uint32_t zrow = 0;
+    if (y1 >= 0 && y1 < R && y2 >= 0 && y2 < R) {
+        if (S & 2)
+            y1 = R - 1 - y1;
+        if (S & 4)
+            y2 = R - 1 - y2;
+        // u[a1] = y1, u[a2] = y2; line index = u[lo] + R u[hi]
+        const int ulo = (lo == a1) ? y1 : y2;
+        const int uhi = (hi == a1) ? y1 : y2;
+        uint32_t line = L[ulo + R * uhi];
+        if (S & 1)
+            line = __brev(line) >> (32 - R);
+        zrow = (T0 >= 0) ? ((line << T0) & rowMask) : (line >> (-T0));
+    }
+    return zrow == trow;
+}
+
+// Exact verification by one thread, row by row.
 template <int R>
 __device__ __noinline__ bool verifyCandidate(const uint64_t* __restrict__ tgrid, const uint16_t* lines, int a0, int a1, int a2, uint32_t S, int T0, int T1, int T2)
 {
-    constexpr uint32_t rowMask = (R == 16) ? 0xFFFFu : ((1u << R) - 1u);
     const uint16_t* L = lines + a0 * R * R;
     const int lo = otherLo(a0), hi = otherHi(a0);
-    for (int w2 = 0; w2 < R; ++w2) {
-        for (int w1 = 0; w1 < R; ++w1) {
-            const uint32_t bitOff = (uint32_t)(R * (w1 + R * w2));
-            const uint32_t trow = (uint32_t)(tgrid[bitOff >> 6] >> (bitOff & 63)) & rowMask;
-            int y1 = w1 - T1, y2 = w2 - T2;
-            uint32_t zrow = 0;
-            if (y1 >= 0 && y1 < R && y2 >= 0 && y2 < R) {
-                if (S & 2)
-                    y1 = R - 1 - y1;
-                if (S & 4)
-                    y2 = R - 1 - y2;
-                // u[a1] = y1, u[a2] = y2; line index = u[lo] + R u[hi]
-                const int ulo = (lo == a1) ? y1 : y2;
-                const int uhi = (hi == a1) ? y1 : y2;
-                uint32_t line = L[ulo + R * uhi];
-                if (S & 1)
-                    line = __brev(line) >> (32 - R);
-                zrow = (T0 >= 0) ? ((line << T0) & rowMask) : (line >> (-T0));
-            }
-            if (zrow != trow)
+    for (int w2 = 0; w2 < R; ++w2)
+        for (int w1 = 0; w1 < R; ++w1)
+            if (!verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, w1, w2))
                 return false;
-        }
+    return true;
+}
+
+// The same verification by a whole warp: lane l checks rows l, l + 32, ... of the R * R rows, 32 rows
+// per step, and the warp stops at the first step with a mismatch. Every lane of the warp calls it with
+// the same arguments.
+template <int R>
+__device__ __noinline__ bool verifyCandidateWarp(const uint64_t* __restrict__ tgrid, const uint16_t* lines, int a0, int a1, uint32_t S, int T0, int T1, int T2,
+    uint32_t lane)
+{
+    constexpr int ROWS = R * R;
+    const uint16_t* L = lines + a0 * R * R;
+    const int lo = otherLo(a0), hi = otherHi(a0);
+    for (int r0 = 0; r0 < ROWS; r0 += 32) {
+        const int r = r0 + (int)lane;
+        const bool ok = r >= ROWS || verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, r % R, r / R);
+        if (!__all_sync(0xffffffffu, ok))
+            return false;
     }
     return true;
 }
@@ -1207,7 +1234,6 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
     // every candidate (target, corner view) of the hit recorded in `m` (find_translation.cpp:820-864)
     struct Src {
         uint32_t rSrc, tLo, tHi, dir;
-        const uint16_t* lines;
         int ux, uy, uz;
     };
     auto source = [&](uint64_t m) {
@@ -1220,7 +1246,6 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         s.rSrc = p.segOff ? r - p.segOff[g] : r;
         s.tLo = p.segOff ? p.segOff[g] : 0u;
         s.tHi = p.segOff ? p.segOff[g + 1] : 0xFFFFFFFFu;
-        s.lines = p.srcLines + (size_t)w * 3 * R * R;
         s.ux = (int)(vidx % R);
         s.uy = (int)((vidx / R) % R);
         s.uz = (int)(vidx / (R * R));
@@ -1230,12 +1255,16 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
     // x, y, z in directions dir. In the reference's terms the source orientation is a = b^-1 (source
     // axis a_i lies along target axis i) with fold directions d_i = dir[a_i], the target corner is
     // c_i = c'[a_i], and S = d ^ c, v_i = u[a_i].
-    auto candidate = [&](uint32_t pay, const Src& s) {
-        const uint32_t tgt = pay >> 6;
+    // Prepares the candidate (target, corner view) `pay` of the hit recorded in `m`; true when it needs
+    // verification, with the target, its key and the transform (a0 | a1 << 2 | S << 4 | T + 32 in
+    // three 6-bit fields from bit 8) in `geo`.
+    auto prepare = [&](uint32_t pay, uint64_t m, uint32_t& tgt, uint64_t& key, uint32_t& geo) -> bool {
+        const Src s = source(m);
+        tgt = pay >> 6;
         const uint32_t pb = (pay >> 3) & 7u, cp = pay & 7u;
         ++cCand;
         if (tgt < s.tLo || tgt >= s.tHi) // another grid of the batch
-            return;
+            return false;
         const int b0 = (int)(pb >> 1), blo = otherLo(b0), bhi = otherHi(b0);
         const int b1 = (pb & 1) ? bhi : blo;
         const int a0 = b0 == 0 ? 0 : (b1 == 0 ? 1 : 2);
@@ -1253,20 +1282,17 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         const int T1 = (S & 2) ? v1 - an1 : an1 - v1;
         const int T2 = (S & 4) ? v2 - an2 : an2 - v2;
         if (!p.allowPerm && pid != 0)
-            return;
+            return false;
         if (!p.allowSym && S != 0)
-            return;
+            return false;
         if (!p.allowTrans && (T0 | T1 | T2) != 0)
-            return;
-        const uint64_t key = encodeFixed64(s.rSrc, pid, S, T0, T1, T2, L);
+            return false;
+        key = encodeFixed64(s.rSrc, pid, S, T0, T1, T2, L);
         const unsigned long long cur = *((volatile unsigned long long*)&p.parents[tgt]);
         if (key >= cur)
-            return;
-        ++cVer;
-        if (!verifyCandidate<R>(p.grids + (size_t)tgt * (R * R * R / 64), s.lines, a0, a1, a2, S, T0, T1, T2))
-            return;
-        ++cOk;
-        atomicMin(&p.parents[tgt], (unsigned long long)key);
+            return false;
+        geo = (uint32_t)a0 | ((uint32_t)a1 << 2) | (S << 4) | ((uint32_t)(T0 + 32) << 8) | ((uint32_t)(T1 + 32) << 14) | ((uint32_t)(T2 + 32) << 20);
+        return true;
     };
     // persistent warps: each takes 32 consecutive records per step
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -1312,8 +1338,34 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
             const uint32_t hs = __shfl_sync(0xffffffffu, start, h);
             const uint32_t hx = __shfl_sync(0xffffffffu, excl, h);
             const uint64_t hm = __shfl_sync(0xffffffffu, meta, h);
-            if (j < total)
-                candidate(__ldg(&p.entries[hs + (j - hx)]), source(hm));
+            uint32_t tgt = 0, geo = 0;
+            uint64_t key = 0;
+            const bool need = j < total && prepare(__ldg(&p.entries[hs + (j - hx)]), hm, tgt, key, geo);
+            // The verifications of this step, one candidate at a time by the whole warp (a lane alone
+            // would run all R * R rows while the rest of the warp waits).
+            for (unsigned pending = __ballot_sync(0xffffffffu, need); pending; pending &= pending - 1) {
+                const int src = __ffs(pending) - 1;
+                const uint32_t vt = __shfl_sync(0xffffffffu, tgt, src);
+                const uint64_t vk = __shfl_sync(0xffffffffu, key, src);
+                const uint32_t vg = __shfl_sync(0xffffffffu, geo, src);
+                const uint32_t vw = (uint32_t)__shfl_sync(0xffffffffu, hm, src); // source index in the range
+                // a verification earlier in this step may have lowered the target's parent already
+                unsigned long long cur = 0;
+                if ((int)lane == src)
+                    cur = *((volatile unsigned long long*)&p.parents[vt]);
+                cur = __shfl_sync(0xffffffffu, cur, src);
+                if (vk >= cur)
+                    continue;
+                if ((int)lane == src)
+                    ++cVer;
+                const int T0 = (int)((vg >> 8) & 63u) - 32, T1 = (int)((vg >> 14) & 63u) - 32, T2 = (int)((vg >> 20) & 63u) - 32;
+                const bool ok = verifyCandidateWarp<R>(p.grids + (size_t)vt * (R * R * R / 64), p.srcLines + (size_t)vw * 3 * R * R, (int)(vg & 3u),
+                    (int)((vg >> 2) & 3u), (vg >> 4) & 7u, T0, T1, T2, lane);
+                if (ok && (int)lane == src) {
+                    ++cOk;
+                    atomicMin(&p.parents[vt], (unsigned long long)vk);
+                }
+            }
         }
     }
     const uint32_t vals[4] = { cHit, cCand, cVer, cOk };
