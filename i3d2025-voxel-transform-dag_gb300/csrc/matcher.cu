@@ -1156,7 +1156,10 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
                             for (int c = 0; c < C; ++c) {
                                 const uint32_t x = filterFold(key[c]);
                                 bits[c] = filterBits(x);
-                                word[c] = ((nonEmpty >> c) & 1u) ? __ldg(&p.filter[filterWordIndex(x, p.filterShift)]) : 0u;
+                                // level 4: box contents rarely repeat, so filter words bypass L1; the small
+                                // boxes of levels 2-3 repeat often enough to hit in it
+                                const uint32_t* fw = &p.filter[filterWordIndex(x, p.filterShift)];
+                                word[c] = ((nonEmpty >> c) & 1u) ? (R == 16 ? __ldcg(fw) : __ldg(fw)) : 0u;
                             }
                             uint32_t hit = 0;
 #pragma unroll

@@ -225,7 +225,7 @@ __global__ void radixHistKernel(const uint64_t* __restrict__ keys, size_t n, uin
 // out digit run by digit run, so consecutive threads store consecutive addresses.
 constexpr size_t kScatterSmem = (size_t)kSortTile * (8 + 4) + (size_t)(kSortWarps + 2) * 256 * 4;
 
-__global__ void __launch_bounds__(kSortThreads) radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+__global__ void __launch_bounds__(kSortThreads, 3) radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
     uint64_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut, size_t n, uint32_t shift, const uint32_t* __restrict__ offsets, uint32_t numTiles)
 {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -241,20 +241,26 @@ __global__ void __launch_bounds__(kSortThreads) radixScatterKernel(const uint64_
     const size_t tileBase = (size_t)blockIdx.x * kSortTile;
     const size_t warpItems = tileBase + (size_t)warp * (32 * kSortRounds);
     uint64_t key[kSortRounds];
-    uint32_t val[kSortRounds];
+    uint32_t rank[kSortRounds / 2]; // per round, the item's rank among the warp's items of its digit (two u16 per word)
     const uint32_t ltMask = (1u << lane) - 1u;
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
         const size_t i = warpItems + (size_t)r * 32 + lane;
         const bool valid = i < n;
         key[r] = valid ? keysIn[i] : 0;
-        val[r] = valid ? valsIn[i] : 0;
         const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+        const uint32_t before = valid ? warpBase[warp][digit] : 0u;
+        __syncwarp();
         if (valid && (peers & ltMask) == 0)
             warpBase[warp][digit] += __popc(peers);
         __syncwarp();
+        const uint32_t rk = before + __popc(peers & ltMask); // < 32 * kSortRounds
+        if (r & 1)
+            rank[r >> 1] |= rk << 16;
+        else
+            rank[r >> 1] = rk;
     }
     __syncthreads();
     {
@@ -294,20 +300,11 @@ __global__ void __launch_bounds__(kSortThreads) radixScatterKernel(const uint64_
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
         const size_t i = warpItems + (size_t)r * 32 + lane;
-        const bool valid = i < n;
-        const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
-        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-        const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
-        uint32_t pos = 0;
-        if (valid)
-            pos = warpBase[warp][digit] + __popc(peers & ltMask);
-        __syncwarp();
-        if (valid && (peers & ltMask) == 0)
-            warpBase[warp][digit] += __popc(peers);
-        __syncwarp();
-        if (valid) {
+        if (i < n) {
+            const uint32_t digit = (uint32_t)(key[r] >> shift) & 0xFF;
+            const uint32_t pos = warpBase[warp][digit] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu);
             sk[pos] = key[r];
-            sv[pos] = val[r];
+            sv[pos] = valsIn[i]; // the values are read once, here: they take no registers during the ranking
         }
     }
     __syncthreads();
