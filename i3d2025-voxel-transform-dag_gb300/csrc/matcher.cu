@@ -1603,8 +1603,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
     // Source batches. Single grid: ranges of sorted positions growing 8x (levels 2-3: 16x; every batch
-    // costs a table rebuild, so a few large batches beat many small ones), starting at eight teams per SM
-    // (fixed, so that the schedule does not move with the probe kernel's occupancy). Batch: the same
+    // costs a table rebuild, so a few large batches beat many small ones) after a first batch of one team
+    // per SM, starting at eight teams per SM (fixed, so that the schedule does not move with the probe
+    // kernel's occupancy). Batch: the same
     // fractions of every grid (1/512, 1/64, 1/8, 1), as a list of sorted positions per batch, with
     // each grid's own next-batch start for the pruning keys.
     std::vector<uint32_t> bounds { 0 };
@@ -1615,6 +1616,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     if (!batched) {
         const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, nSrc / 256);
         const uint64_t growth = R == 16 ? 8 : 16; // smaller grids probe faster, so their rebuilds weigh more
+        // A first batch of one team per SM: the largest sources give most targets that many sources
+        // match (small, common boxes) their parent, and the pruning after it drops them, so that the
+        // next batch's sources do not enumerate their table runs again.
+        bounds.push_back(std::min<uint32_t>(nSrc, (uint32_t)ctx.numSMs * ProbeShape<R>::TEAMS));
         while (bounds.back() < nSrc) {
             const uint32_t b = bounds.back();
             bounds.push_back((uint32_t)std::min<uint64_t>(nSrc, std::max<uint64_t>((uint64_t)b + minBatch, growth * b)));
