@@ -426,14 +426,14 @@ def choose_sample(host, requested: int, budget_s: float):
 GRID_BYTES = {2: 8, 3: 64, 4: 512}
 
 
-def survey_probe_bytes(level: int, st: dict) -> float:
-    """The probe kernel's algorithmic bytes in the survey's model of the search (one R^3 grid read per
+def search_model_bytes(level: int, st: dict) -> float:
+    """The probe kernel's algorithmic bytes in the cost model of the search (one R^3 grid read per
     source item, one 16-byte (hash, range) slot per non-empty probe): M*G + P*16."""
     return st["items"] * GRID_BYTES[level] + st["probes"] * 16
 
 
-def survey_build_bytes(st_all: dict) -> float:
-    """Algorithmic bytes of a whole build in the survey's model: the hierarchical pass (read node, gather
+def build_model_bytes(st_all: dict) -> float:
+    """Algorithmic bytes of a whole build in the same cost model: the hierarchical pass (read node, gather
     8 child pointers, write mapping, write unique) plus, per translation level, items (grid, 8 corner
     entries, parent), 16 bytes per probe, two grids per verification and the resolve pass."""
     b = 0.0
@@ -665,18 +665,18 @@ def run_ours(args, world, rank, local, pg):
     dom = max(probe_times, key=lambda L: probe_times[L])
     ms = probe_times[dom]
     st = last["translation"][dom]
-    alg = survey_probe_bytes(dom, st)
+    alg = search_model_bytes(dom, st)
     achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else None
     peak, peak_kind = load_peaks()
     dram_alg = probe_algorithmic_bytes(dom, st)
     l2_peak = l2_probe_peak(ctx)
     probes_per_s = st["probes"] / (ms / 1e3) if ms > 0 else None
-    build_bytes = survey_build_bytes(last)
+    build_bytes = build_model_bytes(last)
     build_s = dev_ms / args.steps / 1e3
     roof = {"bound": "hbm", "kernel": f"probeKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
             "traffic": load_traffic(dom, args), "algorithmic_bytes": alg, "device_ms": ms,
-            "model": "survey algorithmic bytes of the search: M*G + P*16 (M source items, G grid bytes, P non-empty probes)",
+            "model": "algorithmic bytes of the search's cost model: M*G + P*16 (M source items, G grid bytes, P non-empty probes)",
             "dram_only": {"algorithmic_bytes": dram_alg, "achieved": dram_alg / (ms / 1e3) / 1e9 if ms > 0 else None,
                           "note": "grids in + line orientations and survivor records out; the filter stays in L2"},
             "l2_probe": {"achieved_loads_per_s": probes_per_s, "peak_loads_per_s": l2_peak,

@@ -6,8 +6,8 @@ reproduce every digest byte for byte (tests/test_gpu_golden.py); tests/test_gold
 the small cases with the oracle.
 
 Cases:
-  terrain256  SURVEY config 0: oracle/generator.py terrain(256, seed 1) -> SVO -> toDAG.
-  scene2048   SURVEY config 1, the bench grid: the device-generated 2048^3 primitive scene
+  terrain256  the 256^3 terrain workload: oracle/generator.py terrain(256, seed 1) -> SVO -> toDAG.
+  scene2048   the bench grid: the device-generated 2048^3 primitive scene
               (SceneSpec(PRIMITIVES, 2048, seed 1, 4000 primitives)), as an .svo file written by
               tdag.scene_svdag(...).to_host().to_svo_bytes(); pass its path with --scene2048.
 
