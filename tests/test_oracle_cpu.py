@@ -159,3 +159,16 @@ def test_find_duplicates_self_consistency(oracle):
             if all(0 <= w[k] < R for k in range(3)):
                 p[w[0], w[1], w[2]] = 1
         assert np.array_equal(np.transpose(p, (2, 1, 0)), dense[i])
+
+
+@pytest.mark.parametrize("sym,axis", [(1, 1), (1, 0), (0, 1)])
+@pytest.mark.parametrize("kind", ["terrain", "blocky"])
+def test_hierarchical_equals_build_without_translation(oracle, sym, axis, kind):
+    """constructTransformDAGHierarchical (transform_dag_hierarchical.cpp:304-529) is the construction
+    with translation off: the library's tdag_build_hierarchical runs tdag_build with translation 0,
+    whose bytes the GPU parity tests compare with construct_tdag(..., translation=0)."""
+    from oracle import generator
+    dense = {"terrain": lambda: generator.terrain(64, 3), "blocky": lambda: blocky_grid(64, 4)}[kind]()
+    svo = dag_svo_bytes(oracle, dense)
+    full, _, _ = oracle.construct_tdag(svo, sym, axis, 0, 0)
+    assert full[:-8] == oracle.hierarchical(svo, sym, axis)  # .tdag = structure + 8-byte config
