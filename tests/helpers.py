@@ -61,3 +61,37 @@ def synthetic_tdag(n_leaves, refs_per_leaf, seed):
     root = len(levels) - 1
     s = tdag.EditStructure(levels, leaves, 1 << root, root, 0, "transform")
     return tdag.write_tdag(s, tdag.TransformDAGConfig()), s
+
+
+def mask_tdag16_padding(data: bytes) -> bytes:
+    """A .tdag16 with the bytes that the reference leaves uninitialised set to zero.
+
+    TransformDAG16::writeTo (transform_dag_encoding.cpp:1023-1030) writes two structs raw:
+    TransformDAGConfig (three bools, one padding byte, a uint32_t; transform_dag.h:157-160) and,
+    in each Huffman decoder, the vector of ``Code {uint64_t code; uint32_t bits;}`` (huffman.h:12-17),
+    whose last 4 of 16 bytes are padding. Only those bytes are cleared."""
+    b = bytearray(data)
+    b[3] = 0
+    off = 8 + 2  # TransformDAGConfig, TransformEncodingConfig
+    rd = lambda o, n: int.from_bytes(b[o:o + n], "little")
+    levels = rd(off, 8)
+    off += 8
+    for _ in range(levels):
+        off += 8 + 2 * rd(off, 8)
+    off += 8 + 8 * rd(off, 8)  # leaves
+    off += 4 + 4  # resolution, rootLevel
+    tables = rd(off, 8)
+    off += 8
+    for _ in range(tables):
+        off += 8 + 8 * rd(off, 8)
+    luts = rd(off, 8)
+    off += 8
+    for _ in range(luts):
+        n = rd(off, 8)
+        off += 8
+        for i in range(n):
+            b[off + 16 * i + 12: off + 16 * i + 16] = b"\0\0\0\0"
+        off += 16 * n
+    if off != len(b):
+        raise ValueError(f".tdag16 layout: parsed {off} of {len(b)} bytes")
+    return bytes(b)

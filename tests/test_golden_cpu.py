@@ -1,5 +1,7 @@
 """The oracle against the committed golden digests (tests/golden/golden.json, written by
-tests/golden/make_golden.py): the config-0 terrain case is re-derived here on every run."""
+tests/golden/make_golden.py). The small cases carry digests made by the reference's own code
+(compiled from its sources into oracle/_ref); the oracle re-derives them here on every run, on every
+machine, so the restatement stays pinned to the reference where the reference cannot be built."""
 import hashlib
 import json
 import os
@@ -7,24 +9,39 @@ import os
 import pytest
 
 from conftest import REPO
+from helpers import blocky_grid
 
 GOLDEN = json.load(open(os.path.join(REPO, "tests", "golden", "golden.json")))
+ENCODINGS = (("tdag16_tables_huffman", True, True), ("tdag16_plain", False, False),
+             ("tdag16_tables", True, False), ("tdag16_huffman", False, True))
 
 
 def _d(b):
     return hashlib.sha256(b).hexdigest()
 
 
-def test_oracle_reproduces_terrain256_golden(oracle):
+def _dense(key):
     from oracle import generator
-    g = GOLDEN["terrain256"]
-    svo = oracle.to_dag(oracle.svo_from_dense(generator.terrain(256, 1)))
-    assert _d(svo) == g["svo_sha256"]
+    return {"terrain256": lambda: generator.terrain(256, 1), "blocky128": lambda: blocky_grid(128, 3)}[key]()
+
+
+@pytest.mark.parametrize("key", ["terrain256", "blocky128"])
+def test_oracle_reproduces_reference_digests(oracle, key):
+    g = GOLDEN[key]
+    r = g["reference"]
+    svo = oracle.to_dag(oracle.svo_from_dense(_dense(key)))
+    assert _d(svo) == r["svo_sha256"] == g["svo_sha256"]
     tdag, _, _ = oracle.construct_tdag(svo)
-    assert _d(tdag) == g["tdag_sha256"]
-    for name, pt, hf in (("tdag16_tables_huffman", True, True), ("tdag16_plain", False, False)):
-        data, _ = oracle.encode_tdag16(tdag, pointer_tables=pt, huffman=hf)
-        assert _d(data) == g[name + "_sha256"], name
+    assert _d(tdag) == r["tdag_sha256"] == g["tdag_sha256"]
+    for name, pt, hf in ENCODINGS:
+        data, _ = oracle.encode_tdag16(tdag, pointer_tables=pt, huffman=hf, tie=oracle.TIE_LIBSTDCXX)
+        assert _d(data) == r[name + "_sha256"] == g[name + "_sha256"], name
+        canon, _ = oracle.encode_tdag16(tdag, pointer_tables=pt, huffman=hf, tie=oracle.TIE_CANONICAL)
+        assert _d(canon) == g[name + "_canonical_sha256"], name
+    for vname, want in r["tdag_variants_sha256"].items():
+        s, p, t, lv = int(vname[1]), int(vname[3]), int(vname[5]), int(vname[7])
+        got, _, _ = oracle.construct_tdag(svo, bool(s), bool(p), bool(t), lv)
+        assert _d(got) == want, vname
 
 
 def test_golden_file_covers_the_bench_grid():
