@@ -11,19 +11,26 @@
 //      form (Huffman-coded pointer type or the plain layout) and is stored inline in the node or in
 //      the level's pointer table; nodes are written as a u16 child mask followed by 1-3 u16 per child.
 //
-// Equal counts are ordered by ascending item index (pass 1) and ascending 64-bit pointer value
-// (pass 2): both sorts are stable radix sorts. The reference leaves those ties to std::sort and to
-// std::unordered_map iteration, so its file bytes depend on the standard library build; the
-// decoded voxels and the Huffman tables do not.
+// How items with equal counts are ordered decides the file bytes (not the voxels, sizes or Huffman
+// tables). The reference leaves it to std::sort (pass 1, pointer_encoding.h:49) and to the iteration
+// order of a std::unordered_map followed by std::sort (pass 2, transform_dag_encoding.cpp:276-295).
+//  * TDAG16_TIES_REFERENCE (default): those two steps run on the host, with libstdc++'s std::sort and
+//    std::unordered_map, the reference's hash of a TransformPointer and the reference's insertion
+//    sequence; everything else stays on the device. The bytes equal the reference's as built with
+//    GCC and the serial parallel-algorithm backend (a TBB build may order ties differently).
+//  * TDAG16_TIES_CANONICAL: ties by ascending item index (pass 1) and ascending 64-bit pointer value
+//    (pass 2), both from stable radix sorts on the device, with no host step.
 //
-// Everything is integer work on small arrays (a few bytes per node) dominated by radix sorts; the
-// one host step per level is the 384-symbol length-limited Huffman code (package-merge), which is
-// tiny and fixed-size.
+// Everything else is integer work on small arrays (a few bytes per node) dominated by radix sorts;
+// the other host step per level is the 384-symbol length-limited Huffman code (package-merge), which
+// is tiny and fixed-size.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <memory>
+#include <memory_resource>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -128,6 +135,62 @@ std::vector<PointerCode> huffmanCodes(const std::vector<uint64_t>& freq, uint32_
         next += 1ull << (maxLen - len[s]);
     }
     return codes;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host: the reference's order of equal counts (TDAG16_TIES_REFERENCE).
+// ------------------------------------------------------------------------------------------------
+// std::hash<TransformPointer> (transform_dag.h:412-433): hash_combine (hash.h:10-15) over ptr, the
+// three mirror flags, the three permutation entries and the three translations, each through the
+// identity std::hash of its type; the int translations sign-extend to size_t. The call is not
+// noexcept, like the reference's, so libstdc++ caches the hash codes in the nodes as it does there.
+struct ReferencePointerHash {
+    size_t operator()(uint64_t tp) const
+    {
+        uint64_t seed = hashCombine(0, tpPtr(tp));
+        for (int k = 0; k < 3; ++k)
+            seed = hashCombine(seed, (tp >> (37 + k)) & 1);
+        for (int k = 0; k < 3; ++k)
+            seed = hashCombine(seed, (tp >> (40 + 2 * k)) & 3);
+        for (int k = 0; k < 3; ++k)
+            seed = hashCombine(seed, (uint64_t)(int64_t)tpT(tp, k));
+        return (size_t)seed;
+    }
+};
+
+// sortByReferenceCount's order (pointer_encoding.h:46-49): the indices 0..n-1 under std::sort by
+// count, descending. Unreferenced items (count 0) come last; the caller keeps the first `kept`.
+uint32_t referenceCountOrder(const std::vector<uint32_t>& counts, std::vector<uint32_t>& order)
+{
+    order.resize(counts.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return counts[l] > counts[r]; });
+    uint32_t kept = 0;
+    while (kept < order.size() && counts[order[kept]] != 0)
+        ++kept;
+    return kept;
+}
+
+// The distinct child pointers of a level in the reference's order (transform_dag_encoding.cpp:276-295):
+// counted in a std::unordered_map in node order, children 0..7, then iterated and std::sort-ed by
+// count, descending. `instances` are the level's child pointers in that order (remapped to the
+// encoded child level). Node storage comes from an arena; the iteration order of libstdc++'s map
+// depends on the hash codes, the insertion sequence and its rehash policy, not on the allocator.
+std::vector<uint64_t> referencePointerOrder(const std::vector<uint64_t>& instances)
+{
+    std::pmr::monotonic_buffer_resource arena(instances.size() * 48 + 4096);
+    std::pmr::unordered_map<uint64_t, uint32_t, ReferencePointerHash> counts(&arena);
+    for (uint64_t tp : instances)
+        counts[tp]++;
+    std::vector<std::pair<uint32_t, uint64_t>> byCount;
+    byCount.reserve(counts.size());
+    for (const auto& [tp, n] : counts)
+        byCount.push_back({ n, tp });
+    std::sort(byCount.begin(), byCount.end(), [](const auto& l, const auto& r) { return l.first > r.first; });
+    std::vector<uint64_t> out(byCount.size());
+    for (size_t i = 0; i < byCount.size(); ++i)
+        out[i] = byCount[i].second;
+    return out;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -468,7 +531,7 @@ constexpr unsigned kBlock = 256;
 // the parents' child indices (sortByReferenceCount with prune = true).
 template <int W>
 DevBuf<uint64_t> sortByReferenceCount(Context& c, const DevBuf<uint64_t>& items, uint64_t count, DevBuf<uint64_t>& parents, uint64_t parentCount,
-    uint64_t& keptOut)
+    bool referenceTies, uint64_t& keptOut)
 {
     cudaStream_t s = c.stream;
     const uint64_t slots = parentCount * 8;
@@ -482,14 +545,26 @@ DevBuf<uint64_t> sortByReferenceCount(Context& c, const DevBuf<uint64_t>& items,
         TDAG_LAUNCHED();
     }
     const uint32_t maxCount = (uint32_t)std::min<uint64_t>(slots, 0xFFFFFFFFull);
-    if (count) {
-        refKeysKernel<<<gridFor(count, kBlock), kBlock, 0, s>>>(counts.get(), count, maxCount, keys.get(), vals.get(), kept.get());
-        TDAG_LAUNCHED();
-        radixSortPairs(keys.get(), vals.get(), count, 0, std::max(1u, bitWidth(maxCount)), s);
-    }
     uint32_t k = 0;
-    TDAG_CUDA(cudaMemcpyAsync(&k, kept.get(), 4, cudaMemcpyDeviceToHost, s));
-    c.checkStatus("encode16: reference counts");
+    if (referenceTies) {
+        std::vector<uint32_t> hostCounts(count), order;
+        if (count)
+            TDAG_CUDA(cudaMemcpyAsync(hostCounts.data(), counts.get(), count * 4, cudaMemcpyDeviceToHost, s));
+        c.checkStatus("encode16: reference counts");
+        k = referenceCountOrder(hostCounts, order);
+        if (k) {
+            TDAG_CUDA(cudaMemcpyAsync(vals.get(), order.data(), (uint64_t)k * 4, cudaMemcpyHostToDevice, s));
+            TDAG_CUDA(cudaStreamSynchronize(s)); // `order` is pageable host memory released on return
+        }
+    } else {
+        if (count) {
+            refKeysKernel<<<gridFor(count, kBlock), kBlock, 0, s>>>(counts.get(), count, maxCount, keys.get(), vals.get(), kept.get());
+            TDAG_LAUNCHED();
+            radixSortPairs(keys.get(), vals.get(), count, 0, std::max(1u, bitWidth(maxCount)), s);
+        }
+        TDAG_CUDA(cudaMemcpyAsync(&k, kept.get(), 4, cudaMemcpyDeviceToHost, s));
+        c.checkStatus("encode16: reference counts");
+    }
     DevBuf<uint64_t> out(std::max<uint64_t>((uint64_t)k * W, 1), s);
     DevBuf<uint32_t> mapping(std::max<uint64_t>(count, 1), s);
     if (k) {
@@ -520,6 +595,9 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
     cudaStream_t s = c.stream;
     const uint32_t root = dag.root_level;
     TDAG_CHECK(root >= 3 && root < TDAG_MAX_LEVELS, TDAG_ERR_ARG, "the encoder needs a root level of 3 or more");
+    TDAG_CHECK(enc.tie_order == TDAG16_TIES_REFERENCE || enc.tie_order == TDAG16_TIES_CANONICAL, TDAG_ERR_ARG,
+        "tie_order must be TDAG16_TIES_REFERENCE or TDAG16_TIES_CANONICAL");
+    const bool referenceTies = enc.tie_order == TDAG16_TIES_REFERENCE;
     const uint64_t launches0 = g_kernelLaunches.load();
     TDAG_CUDA(cudaEventRecord(c.ev[5], s));
 
@@ -541,12 +619,12 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
     // Pass 1: top-down reference-count order (pointer_encoding.h:27-72; transform_dag_encoding.cpp:246-253).
     for (uint32_t l = root - 1; l > 2; --l) {
         uint64_t kept = 0;
-        nodes[l] = sortByReferenceCount<8>(c, nodes[l], counts[l], nodes[l + 1], counts[l + 1], kept);
+        nodes[l] = sortByReferenceCount<8>(c, nodes[l], counts[l], nodes[l + 1], counts[l + 1], referenceTies, kept);
         counts[l] = kept;
     }
     {
         uint64_t kept = 0;
-        leaves = sortByReferenceCount<1>(c, leaves, counts[2], nodes[3], counts[3], kept);
+        leaves = sortByReferenceCount<1>(c, leaves, counts[2], nodes[3], counts[3], referenceTies, kept);
         counts[2] = kept;
     }
 
@@ -586,9 +664,14 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
         DevBuf<uint32_t> vals(std::max<uint32_t>(m, 1), s), runFlag(std::max<uint32_t>(m, 1), s), runScan(std::max<uint32_t>(m, 1), s);
         DevBuf<uint32_t> slotRun(std::max<uint64_t>(slots, 1), s);
         uint32_t u = 0;
+        std::vector<uint64_t> instances; // the level's child pointers in node order (reference ties)
         if (m) {
             instanceKeysKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(nodes[l].get(), instSlots.get(), m, keys.get(), vals.get());
             TDAG_LAUNCHED();
+            if (referenceTies) {
+                instances.resize(m);
+                TDAG_CUDA(cudaMemcpyAsync(instances.data(), keys.get(), (uint64_t)m * 8, cudaMemcpyDeviceToHost, s));
+            }
             radixSortPairs(keys.get(), vals.get(), m, 0, 64, s);
             runFlagsKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(keys.get(), m, runFlag.get());
             TDAG_LAUNCHED();
@@ -603,7 +686,21 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
             TDAG_LAUNCHED();
             runCountKeysKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(runStart.get(), u, m, m, runCount.get(), countKeys.get(), byCount.get());
             TDAG_LAUNCHED();
-            radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(m)), s);
+            if (referenceTies) {
+                // Runs are numbered in ascending pointer value; name the reference's order by run.
+                std::vector<uint64_t> values(u);
+                TDAG_CUDA(cudaMemcpyAsync(values.data(), runVal.get(), (uint64_t)u * 8, cudaMemcpyDeviceToHost, s));
+                c.checkStatus("encode16: distinct pointers");
+                const std::vector<uint64_t> order = referencePointerOrder(instances);
+                TDAG_CHECK(order.size() == u, TDAG_ERR_CUDA, "encode16: distinct pointer counts disagree");
+                std::vector<uint32_t> runOrder(u);
+                for (uint32_t k = 0; k < u; ++k)
+                    runOrder[k] = (uint32_t)(std::lower_bound(values.begin(), values.end(), order[k]) - values.begin());
+                TDAG_CUDA(cudaMemcpyAsync(byCount.get(), runOrder.data(), (uint64_t)u * 4, cudaMemcpyHostToDevice, s));
+                TDAG_CUDA(cudaStreamSynchronize(s)); // `runOrder` is released at the end of this scope
+            } else {
+                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(m)), s);
+            }
             scatterRankKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(byCount.get(), u, rankOfRun.get());
             TDAG_LAUNCHED();
         }

@@ -97,10 +97,21 @@ class TransformDAGConfig:
 @dataclasses.dataclass
 class TransformEncodingConfig:
     """TransformEncodingConfig (tools/svdag_encoding/src/transform_dag_encoding.h:180-182). The
-    svdag_encoding tool defaults both flags off (main.cpp:34); the renderer's files set both."""
+    svdag_encoding tool defaults both flags off (main.cpp:34); the renderer's files set both.
+
+    ``tie_order`` is not a reference setting: "reference" (the default) gives the reference's bytes
+    (equal reference counts ordered by libstdc++'s std::sort and std::unordered_map iteration, two
+    host steps per level); "canonical" orders them by index and pointer value on the device only."""
 
     pointer_tables: bool = False
     huffman_code: bool = False
+    tie_order: str = "reference"
+
+    def tie_code(self) -> int:
+        try:
+            return {"reference": 0, "canonical": 1}[self.tie_order]
+        except KeyError:
+            raise ValueError(f"tie_order must be 'reference' or 'canonical', not {self.tie_order!r}") from None
 
 
 # ------------------------------------------------------------------------------------------------
@@ -555,7 +566,7 @@ def construct_transform_dag16(dag, dag_config: TransformDAGConfig = TransformDAG
         rp_in = dag._rp
     else:
         rp_in = ctypes.pointer(_host_result_view(dag, keep))
-    enc = _abi.EncodingConfig(int(encoding_config.pointer_tables), int(encoding_config.huffman_code))
+    enc = _abi.EncodingConfig(int(encoding_config.pointer_tables), int(encoding_config.huffman_code), encoding_config.tie_code())
     op = ctypes.POINTER(_abi.Tdag16Result)()
     _abi.check(lib().tdag_encode16(ctx.handle, rp_in, ctypes.byref(_config_struct(dag_config)), ctypes.byref(enc), ctypes.byref(op)))
     try:

@@ -97,7 +97,7 @@ class Tuning(ctypes.Structure):
 
 
 class EncodingConfig(ctypes.Structure):
-    _fields_ = [("pointer_tables", ctypes.c_int32), ("huffman_code", ctypes.c_int32)]
+    _fields_ = [("pointer_tables", ctypes.c_int32), ("huffman_code", ctypes.c_int32), ("tie_order", ctypes.c_int32)]
 
 
 class Tdag16LevelStats(ctypes.Structure):

@@ -6,10 +6,15 @@
  * by BinaryWriter::write(TransformDAG16) (transform_dag_encoding.cpp:1023-1030), as the svdag_encoding
  * tool does for a .tdag16 output (tools/svdag_encoding/src/main.cpp:87-134).
  *
- * The result is the .tdag16 file image. It decodes to the same voxels as the reference's encoding of
- * the same transform DAG and uses the same Huffman tables; equal reference counts are ordered by
- * ascending item index and ascending pointer value, where the reference leaves the order to std::sort
- * and std::unordered_map iteration (so its bytes depend on the standard-library build).
+ * The result is the .tdag16 file image. Two steps of the reference order items with equal reference
+ * counts by whatever std::sort and std::unordered_map iteration give (pointer_encoding.h:49;
+ * transform_dag_encoding.cpp:276-295), so the file bytes depend on the standard library. By default
+ * (TDAG16_TIES_REFERENCE) the encoder runs exactly those two steps on the host with libstdc++'s
+ * std::sort and std::unordered_map, the reference's hash of a TransformPointer and the reference's
+ * insertion sequence, and its bytes equal the reference's as built with GCC (serial parallel-algorithm
+ * backend); struct padding that the reference leaves uninitialised is written as zero.
+ * TDAG16_TIES_CANONICAL orders ties by ascending item index and pointer value with stable radix sorts
+ * on the device: the same voxels, Huffman tables and sizes, no host step, different bytes.
  */
 #ifndef TDAG16_H_
 #define TDAG16_H_
@@ -25,7 +30,11 @@ extern "C" {
 typedef struct tdag_encoding_config {
     int32_t pointer_tables; /* frequent pointers through a per-level table (--pointertables) */
     int32_t huffman_code; /* Huffman-coded pointer types (--huffman) */
+    int32_t tie_order; /* TDAG16_TIES_REFERENCE (0, the reference's bytes) or TDAG16_TIES_CANONICAL (1) */
 } tdag_encoding_config;
+
+#define TDAG16_TIES_REFERENCE 0
+#define TDAG16_TIES_CANONICAL 1
 
 /* DAGEncodingStats::LevelStats (transform_dag_encoding.h:187-203), index = tree level. */
 typedef struct tdag16_level_stats {

@@ -183,7 +183,7 @@ def decode_fixed64(e: int, level: int) -> int:
 # ------------------------------------------------------------------------------------------------
 # .tdag16 (tdag16_oracle.cpp)
 # ------------------------------------------------------------------------------------------------
-TIE_CANONICAL = 0  # ties by ascending item index / ascending pointer value (the library's order)
+TIE_CANONICAL = 0  # ties by ascending item index / ascending pointer value (the library's canonical option)
 TIE_LIBSTDCXX = 1  # std::sort + std::unordered_map, as the reference behaves with libstdc++ (serial backend)
 LEVEL16_KEYS = ("num_nodes", "memory_in_bytes", "table_size", "unique_pointers", "table_u16", "table_u32",
                 "table_u48", "direct_u16", "direct_u32", "direct_u48")
@@ -223,8 +223,9 @@ def huffman_decode(codes, key):
     return int(s.value), int(n.value)
 
 
-def encode_tdag16(tdag: bytes, pointer_tables=False, huffman=False, tie=TIE_CANONICAL):
-    """constructTransformDAG16 on .tdag bytes -> (.tdag16 bytes, per-level stats dicts)."""
+def encode_tdag16(tdag: bytes, pointer_tables=False, huffman=False, tie=TIE_LIBSTDCXX):
+    """constructTransformDAG16 on .tdag bytes -> (.tdag16 bytes, per-level stats dicts). The default tie
+    order is the reference's (libstdc++), which the reference compiled here reproduces byte for byte."""
     a, p = _u8(tdag)
     out = ctypes.POINTER(ctypes.c_uint8)()
     n = ctypes.c_uint64()

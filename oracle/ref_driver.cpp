@@ -19,7 +19,9 @@
 //  * ref_encode_tdag16: a .tdag read and encoded as svdag_encoding does
 //    (svdag_encoding/src/main.cpp:88-96, 126-132);
 //  * ref_to_static / ref_construct_static_tdag: StaticStructure(EditStructure) (structure.h:765-798)
-//    and constructStaticTransformDAG (transform_dag.cpp:242-390), StaticStructure::writeTo bytes.
+//    and constructStaticTransformDAG (transform_dag.cpp:242-390), StaticStructure::writeTo bytes;
+//  * ref_encode_static_tdag16: constructTransformDAG16 of a StaticStructure<void, TransformPointer>
+//    (transform_dag_encoding.cpp:519-697), written like ref_encode_tdag16.
 #include "transform_dag_encoding.h"
 #include <voxcom/utility/binary_reader.h>
 #include <voxcom/utility/binary_writer.h>
@@ -191,6 +193,29 @@ int ref_encode_tdag16(const uint8_t* tdag, uint64_t len, int pointerTables, int 
         encodingConfig.huffmanCode = huffman != 0;
         DAGEncodingStats stats;
         const TransformDAG16 encoded = constructTransformDAG16(std::move(transformDAG), dagConfig, encodingConfig, stats);
+        std::ostringstream os(std::ios::binary);
+        BinaryWriter writer { os };
+        writer.write(encoded);
+        return emit(os, out, outLen);
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int ref_encode_static_tdag16(const uint8_t* st, uint64_t len, int sym, int axis, int trans, uint32_t level, int pointerTables,
+    int huffman, uint8_t** out, uint64_t* outLen)
+{
+    try {
+        auto is = inStream(st, len);
+        BinaryReader reader { is };
+        StaticStructure<void, TransformPointer> in;
+        in.readFrom(reader);
+        const auto cfg = makeConfig(sym, axis, trans, level);
+        TransformEncodingConfig encodingConfig;
+        encodingConfig.pointerTables = pointerTables != 0;
+        encodingConfig.huffmanCode = huffman != 0;
+        DAGEncodingStats stats;
+        const TransformDAG16 encoded = constructTransformDAG16(std::move(in), cfg, encodingConfig, stats);
         std::ostringstream os(std::ios::binary);
         BinaryWriter writer { os };
         writer.write(encoded);

@@ -58,6 +58,7 @@ def lib():
         L.ref_encode_tdag16.argtypes = [u8p, ctypes.c_uint64, i, i, u8pp, u64p]
         L.ref_to_static.argtypes = [u8p, ctypes.c_uint64, u8pp, u64p]
         L.ref_construct_static_tdag.argtypes = [u8p, ctypes.c_uint64, i, i, i, ctypes.c_uint32, u8pp, u64p]
+        L.ref_encode_static_tdag16.argtypes = [u8p, ctypes.c_uint64, i, i, i, ctypes.c_uint32, i, i, u8pp, u64p]
         _lib = L
     return _lib
 
@@ -112,3 +113,10 @@ def to_static(svo: bytes) -> bytes:
 def construct_static_tdag(static_bytes: bytes, symmetry=True, axis=True, translation=True, max_level=4) -> bytes:
     return _call(lib().ref_construct_static_tdag, *_buf(static_bytes), int(symmetry), int(axis), int(translation),
                  int(max_level))
+
+
+def encode_static_tdag16(static_tdag: bytes, symmetry=True, axis=True, translation=True, max_level=4, pointer_tables=False,
+                         huffman=False) -> bytes:
+    """constructTransformDAG16 of a StaticStructure<void, TransformPointer> (StaticStructure::writeTo bytes)."""
+    return _call(lib().ref_encode_static_tdag16, *_buf(static_tdag), int(symmetry), int(axis), int(translation), int(max_level),
+                 int(pointer_tables), int(huffman))

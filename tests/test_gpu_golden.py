@@ -1,7 +1,9 @@
 """Full-size parity against the committed golden digests (tests/golden/golden.json): the library's
-.svo, .tdag and .tdag16 bytes of the config-0 terrain and of the 2048^3 bench grid must equal the
-oracle's, digest for digest. The 2048^3 digests were computed by the oracle on the same SVDAG
-(tests/golden/make_golden.py), so this checks the whole pipeline bit for bit at the bench size."""
+.svo, .tdag and .tdag16 bytes of the config-0 terrain, a blocky grid and the 2048^3 bench grid must
+equal the golden ones, digest for digest. The small cases' digests were made by the reference's own
+code (compiled from its sources into oracle/_ref) and by the oracle, which agree; the 2048^3 digests
+were computed by the oracle on the same SVDAG (tests/golden/make_golden.py). So the whole pipeline
+(SVO -> toDAG -> Transform DAG -> .tdag16) is checked bit for bit, in both .tdag16 tie orders."""
 import hashlib
 import json
 import os
@@ -9,9 +11,12 @@ import os
 import pytest
 
 from conftest import REPO
+from helpers import blocky_grid
 
 pytestmark = pytest.mark.gpu
 GOLDEN = json.load(open(os.path.join(REPO, "tests", "golden", "golden.json")))
+ENCODINGS = (("tdag16_tables_huffman", True, True), ("tdag16_plain", False, False),
+             ("tdag16_tables", True, False), ("tdag16_huffman", False, True))
 
 
 def _d(b):
@@ -23,15 +28,28 @@ def _check(tdaglib, gpu_ctx, g, sv):
     cfg = tdaglib.TransformDAGConfig()
     dev = tdaglib.construct_transform_dag_device(sv, cfg, ctx=gpu_ctx)
     assert _d(tdaglib.write_tdag(dev.to_host(gpu_ctx), cfg)) == g["tdag_sha256"]
-    for name, pt, hf in (("tdag16_tables_huffman", True, True), ("tdag16_plain", False, False)):
-        data = tdaglib.construct_transform_dag16(dev, cfg, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx)
-        assert _d(data) == g[name + "_sha256"], name
+    checked = 0
+    for name, pt, hf in ENCODINGS:
+        for tie, key in (("reference", name + "_sha256"), ("canonical", name + "_canonical_sha256")):
+            if key in g:
+                data = tdaglib.construct_transform_dag16(dev, cfg, tdaglib.TransformEncodingConfig(pt, hf, tie), ctx=gpu_ctx)
+                assert _d(data) == g[key], (name, tie)
+                checked += 1
+    assert checked >= 2
 
 
 def test_terrain256_matches_golden(tdaglib, gpu_ctx):
     from oracle import generator
+    g = GOLDEN["terrain256"]
+    assert g["reference"]["tdag_sha256"] == g["tdag_sha256"]
     sv = tdaglib.svdag_from_dense(generator.terrain(256, 1), ctx=gpu_ctx)
-    _check(tdaglib, gpu_ctx, GOLDEN["terrain256"], sv)
+    _check(tdaglib, gpu_ctx, g, sv)
+
+
+def test_blocky128_matches_golden(tdaglib, gpu_ctx):
+    g = GOLDEN["blocky128"]
+    sv = tdaglib.svdag_from_dense(blocky_grid(128, 3), ctx=gpu_ctx)
+    _check(tdaglib, gpu_ctx, g, sv)
 
 
 def test_bench_grid_2048_matches_golden(tdaglib, gpu_ctx):

@@ -1,9 +1,10 @@
 """GPU parity of the .tdag16 encoder (tdag_encode16) against the oracle's encoder, byte for byte.
 
-The oracle orders equal reference counts by ascending item index and ascending pointer value (its
-canonical tie order, the one the library implements); both are compared on every encoding variant
-(plain, Huffman, pointer tables, both), on transform DAGs built by the oracle and by the GPU, and on
-a synthetic DAG whose pointer table outgrows 16-bit indices.
+Both tie orders are compared: the default (the reference's: libstdc++ std::sort and
+std::unordered_map iteration, which the oracle reproduces and which is pinned to the reference's own
+encoder by test_reference_pin_cpu.py) and the canonical one (ascending item index and pointer value).
+Every encoding variant (plain, Huffman, pointer tables, both) is covered, on transform DAGs built by
+the oracle and by the GPU, and on a synthetic DAG whose pointer table outgrows 16-bit indices.
 """
 import numpy as np
 import pytest
@@ -15,9 +16,12 @@ pytestmark = pytest.mark.gpu
 ENCODINGS = [(False, False), (False, True), (True, False), (True, True)]
 
 
-def _gpu_encode(tdaglib, gpu_ctx, tdag_bytes, pt, hf):
+TIES = [("reference", 1), ("canonical", 0)]  # library tie_order, oracle tie mode
+
+
+def _gpu_encode(tdaglib, gpu_ctx, tdag_bytes, pt, hf, tie="reference"):
     s, cfg = tdaglib.read_tdag(tdag_bytes)
-    return tdaglib.construct_transform_dag16(s, cfg, tdaglib.TransformEncodingConfig(pt, hf), ctx=gpu_ctx, return_stats=True)
+    return tdaglib.construct_transform_dag16(s, cfg, tdaglib.TransformEncodingConfig(pt, hf, tie), ctx=gpu_ctx, return_stats=True)
 
 
 CASES = [
@@ -35,10 +39,10 @@ def test_encode16_matches_oracle(oracle, tdaglib, gpu_ctx, name, make, cfg):
     from oracle import generator
     dense = make(generator)
     t, _, _ = oracle.construct_tdag(dag_svo_bytes(oracle, dense), **cfg)
-    for pt, hf in ENCODINGS:
-        ref, ref_stats = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
-        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf)
-        assert got == ref, (name, pt, hf)
+    for (pt, hf), (tie, otie) in [(e, t_) for e in ENCODINGS for t_ in TIES]:
+        ref, ref_stats = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf, tie=otie)
+        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf, tie)
+        assert got == ref, (name, pt, hf, tie)
         for l in range(2, len(ref_stats)):
             g, r = st["levels"][l], ref_stats[l]
             assert (g["num_nodes"], g["memory_in_bytes"], g["table_size"]) == (r["num_nodes"], r["memory_in_bytes"], r["table_size"])
@@ -51,10 +55,10 @@ def test_encode16_matches_oracle(oracle, tdaglib, gpu_ctx, name, make, cfg):
 
 def test_encode16_pointer_table_widening(oracle, tdaglib, gpu_ctx):
     t, _ = synthetic_tdag(70000, 5, 1)
-    for pt, hf in [(True, True), (True, False)]:
-        ref, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf)
-        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf)
-        assert got == ref, (pt, hf)
+    for (pt, hf), (tie, otie) in [(e, t_) for e in [(True, True), (True, False)] for t_ in TIES]:
+        ref, _ = oracle.encode_tdag16(t, pointer_tables=pt, huffman=hf, tie=otie)
+        got, st = _gpu_encode(tdaglib, gpu_ctx, t, pt, hf, tie)
+        assert got == ref, (pt, hf, tie)
         assert st["levels"][3]["table_pointers"][0] == 65536
 
 

@@ -120,3 +120,15 @@ def test_terrain128_end_to_end_equals_reference(reflib, oracle):
     for pt, hf in ((0, 0), (1, 1)):
         enc, _ = oracle.encode_tdag16(got, pointer_tables=bool(pt), huffman=bool(hf), tie=oracle.TIE_LIBSTDCXX)
         assert enc == mask_tdag16_padding(reflib.encode_tdag16(tdag, pt, hf))
+
+
+@pytest.mark.parametrize("pt,hf", [(0, 0), (1, 1)])
+def test_static_tdag16_equals_reference(reflib, oracle, grids, pt, hf):
+    """constructTransformDAG16 of a static transform DAG (transform_dag_encoding.cpp:519-697) makes the
+    same bytes as the encoder of the unpacked structure, which is how the library encodes it."""
+    import tdag
+    dag = reflib.to_dag(reflib.svo_from_dense(grids["blocky64"]))
+    st = reflib.construct_static_tdag(reflib.to_static(dag))
+    edit = tdag.write_tdag(tdag.StaticStructure.from_bytes(st, "transform").to_edit(), tdag.TransformDAGConfig())
+    got, _ = oracle.encode_tdag16(edit, pointer_tables=bool(pt), huffman=bool(hf), tie=oracle.TIE_LIBSTDCXX)
+    assert got == mask_tdag16_padding(reflib.encode_static_tdag16(st, pointer_tables=pt, huffman=hf))
