@@ -16,8 +16,13 @@ roofline: the dominant kernel -- the translation probe kernel of the level with 
           MEASURED_PEAKS.json. Beside it: the DRAM-only bytes; its filter loads per second against this
           GPU's random-load ceiling for L2-resident buffers (tdag_l2_probe_peak), the resource that
           actually bounds it; and the whole build's model bytes over the build time.
-cpu_baseline / --impl reference: the CPU oracle (a restatement of the reference's CPU path, all
-          host threads) on a bounded sub-volume sample of the same grid.
+cpu_baseline: the CPU oracle (the restatement of the reference's CPU path, pinned byte for byte to
+          the reference's own code; all host threads) on the WHOLE grid, once, in a child process with
+          a time limit (--cpu-baseline full, the default for the single-grid workload); its key
+          "sample" adds the same oracle on seeded random sub-volumes, as the reference arm runs it.
+--impl reference: the same oracle on a different seeded random aligned sub-volume of the same grid
+          per step (256^3 by default), generated on the CPU by oracle/scene_oracle.cpp, so that this
+          arm loads no product library.
 
 Multi-GPU: the path does not shard; --gpus N runs N independent replicas (one per rank), and value
 is the sum of their throughputs (max-over-ranks timing).
@@ -57,8 +62,11 @@ def parse_args():
     ap.add_argument("--scene", default="primitives", choices=["primitives", "terrain"],
                     help="primitives: the primitive-union shell (configs 1, 3, 4); terrain: solid fBm terrain (config 0, 256^3)")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: auto)")
+    ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: 256, or the grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-baseline", default="auto", choices=["auto", "full", "sample"],
+                    help="full: the oracle on the whole grid once (auto: up to 2048^3); sample: random sub-volumes only")
+    ap.add_argument("--cpu-baseline-timeout", type=float, default=900.0, help="seconds allowed to the whole-grid oracle build")
     ap.add_argument("--workload", default="single", choices=["single", "batch96", "proposal"],
                     help="single: one 2048^3 grid (headline); batch96: 96 grids of 128^3..1024^3 in one batched build; "
                          "proposal: learned source proposals (approximate) against the exhaustive build of the same grid")
@@ -231,6 +239,64 @@ def scene_spec(args):
     return tdag.SceneSpec(kind=tdag.SCENE_PRIMITIVES, resolution=args.resolution, seed=args.seed, num_primitives=args.primitives)
 
 
+def cpu_samples(args, count: int, side: int = 0, seed: int = 12345):
+    """`count` aligned side^3 sub-volumes of the workload's grid, drawn without replacement (seeded)
+    among the non-empty ones and reused cyclically when there are fewer, as (.svo bytes of the SVDAG,
+    solid voxels, origin). Generated on the CPU by the oracle's scene statement: the restriction of
+    the whole grid to each sub-box, shell included (scene_oracle.cpp). The config-0 terrain is small
+    enough to be its own sample."""
+    from oracle import generator
+    from oracle import oracle as orc
+    orc.build()
+    if getattr(args, "scene", "primitives") == "terrain":
+        dense = generator.terrain(args.resolution, args.seed)
+        svo = orc.to_dag(orc.svo_from_dense(dense))
+        return [(svo, int(dense.sum()), (0, 0, 0))] * count
+    side = min(side or args.sample_resolution or 256, args.resolution)
+    per = args.resolution // side
+    rng = np.random.default_rng(seed)
+    out = []
+    for idx in rng.permutation(per ** 3):
+        if len(out) == count:
+            break
+        origin = (int(idx % per) * side, int(idx // per % per) * side, int(idx // (per * per)) * side)
+        dense = orc.scene_dense(args.resolution, args.seed, args.primitives, origin=origin, size=side)
+        vox = int(dense.sum())
+        if vox:
+            out.append((orc.to_dag(orc.svo_from_dense(dense)), vox, origin))
+    return [out[i % len(out)] for i in range(count)] if out else []
+
+
+def oracle_build_seconds(svo: bytes) -> float:
+    """One oracle constructTransformDAG (default config) on .svo bytes, all host threads: seconds."""
+    from oracle import oracle as orc
+    orc.build()
+    t0 = time.perf_counter()
+    orc.construct_tdag(svo, True, True, True, 4)
+    return time.perf_counter() - t0
+
+
+def _oracle_child(svo: bytes, q):
+    q.put(oracle_build_seconds(svo))
+
+
+def oracle_build_seconds_limited(svo: bytes, timeout_s: float):
+    """oracle_build_seconds in a spawned child process, given up after timeout_s (None then)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    p = ctx.Process(target=_oracle_child, args=(svo, q), daemon=True)
+    p.start()
+    try:
+        return q.get(timeout=timeout_s)
+    except Exception:
+        return None
+    finally:
+        if p.is_alive():
+            p.terminate()
+        p.join(timeout=10)
+
+
 def workload_config(args, voxels=None):
     if getattr(args, "scene", "primitives") == "terrain":
         what = f"{args.resolution}^3 solid fBm terrain (5 octaves, base frequency 1/64, seed {args.seed})"
@@ -342,85 +408,6 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------------------------
-# CPU sample: a sub-volume of the same grid, as its own SVDAG (.svo bytes)
-# ------------------------------------------------------------------------------------------------
-def sub_volume_svo(host, sample_res: int):
-    """Extract the SVDAG of the densest aligned sample_res^3 sub-volume reachable from the root."""
-    import tdag
-    target_level = sample_res.bit_length() - 1
-    levels = host.nodes_per_level
-    # voxel counts per node, bottom-up
-    pc = np.array([bin(int(v)).count("1") for v in host.sub_grids], dtype=np.int64)
-    counts = {2: pc}
-    for lvl in range(3, host.root_level + 1):
-        n = levels[lvl].astype(np.int64)
-        e = n == tdag.EMPTY_CHILD
-        counts[lvl] = np.where(e, 0, counts[lvl - 1][np.where(e, 0, n)]).sum(axis=1)
-    # walk down from the root along the densest child to the target level
-    node = 0
-    for lvl in range(host.root_level, target_level, -1):
-        ch = levels[lvl][node].astype(np.int64)
-        best, bestc = None, -1
-        for c in ch:
-            if c != tdag.EMPTY_CHILD and counts[lvl - 1][c] > bestc:
-                best, bestc = int(c), int(counts[lvl - 1][c])
-        node = best
-    # collect reachable items per level and re-index
-    new_levels = [np.zeros((0, 8), np.uint32) for _ in range(target_level + 1)]
-    frontier = np.array([node], dtype=np.int64)
-    remap_prev = None
-    order = {}
-    for lvl in range(target_level, 2, -1):
-        order[lvl] = frontier
-        ch = levels[lvl][frontier].astype(np.int64)
-        nxt = np.unique(ch[ch != tdag.EMPTY_CHILD])
-        frontier = nxt
-    order[2] = frontier
-    for lvl in range(3, target_level + 1):
-        ids = order[lvl]
-        below = order[lvl - 1]
-        ch = levels[lvl][ids].astype(np.int64)
-        e = ch == tdag.EMPTY_CHILD
-        pos = np.searchsorted(below, np.where(e, below[0] if len(below) else 0, ch))
-        new_levels[lvl] = np.where(e, tdag.EMPTY_CHILD, pos).astype(np.uint32)
-    sub = tdag.EditStructure(new_levels, host.sub_grids[order[2]].copy(), sample_res, target_level, 1, "u32")
-    return sub.to_svo_bytes(), int(counts[target_level][node])
-
-
-def cpu_sample_run(svo: bytes, threads: int = 0):
-    from oracle import oracle as orc
-    orc.build()
-    if threads:
-        orc.set_threads(threads)
-    t0 = time.perf_counter()
-    _, st, _ = orc.construct_tdag(svo, True, True, True, 4)
-    return time.perf_counter() - t0, st
-
-
-def choose_sample(host, requested: int, budget_s: float):
-    """Pick the largest sub-volume side (power of two) whose oracle run fits the time budget."""
-    sizes = [requested] if requested else [512, 256, 128]
-    last = None
-    for s in sizes:
-        if s >= host.resolution:
-            continue
-        svo, vox = sub_volume_svo(host, s)
-        last = (s, svo, vox)
-        if requested:
-            break
-        # estimate from a probe on the next smaller side
-        if s > 128:
-            psvo, pvox = sub_volume_svo(host, s // 2)
-            dt, _ = cpu_sample_run(psvo)
-            est = dt * (vox / max(pvox, 1))
-            if est <= budget_s:
-                return last
-            continue
-        return last
-    return last
-
-
-# ------------------------------------------------------------------------------------------------
 # roofline of the dominant kernel
 # ------------------------------------------------------------------------------------------------
 GRID_BYTES = {2: 8, 3: 64, 4: 512}
@@ -494,36 +481,33 @@ def load_traffic(level: int, args):
 
 # ------------------------------------------------------------------------------------------------
 def run_reference(args, world, rank, pg):
-    """Reference arm: the CPU restatement of the reference path (all host threads) on a bounded
-    sub-volume sample of the same grid; only rank 0 works."""
+    """Reference arm: the CPU restatement of the reference path (pinned byte for byte to the reference's
+    own code; all host threads), one seeded random aligned sub-volume of the same grid per step,
+    generated on the CPU. Loads no product library. Only rank 0 works."""
     if rank != 0:
         barrier(pg)
         return
-    import tdag
-    ctx = tdag.default_context()
-    spec = scene_spec(args)
-    g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
-    host = g.to_host()
-    g.free()
-    s = args.sample_resolution or 256
-    svo, vox = sub_volume_svo(host, s)
     from oracle import oracle as orc
     orc.build()
     cores = orc.max_threads()
-    for _ in range(args.warmup):
-        cpu_sample_run(svo)
-    times = []
-    for _ in range(args.steps):
-        dt, _ = cpu_sample_run(svo)
-        times.append(dt)
+    samples = cpu_samples(args, max(args.warmup, 0) + args.steps)
+    for svo, _, _ in samples[: max(args.warmup, 0)]:
+        oracle_build_seconds(svo)
+    times, voxels = [], 0
+    for svo, vox, _ in samples[max(args.warmup, 0):]:
+        times.append(oracle_build_seconds(svo))
+        voxels += vox
     total = sum(times)
-    value = vox * len(times) / total / 1e6
+    value = voxels / total / 1e6
+    side = min(args.sample_resolution or 256, args.resolution)
+    what = ("the whole 256^3 terrain per step" if getattr(args, "scene", "primitives") == "terrain" else
+            f"a different seeded random aligned {side}^3 sub-volume of the same grid per step ({voxels} solid voxels over "
+            f"{args.steps} steps), generated on the CPU")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": workload_config(args, host.compute_voxel_count()),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{s}^3 densest sub-volume of the same grid ({vox} solid voxels) per step"},
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": what},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -673,7 +657,7 @@ def run_ours(args, world, rank, local, pg):
     probes_per_s = st["probes"] / (ms / 1e3) if ms > 0 else None
     build_bytes = build_model_bytes(last)
     build_s = dev_ms / args.steps / 1e3
-    roof = {"bound": "hbm", "kernel": f"probeKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
+    roof = {"bound": "l2", "kernel": f"probeKernel<R={1 << dom}> (translation level {dom})", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
             "traffic": load_traffic(dom, args), "algorithmic_bytes": alg, "device_ms": ms,
             "model": "algorithmic bytes of the search's cost model: M*G + P*16 (M source items, G grid bytes, P non-empty probes)",
@@ -704,10 +688,22 @@ def run_ours(args, world, rank, local, pg):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
         orc.build()
-        s, svo, vox = choose_sample(host, args.sample_resolution, budget_s=20.0)
-        dt, _ = cpu_sample_run(svo)
-        out["cpu_baseline"] = {"value": vox / dt / 1e6, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
-                               "sample": f"{s}^3 densest sub-volume of the same grid ({vox} solid voxels), one oracle build, {dt:.1f} s"}
+        cores = orc.max_threads()
+        samples = cpu_samples(args, 8)
+        sdt = sum(oracle_build_seconds(svo) for svo, _, _ in samples)
+        svox = sum(v for _, v, _ in samples)
+        side = min(args.sample_resolution or 256, args.resolution)
+        sample = {"value": svox / sdt / 1e6, "unit": UNIT, "cores": cores,
+                  "sample": f"8 seeded random aligned {side}^3 sub-volumes of the same grid ({svox} solid voxels), {sdt:.1f} s"}
+        mode = args.cpu_baseline if args.cpu_baseline != "auto" else ("full" if args.resolution <= 2048 else "sample")
+        full_s = oracle_build_seconds_limited(host.to_svo_bytes(), args.cpu_baseline_timeout) if mode == "full" else None
+        if full_s:
+            out["cpu_baseline"] = {"value": voxels / full_s / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+                                   "sample": f"the whole grid ({voxels} solid voxels): one oracle build of its SVDAG, {full_s:.1f} s",
+                                   "sample_subvolumes": sample}
+        else:
+            why = "" if mode == "sample" else f" (the whole-grid build did not finish within {args.cpu_baseline_timeout:.0f} s)"
+            out["cpu_baseline"] = dict(sample, kind="port", sample=sample["sample"] + why)
     if rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -15,6 +15,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -70,15 +71,76 @@ const TransformTables& hostTables()
     return t;
 }
 
-void Context::checkStatus(const std::string& where)
+uint32_t Context::takeStatus(uint32_t* aux)
 {
     TDAG_CUDA(cudaMemcpyAsync(hostStatus, status, 16, cudaMemcpyDeviceToHost, stream));
     TDAG_CUDA(cudaStreamSynchronize(stream));
-    if (hostStatus[0] != 0) {
-        const uint32_t code = hostStatus[0], aux = hostStatus[1];
+    const uint32_t code = hostStatus[0];
+    if (aux)
+        *aux = hostStatus[1];
+    if (code != 0) {
         TDAG_CUDA(cudaMemsetAsync(status, 0, 16, stream));
         TDAG_CUDA(cudaStreamSynchronize(stream));
+    }
+    return code;
+}
+
+void Context::checkStatus(const std::string& where)
+{
+    uint32_t aux = 0;
+    const uint32_t code = takeStatus(&aux);
+    if (code != 0)
         throw Error((int)code, where + ": device reported error " + std::to_string(code) + " (aux " + std::to_string(aux) + ")");
+}
+
+uint64_t Context::classTableCapacity(uint64_t n) const
+{
+    const uint64_t load = tuning.class_table_load_percent ? tuning.class_table_load_percent : 50;
+    uint64_t cap = 1;
+    const uint64_t want = n * 100 / load + 16;
+    while (cap < want)
+        cap <<= 1;
+    return cap;
+}
+
+namespace {
+std::mutex g_budgetMutex;
+std::unordered_map<cudaStream_t, std::shared_ptr<MemoryBudget>> g_budgets;
+std::atomic<bool> g_anyBudget { false };
+}
+
+std::shared_ptr<MemoryBudget> budgetOf(cudaStream_t stream)
+{
+    if (!g_anyBudget.load(std::memory_order_acquire))
+        return nullptr;
+    std::lock_guard<std::mutex> lock(g_budgetMutex);
+    const auto it = g_budgets.find(stream);
+    return it == g_budgets.end() ? nullptr : it->second;
+}
+
+void registerBudget(cudaStream_t stream, uint64_t limit)
+{
+    std::lock_guard<std::mutex> lock(g_budgetMutex);
+    auto b = std::make_shared<MemoryBudget>();
+    b->limit = limit;
+    g_budgets[stream] = std::move(b);
+    g_anyBudget.store(true, std::memory_order_release);
+}
+
+void unregisterBudget(cudaStream_t stream)
+{
+    std::lock_guard<std::mutex> lock(g_budgetMutex);
+    g_budgets.erase(stream);
+    g_anyBudget.store(!g_budgets.empty(), std::memory_order_release);
+}
+
+void chargeBudget(MemoryBudget& b, uint64_t bytes)
+{
+    const uint64_t before = b.used.fetch_add(bytes);
+    if (before + bytes > b.limit) {
+        b.used -= bytes;
+        throw Error(TDAG_ERR_OOM, "device memory limit of the context reached: " + std::to_string(before) + " B held, " + std::to_string(bytes) +
+                " B requested, limit " + std::to_string(b.limit) + " B");
     }
 }
 
@@ -335,6 +397,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
     TDAG_CHECK(in.leafCount < (1ull << 31), TDAG_ERR_ARG, "too many leaves");
     validateInput(ctx, in);
     cudaStream_t s = ctx.stream;
+    ctx.tableRegrows = 0;
     const uint64_t launches0 = g_kernelLaunches.load();
     TDAG_CUDA(cudaEventRecord(ctx.ev[2], s));
     const uint32_t midLevel = cfg.max_translation_level + 1;
@@ -373,6 +436,7 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
         TDAG_CUDA(cudaEventElapsedTime(&stats->translation_ms, ctx.ev[3], ctx.ev[4]));
         TDAG_CUDA(cudaEventElapsedTime(&stats->total_ms, ctx.ev[2], ctx.ev[4]));
         stats->kernel_launches = g_kernelLaunches.load() - launches0;
+        stats->table_regrows = ctx.tableRegrows;
     }
     return out;
 }
@@ -560,6 +624,8 @@ int tdag_ctx_create(int device, const tdag_tuning* tuning, tdag_ctx** out)
         if (tuning)
             c.tuning = *tuning;
         TDAG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        if (c.tuning.device_memory_limit)
+            registerBudget(c.stream, c.tuning.device_memory_limit);
         cudaMemPool_t pool;
         TDAG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
         uint64_t threshold = ~0ull;
@@ -574,6 +640,7 @@ int tdag_ctx_create(int device, const tdag_tuning* tuning, tdag_ctx** out)
         // Probe that the kernels load on this device (fails loudly on a non-sm_103 GPU).
         cudaFuncAttributes fa;
         TDAG_CUDA(cudaFuncGetAttributes(&fa, flattenKernel<2>));
+        prepareNoAlloc(c);
     });
     if (rc != TDAG_OK) {
         tdag_ctx_destroy(holder.release());
@@ -602,8 +669,10 @@ int tdag_ctx_destroy(tdag_ctx* ctx)
         cudaFreeHost(c.hostStatus);
     if (c.stage)
         cudaFreeHost(c.stage);
-    if (c.stream)
+    if (c.stream) {
+        unregisterBudget(c.stream);
         cudaStreamDestroy(c.stream);
+    }
     delete ctx;
     return TDAG_OK;
 }

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <atomic>
 #include <cstdio>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <cuda_runtime.h>
@@ -183,6 +184,21 @@ struct TransformTables {
 const TransformTables& hostTables();
 
 // ------------------------------------------------------------------------------------------------
+// Device-memory budgets (tdag_tuning.device_memory_limit). A context created with a limit registers
+// its stream; every DevBuf allocated on that stream is charged to the budget until it is released,
+// and an allocation that would pass the limit throws TDAG_ERR_OOM before reaching the driver. The
+// budget is shared by the buffers charged to it, so results that outlive their context stay valid.
+// ------------------------------------------------------------------------------------------------
+struct MemoryBudget {
+    uint64_t limit = 0;
+    std::atomic<uint64_t> used { 0 };
+};
+std::shared_ptr<MemoryBudget> budgetOf(cudaStream_t stream); // null: no limit on this stream
+void registerBudget(cudaStream_t stream, uint64_t limit);
+void unregisterBudget(cudaStream_t stream);
+void chargeBudget(MemoryBudget& b, uint64_t bytes); // throws TDAG_ERR_OOM past the limit
+
+// ------------------------------------------------------------------------------------------------
 // Small device-memory helpers (stream-ordered allocations from the context's pool).
 // ------------------------------------------------------------------------------------------------
 template <typename T>
@@ -190,13 +206,26 @@ struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
     cudaStream_t s = 0;
+    std::shared_ptr<MemoryBudget> budget; // set when the stream has a device-memory limit
     DevBuf() = default;
     DevBuf(size_t count, cudaStream_t stream)
         : n(count)
         , s(stream)
     {
-        if (count)
-            TDAG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), stream));
+        if (count) {
+            if (auto b = budgetOf(stream)) {
+                chargeBudget(*b, count * sizeof(T));
+                budget = std::move(b);
+            }
+            const cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), stream);
+            if (e != cudaSuccess) {
+                p = nullptr;
+                if (budget)
+                    budget->used -= count * sizeof(T);
+                budget.reset();
+                TDAG_CUDA(e);
+            }
+        }
     }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
@@ -208,6 +237,7 @@ struct DevBuf {
             p = o.p;
             n = o.n;
             s = o.s;
+            budget = std::move(o.budget);
             o.p = nullptr;
             o.n = 0;
         }
@@ -216,8 +246,12 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void release()
     {
-        if (p)
+        if (p) {
             cudaFreeAsync(p, s);
+            if (budget)
+                budget->used -= n * sizeof(T);
+        }
+        budget.reset();
         p = nullptr;
         n = 0;
     }

@@ -78,3 +78,21 @@ extern "C" int tdag_l2_probe_peak(tdag_ctx* ctx, uint64_t buffer_bytes, uint64_t
         *loads_per_s = (double)threads * rounds * kPeakInFlight / (ms / 1e3);
     });
 }
+
+extern "C" int tdag_device_pool_usage(tdag_ctx* ctx, uint64_t* used_bytes, uint64_t* reserved_bytes)
+{
+    using namespace tdag;
+    if (!ctx || !used_bytes || !reserved_bytes)
+        return failWith(TDAG_ERR_ARG, "null argument");
+    return guardedCall([&] {
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        cudaMemPool_t pool;
+        TDAG_CUDA(cudaDeviceGetDefaultMemPool(&pool, c.device));
+        uint64_t used = 0, reserved = 0; // the attributes are 64-bit values
+        TDAG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+        TDAG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+        *used_bytes = used;
+        *reserved_bytes = reserved;
+    });
+}

@@ -471,6 +471,12 @@ void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s)
     fillU32Kernel<<<gridFor(n, 256), 256, 0, s>>>(p, v, n);
     TDAG_LAUNCHED();
 }
+void preloadFillKernels()
+{
+    cudaFuncAttributes fa;
+    TDAG_CUDA(cudaFuncGetAttributes(&fa, fillU64Kernel));
+    TDAG_CUDA(cudaFuncGetAttributes(&fa, fillU32Kernel));
+}
 
 // Shared tail of one level: class table -> canonicals -> emission order -> mapping.
 // sigWords = 1 (leaves) or 8 (nodes). Produces mapping (n), inv per handle (u) and the emit order.
@@ -480,29 +486,26 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     std::vector<uint64_t>& handleOff)
 {
     cudaStream_t s = ctx.stream;
-    const uint64_t cap = pow2AtLeast((uint64_t)n * 2 + 16);
-    DevBuf<uint64_t> slots(cap, s);
-    DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
-    fillU64(slots.get(), kEmptySlot, cap, s);
-    fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
-    if (sigWords == 1)
-        classInsertKernel<1><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    else if (sigWords == 2)
-        classInsertKernel<2><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    else if (sigWords == 8)
-        classInsertKernel<8><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    else
-        classInsertKernel<9><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    TDAG_LAUNCHED();
-    slots.release();
-
     DevBuf<uint32_t> canonOf(n, s), isCanon(n, s);
     DevBuf<uint8_t> tOf(n, s);
     DevBuf<uint64_t> invOf(n, s);
-    resolve(slotOf.get(), minIdx.get(), canonOf.get(), tOf.get(), invOf.get(), isCanon.get());
-    slotOf.release();
-    minIdx.release();
-    ctx.checkStatus("hierarchical level " + std::to_string(level));
+    withClassTable(ctx, n, "hierarchical level " + std::to_string(level), [&](uint64_t cap) {
+        DevBuf<uint64_t> slots(cap, s);
+        DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
+        fillU64(slots.get(), kEmptySlot, cap, s);
+        fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
+        if (sigWords == 1)
+            classInsertKernel<1><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        else if (sigWords == 2)
+            classInsertKernel<2><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        else if (sigWords == 8)
+            classInsertKernel<8><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        else
+            classInsertKernel<9><<<gridFor(n, kThreads), kThreads, 0, s>>>(sig, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        TDAG_LAUNCHED();
+        slots.release();
+        resolve(slotOf.get(), minIdx.get(), canonOf.get(), tOf.get(), invOf.get(), isCanon.get());
+    });
 
     DevBuf<uint32_t> canonList(n, s);
     const uint32_t u = compactFlags(isCanon.get(), canonList.get(), n, s);

@@ -21,9 +21,42 @@ struct Context {
     size_t stageBytes = 0;
     int pageableAccess = -1; // cudaDevAttrPageableMemoryAccess of the device (-1: not queried yet)
 
+    uint32_t tableRegrows = 0; // class-table doublings of the current build
+    unsigned char* noAllocScratch = nullptr; // device address of the no-allocation matcher's array
+
     // Synchronise the stream, read the device status word, throw on a recorded error.
     void checkStatus(const std::string& where);
+    // Synchronise, read and clear the device status word; returns its error code (0: none).
+    uint32_t takeStatus(uint32_t* aux = nullptr);
+    // Slots of a class table for n items at the tuned load (power of two, at least n / load + 16).
+    uint64_t classTableCapacity(uint64_t n) const;
+    uint32_t tableRegrowLimit() const { return tuning.table_regrow_limit ? tuning.table_regrow_limit : 4u; }
 };
+
+// Runs attempt(capacity) — a class-table insert and the kernels that read the table — and then
+// checks the device status. A table whose bounded probes ran out (TDAG_ERR_TABLE_FULL) is doubled
+// and the attempt rerun, up to the context's regrow limit; each doubling is counted in
+// ctx.tableRegrows. Any other device error, or a table still full at the limit, throws. The table
+// capacity changes no result: class membership and class minima do not depend on slot positions.
+template <typename F>
+void withClassTable(Context& ctx, uint64_t n, const std::string& where, F&& attempt)
+{
+    uint64_t cap = ctx.classTableCapacity(n);
+    for (uint32_t regrows = 0;; ++regrows) {
+        attempt(cap);
+        uint32_t aux = 0;
+        const uint32_t code = ctx.takeStatus(&aux);
+        if (code == 0)
+            return;
+        if (code == TDAG_ERR_TABLE_FULL && regrows < ctx.tableRegrowLimit()) {
+            cap *= 2;
+            ++ctx.tableRegrows;
+            continue;
+        }
+        throw Error((int)code, where + ": device reported error " + std::to_string(code) + " (aux " + std::to_string(aux) + ")" +
+                (code == TDAG_ERR_TABLE_FULL ? " after " + std::to_string(regrows) + " table regrows" : std::string()));
+    }
+}
 
 // Device-resident view of an EditStructure<void, uint32_t>, or of a batch of them concatenated level
 // by level in grid order (child indices then address the concatenated level below). For a batch,
@@ -86,6 +119,8 @@ inline uint64_t allowedMask(const tdag_config& c)
 
 void fillU64(uint64_t* p, uint64_t v, size_t n, cudaStream_t s);
 void fillU32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s);
+void preloadFillKernels(); // loads the fill kernels' code now (primitives or hierarchical TU)
+void prepareNoAlloc(Context& ctx); // matcher.cu; called by tdag_ctx_create
 
 HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_config& cfg, uint32_t midLevel, tdag_stats* stats);
 

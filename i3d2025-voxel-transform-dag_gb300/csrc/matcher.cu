@@ -1922,9 +1922,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
 // Limits: at most kNoAllocMaxItems items per call (levels 2..4). The array is part of the module:
 // every GPU that loads libtdag.so holds it until the process exits. All calls share it, so calls
 // that overlap on the GPU (two contexts, or two threads on one context) race and must be
-// serialised by the caller. The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current); make that first call before
-// any stream capture.
+// serialised by the caller. tdag_ctx_create resolves the array's device address with
+// cudaGetSymbolAddress (with the context's device current) and keeps it in the context, and it
+// loads the kernels of this path, so that the driver's lazy module loading places the array and
+// the code at context creation rather than inside the first call. The call is synchronous on the
+// context's stream: it reads the device status word before it returns.
 // ================================================================================================
 namespace {
 
@@ -2123,23 +2125,41 @@ void runMatcherNoAlloc(Context& ctx, unsigned char* scratch, const uint64_t* gri
     ctx.checkStatus("no-alloc matcher level " + std::to_string(LV));
 }
 
-std::mutex g_noAllocMutex;
-unsigned char* g_noAllocAddr[64] = {};
-
-// Device address of the scratch array for the current device (looked up once per device).
-unsigned char* noAllocScratchAddress(int device)
+template <typename K>
+void loadKernel(K* kernel)
 {
-    TDAG_CHECK(device >= 0 && device < 64, TDAG_ERR_ARG, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_noAllocMutex);
-    if (!g_noAllocAddr[device]) {
-        void* p = nullptr;
-        TDAG_CUDA(cudaGetSymbolAddress(&p, g_noAllocScratch));
-        g_noAllocAddr[device] = static_cast<unsigned char*>(p);
-    }
-    return g_noAllocAddr[device];
+    cudaFuncAttributes fa;
+    TDAG_CUDA(cudaFuncGetAttributes(&fa, kernel));
 }
 
 } // namespace
+
+// Called by tdag_ctx_create with the context's device current: the scratch array's device address
+// (kept in the context, so that it always belongs to the current primary context of the device) and
+// every kernel the no-allocation path launches, loaded now instead of lazily inside its first call.
+void prepareNoAlloc(Context& ctx)
+{
+    void* p = nullptr;
+    TDAG_CUDA(cudaGetSymbolAddress(&p, g_noAllocScratch));
+    ctx.noAllocScratch = static_cast<unsigned char*>(p);
+    loadKernel(noAllocRankKernel<1>);
+    loadKernel(noAllocRankKernel<8>);
+    loadKernel(noAllocRankKernel<64>);
+    loadKernel(cornerHashKernel<4>);
+    loadKernel(cornerHashKernel<8>);
+    loadKernel(cornerHashKernel<16>);
+    loadKernel(searchKernel<4, 2>);
+    loadKernel(searchKernel<8, 3>);
+    loadKernel(searchKernel<16, 4>);
+    loadKernel(tableInsertKernel);
+    loadKernel(noAllocScanKernel);
+    loadKernel(tableScatterKernel);
+    loadKernel(tableRangesKernel);
+    loadKernel(decodeParentsKernel);
+    loadKernel(noAllocUniquesKernel);
+    loadKernel(finalMappingKernel);
+    preloadFillKernels();
+}
 
 MatchOutput runMatcher(Context& ctx, uint32_t level, const uint64_t* grids, uint32_t n, const tdag_config& cfg, tdag_level_stats* stats, const Segments* seg,
     const uint32_t* sources, uint32_t numSources)
@@ -2188,7 +2208,8 @@ extern "C" int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level,
             TDAG_CUDA(cudaStreamSynchronize(c.stream));
             return;
         }
-        unsigned char* scratch = noAllocScratchAddress(c.device);
+        unsigned char* scratch = c.noAllocScratch;
+        TDAG_CHECK(scratch != nullptr, TDAG_ERR_NO_DEVICE, "the context has no no-allocation scratch array");
         if (level == 2)
             runMatcherNoAlloc<2>(c, scratch, d_grids, n, *cfg, d_out_mapping, d_out_unique, d_n_unique);
         else if (level == 3)

@@ -504,23 +504,21 @@ void buildTree(Context& ctx, DevBuf<uint64_t>& leafArray, uint64_t numLeafCells,
 uint32_t dedupLevel(Context& ctx, const uint64_t* keys, int words, uint32_t n, DevBuf<uint32_t>& mapping, DevBuf<uint32_t>& firsts)
 {
     cudaStream_t s = ctx.stream;
-    const uint64_t cap = pow2AtLeast((uint64_t)n * 2 + 16);
-    DevBuf<uint64_t> slots(cap, s);
-    DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
-    fillU64(slots.get(), kEmptySlot, cap, s);
-    fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
-    if (words == 1)
-        classInsertKernel<1><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    else
-        classInsertKernel<4><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
-    TDAG_LAUNCHED();
-    slots.release();
     DevBuf<uint32_t> flags(n, s), canon(n, s);
-    firstFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(slotOf.get(), minIdx.get(), n, flags.get(), canon.get());
-    TDAG_LAUNCHED();
-    slotOf.release();
-    minIdx.release();
-    ctx.checkStatus("toDAG");
+    withClassTable(ctx, n, "toDAG", [&](uint64_t cap) {
+        DevBuf<uint64_t> slots(cap, s);
+        DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
+        fillU64(slots.get(), kEmptySlot, cap, s);
+        fillU32(minIdx.get(), 0xFFFFFFFFu, cap, s);
+        if (words == 1)
+            classInsertKernel<1><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        else
+            classInsertKernel<4><<<gridFor(n, 256), 256, 0, s>>>(keys, n, slots.get(), minIdx.get(), slotOf.get(), cap - 1, ctx.status);
+        TDAG_LAUNCHED();
+        slots.release();
+        firstFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(slotOf.get(), minIdx.get(), n, flags.get(), canon.get());
+        TDAG_LAUNCHED();
+    });
     firsts = DevBuf<uint32_t>(n, s);
     DevBuf<uint32_t> handleOf(n, s);
     const uint32_t u = compactFlags(flags.get(), firsts.get(), n, s);

@@ -50,7 +50,7 @@ class LevelStats(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("hierarchical", LevelStats * MAX_LEVELS), ("translation", LevelStats * MAX_LEVELS),
                 ("total_ms", ctypes.c_float), ("hierarchical_ms", ctypes.c_float),
-                ("translation_ms", ctypes.c_float), ("reserved", ctypes.c_float), ("kernel_launches", ctypes.c_uint64)]
+                ("translation_ms", ctypes.c_float), ("table_regrows", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint64)]
 
 
 class Result(ctypes.Structure):
@@ -93,7 +93,8 @@ class Primitive(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("filter_bits_per_key", ctypes.c_uint32), ("table_load_percent", ctypes.c_uint32),
-                ("search_ctas_per_sm", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("search_ctas_per_sm", ctypes.c_uint32), ("class_table_load_percent", ctypes.c_uint32),
+                ("table_regrow_limit", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("device_memory_limit", ctypes.c_uint64)]
 
 
 class EncodingConfig(ctypes.Structure):
@@ -128,6 +129,7 @@ EXPORTED = (
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_build_static", "tdag_static_result_free",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
+    "tdag_device_pool_usage",  # include/tdag_diag.h
     "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
     "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify", "tdag16_raycast",
 )
@@ -176,6 +178,7 @@ def lib(path: str = None):
                                                          vp, vp, vp]
         L.tdag_result_to_host.argtypes = [vp, ctypes.POINTER(Result), ctypes.POINTER(ctypes.POINTER(Result))]
         L.tdag_l2_probe_peak.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+        L.tdag_device_pool_usage.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         L.tdag_find_duplicates_level_device.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.POINTER(Config), vp, ctypes.c_uint32,
                                                         vp, vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(LevelStats)]
         L.tdag_build_device_proposed.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Config), PROPOSAL_FN, vp,
@@ -212,6 +215,7 @@ def level_stats_to_dict(s: LevelStats) -> dict:
 def stats_to_dict(s: Stats, root_level: int) -> dict:
     return {
         "kernel_launches": s.kernel_launches, "total_ms": s.total_ms, "hierarchical_ms": s.hierarchical_ms, "translation_ms": s.translation_ms,
+        "table_regrows": s.table_regrows,
         "hierarchical": {l: level_stats_to_dict(s.hierarchical[l]) for l in range(2, root_level + 1)},
         "translation": {l: level_stats_to_dict(s.translation[l]) for l in range(2, 5)},
     }

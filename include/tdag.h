@@ -79,7 +79,7 @@ typedef struct tdag_stats {
     float total_ms; /* device time of the whole construction (tdag_build*: without host copies) */
     float hierarchical_ms;
     float translation_ms;
-    float reserved;
+    uint32_t table_regrows; /* class tables doubled after TDAG_ERR_TABLE_FULL (see tdag_tuning) */
     uint64_t kernel_launches; /* kernels this library launched for the construction */
 } tdag_stats;
 
@@ -102,7 +102,15 @@ typedef struct tdag_tuning {
     uint32_t filter_bits_per_key; /* membership filter size (power of two rounded) */
     uint32_t table_load_percent; /* corner-hash table load factor in percent (50..85) */
     uint32_t search_ctas_per_sm; /* persistent search CTAs per SM */
+    uint32_t class_table_load_percent; /* initial load of the class tables of the hierarchical pass and
+                                        * toDAG (default 50). A table whose bounded probes run out
+                                        * (TDAG_ERR_TABLE_FULL on the device) is doubled and the pass
+                                        * rerun; above 100 the first table is certain to be too small. */
+    uint32_t table_regrow_limit; /* doublings allowed per table (default 4); past them the call
+                                  * returns TDAG_ERR_TABLE_FULL */
     uint32_t reserved;
+    uint64_t device_memory_limit; /* bytes of device memory the context's calls may hold at once
+                                   * (0 = no limit); an allocation past it fails with TDAG_ERR_OOM */
 } tdag_tuning;
 
 /* Library/version information. */
@@ -156,8 +164,10 @@ int tdag_find_duplicates_level(tdag_ctx* ctx, uint32_t level, const uint64_t* gr
  * one 4 MiB array compiled into libtdag.so; the call makes no cudaMalloc/cudaFree. At most 4096
  * items per call (levels 2..4; larger calls return TDAG_ERR_ARG). The array is shared by all calls
  * on all contexts of a device: calls that overlap on the GPU race and must be serialised by the
- * caller. The first call on a device looks up the array's address (once per device); make it before
- * any stream capture. *d_n_unique is written on the device. */
+ * caller. tdag_ctx_create resolves the array's address and loads this path's kernels, so the driver's
+ * lazy loading places them at context creation, not inside a call. The call is synchronous on the
+ * context's stream (it reads the device status word before returning). *d_n_unique is written on
+ * the device. */
 int tdag_find_duplicates_level_noalloc(tdag_ctx* ctx, uint32_t level, const uint64_t* d_grids, uint32_t n,
     const tdag_config* config, uint64_t* d_out_mapping, uint32_t* d_out_unique, uint32_t* d_n_unique);
 

@@ -20,7 +20,7 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++ -O3 -fopenmp)."""
-    sources = [os.path.join(_HERE, f) for f in ("tdag_oracle.cpp", "tdag16_oracle.cpp", "Makefile")]
+    sources = [os.path.join(_HERE, f) for f in ("tdag_oracle.cpp", "tdag16_oracle.cpp", "scene_oracle.cpp", "Makefile")]
     if force or not os.path.exists(_LIB_PATH) or (
         os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(f) for f in sources)
     ):
@@ -65,6 +65,9 @@ def lib():
                                                 u8pp, u64p]
         L.orc_static_tdag_decode.argtypes = [u8p, ctypes.c_uint64, u8p, ctypes.c_uint32]
         L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_scene_last_error.restype = ctypes.c_char_p
+        L.orc_scene_primitives.argtypes = [ctypes.c_uint32] * 4 + [ctypes.c_void_p, ctypes.c_uint32, u32p]
+        L.orc_scene_dense.argtypes = [ctypes.c_uint32] * 4 + [ctypes.c_int] + [ctypes.c_uint32] * 4 + [u8p]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
@@ -285,4 +288,33 @@ def static_tdag_decode(static_tdag: bytes, res: int) -> np.ndarray:
     a, p = _u8(static_tdag)
     dense = np.zeros((res, res, res), dtype=np.uint8)
     _chk(lib().orc_static_tdag_decode(p, len(static_tdag), dense.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), res))
+    return dense
+
+
+# ------------------------------------------------------------------------------------------------
+# Procedural primitive scenes (scene_oracle.cpp)
+# ------------------------------------------------------------------------------------------------
+PRIMITIVE_DTYPE = np.dtype([("type", "<u4"), ("xform", "<u4"), ("size", "<i4", 3), ("radius", "<i4"), ("offset", "<i4", 3),
+                            ("seed", "<u4"), ("source", "<u4"), ("reserved", "<u4")])
+
+
+def scene_primitives(resolution: int, seed: int, num_primitives: int, copy_percent: int = 30) -> np.ndarray:
+    """The primitive list of a scene, as a structured array laid out like tdag_primitive."""
+    out = np.zeros(max(num_primitives, 1), PRIMITIVE_DTYPE)
+    n = ctypes.c_uint32()
+    if lib().orc_scene_primitives(resolution, seed, num_primitives, copy_percent, out.ctypes.data_as(ctypes.c_void_p), len(out),
+                                  ctypes.byref(n)) != 0:
+        raise OracleError(lib().orc_scene_last_error().decode())
+    return out[: n.value]
+
+
+def scene_dense(resolution: int, seed: int, num_primitives: int, copy_percent: int = 30, shell: bool = True, origin=(0, 0, 0),
+                size: int = 0) -> np.ndarray:
+    """dense[z, y, x] of the sub-box of side ``size`` (default: the whole grid) at ``origin`` of a
+    primitive scene: exactly the restriction of the whole grid, its shell included."""
+    size = size or resolution
+    dense = np.zeros((size, size, size), np.uint8)
+    if lib().orc_scene_dense(resolution, seed, num_primitives, copy_percent, int(shell), int(origin[0]), int(origin[1]), int(origin[2]),
+                             size, dense.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))) != 0:
+        raise OracleError(lib().orc_scene_last_error().decode())
     return dense

@@ -70,3 +70,33 @@ def test_peak_source(bench):
     peak, kind = bench.load_peaks()
     assert peak > 0
     assert kind == ("measured" if os.path.exists(os.path.join(REPO, "MEASURED_PEAKS.json")) else "fallback")
+
+
+def test_cpu_samples_are_restrictions_of_the_grid(bench, oracle):
+    """The reference arm's per-step inputs: distinct seeded sub-volumes, each the SVDAG of the grid's
+    restriction to its box (checked against the whole 128^3 grid)."""
+    import numpy as np
+    args = _args(resolution=128, primitives=60, sample_resolution=32)
+    samples = bench.cpu_samples(args, 5)
+    full = oracle.scene_dense(128, 1, 60)
+    origins = [o for _, _, o in samples]
+    assert len(set(origins)) == 5
+    for svo, vox, (x, y, z) in samples:
+        sub = full[z:z + 32, y:y + 32, x:x + 32]
+        assert vox == int(sub.sum()) > 0
+        assert svo == oracle.to_dag(oracle.svo_from_dense(sub))
+
+
+def test_reference_arm_runs_without_the_product_library(tmp_path):
+    """--impl reference prints its JSON line and never loads libtdag.so."""
+    import subprocess
+    import sys
+    code = ("import runpy, sys; sys.argv=['bench.py','--impl','reference','--steps','2','--warmup','1','--resolution','128',"
+            "'--primitives','60','--sample-resolution','32']; runpy.run_path('bench.py', run_name='__main__'); "
+            "print('LOADED', [m for m in open('/proc/self/maps').read().split() if m.endswith('.so') and 'libtdag' in m])")
+    r = subprocess.run([sys.executable, "-c", code], cwd=REPO, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    line = json.loads(lines[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+    assert "LOADED []" in r.stdout
