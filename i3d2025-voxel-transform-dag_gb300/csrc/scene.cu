@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "class_table.cuh"
+#include "slab_hash.cuh"
 #include "common.cuh"
 #include "internal.cuh"
 
@@ -600,92 +601,68 @@ __device__ __forceinline__ uint64_t contentFp(const uint64_t* k)
         fp = mix64(fp ^ k[w]);
     return fp;
 }
-// Global id of every key that the table already holds, else kNotFound (bounded probing).
+// Global content tables: one slab hash table per level (slab_hash.cuh), warp per key. Lane k < W holds
+// word k of the key; the fingerprint decides the bucket (low bits) and the tag (high 32 bits).
 constexpr uint32_t kNotFound = 0xFFFFFFFFu;
 template <int W>
-__global__ void globalFindKernel(const uint64_t* __restrict__ keys, uint32_t n, const uint64_t* __restrict__ slots, uint64_t capMask,
-    const uint64_t* __restrict__ items, uint32_t* __restrict__ outId, uint32_t* __restrict__ missing, uint32_t* status)
+__device__ __forceinline__ bool warpKey(const uint64_t* __restrict__ keys, uint64_t i, uint64_t& myWord, uint64_t& fp)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    myWord = lane < (uint32_t)W ? keys[i * W + lane] : 0ull;
+    uint64_t k[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        k[w] = __shfl_sync(0xffffffffu, myWord, w);
+    fp = contentFp<W>(k);
+    return true;
+}
+// The global id of every key the table already holds, else kNotFound with missing[i] = 1.
+template <int W>
+__global__ void slabFindKernel(const uint64_t* __restrict__ keys, uint32_t n, SlabPoolView pool, const uint64_t* __restrict__ items,
+    uint32_t* __restrict__ outId, uint32_t* __restrict__ missing, uint32_t* status)
+{
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n)
         return;
-    uint64_t k[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w)
-        k[w] = keys[(uint64_t)i * W + w];
-    const uint64_t fp = contentFp<W>(k);
-    const uint32_t tag = (uint32_t)(fp >> 32);
-    uint64_t slot = fp & capMask;
-    for (uint64_t probe = 0; probe <= capMask; ++probe) {
-        const uint64_t cur = slots[slot];
-        if (cur == kEmptySlot) {
-            outId[i] = kNotFound;
-            missing[i] = 1;
-            return;
-        }
-        if ((uint32_t)(cur >> 32) == tag) {
-            const uint32_t id = (uint32_t)cur;
-            bool eq = true;
-#pragma unroll
-            for (int w = 0; w < W; ++w)
-                eq &= items[(uint64_t)id * W + w] == k[w];
-            if (eq) {
-                outId[i] = id;
-                missing[i] = 0;
-                return;
-            }
-        }
-        slot = (slot + 1) & capMask;
+    uint64_t word, fp;
+    warpKey<W>(keys, i, word, fp);
+    const uint32_t id = slabFind<W>(pool, (uint32_t)fp & (pool.numBuckets - 1), (uint32_t)(fp >> 32), word, items, status);
+    if ((threadIdx.x & 31) == 0) {
+        outId[i] = id;
+        missing[i] = id == kNotFound ? 1u : 0u;
     }
-    setDeviceError(status, TDAG_ERR_TABLE_FULL, 410);
-    outId[i] = kNotFound;
-    missing[i] = 0;
 }
-// Append the missing keys as ids base + rank (rank = order among the missing ones) and insert them.
+// Append the missing keys as ids base + rank (rank = order among the missing ones, so ids follow first
+// appearance) and insert them. done[i] records a finished insertion, so that a rerun after the host
+// grew the slab pool skips it.
 template <int W>
-__global__ void globalAppendKernel(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ missing, const uint32_t* __restrict__ rank,
-    uint64_t base, uint64_t* __restrict__ items, uint64_t* __restrict__ slots, uint64_t capMask, uint32_t* __restrict__ outId, uint32_t* status)
+__global__ void slabAppendKernel(const uint64_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ missing, const uint32_t* __restrict__ rank,
+    uint64_t base, uint64_t* __restrict__ items, SlabPoolView pool, uint32_t* __restrict__ outId, uint32_t* __restrict__ done, uint32_t* status)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !missing[i])
+    const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n || !missing[i] || done[i])
         return;
+    const uint32_t lane = threadIdx.x & 31;
+    uint64_t word, fp;
+    warpKey<W>(keys, i, word, fp);
     const uint64_t id = base + rank[i];
-    uint64_t k[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        k[w] = keys[(uint64_t)i * W + w];
-        items[id * W + w] = k[w];
+    if (lane < (uint32_t)W)
+        items[id * W + lane] = word;
+    if (slabInsert(pool, (uint32_t)fp & (pool.numBuckets - 1), (fp >> 32) << 32 | id, (uint32_t)(i * 0x9E3779B9u), status) && lane == 0) {
+        outId[i] = (uint32_t)id;
+        done[i] = 1;
     }
-    outId[i] = (uint32_t)id;
-    const uint64_t fp = contentFp<W>(k);
-    const uint64_t mine = (fp >> 32) << 32 | id;
-    uint64_t slot = fp & capMask;
-    for (uint64_t probe = 0; probe <= capMask; ++probe) {
-        if (atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine) == kEmptySlot)
-            return;
-        slot = (slot + 1) & capMask;
-    }
-    setDeviceError(status, TDAG_ERR_TABLE_FULL, 411);
 }
+// Reinsert the items [0, count) into a table with more buckets (growth).
 template <int W>
-__global__ void globalRehashKernel(const uint64_t* __restrict__ items, uint64_t count, uint64_t* __restrict__ slots, uint64_t capMask, uint32_t* status)
+__global__ void slabRehashKernel(const uint64_t* __restrict__ items, uint64_t count, SlabPoolView pool, uint32_t* status)
 {
-    const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t id = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (id >= count)
         return;
-    uint64_t k[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w)
-        k[w] = items[id * W + w];
-    const uint64_t fp = contentFp<W>(k);
-    const uint64_t mine = (fp >> 32) << 32 | id;
-    uint64_t slot = fp & capMask;
-    for (uint64_t probe = 0; probe <= capMask; ++probe) {
-        if (atomicCAS((unsigned long long*)&slots[slot], (unsigned long long)kEmptySlot, (unsigned long long)mine) == kEmptySlot)
-            return;
-        slot = (slot + 1) & capMask;
-    }
-    setDeviceError(status, TDAG_ERR_TABLE_FULL, 412);
+    uint64_t word, fp;
+    warpKey<W>(items, id, word, fp);
+    slabInsert(pool, (uint32_t)fp & (pool.numBuckets - 1), (fp >> 32) << 32 | id, (uint32_t)(id * 0x85EBCA77u), status);
 }
 __global__ void composeIdsKernel(const uint32_t* __restrict__ mapping, uint32_t n, const uint32_t* __restrict__ uniqueId, uint32_t* __restrict__ out)
 {
@@ -694,13 +671,96 @@ __global__ void composeIdsKernel(const uint32_t* __restrict__ mapping, uint32_t 
         out[i] = uniqueId[mapping[i]];
 }
 
+// A slab hash table and its pool (slab_hash.cuh).
+struct SlabTable {
+    DevBuf<unsigned long long> slabs;
+    DevBuf<uint32_t> bitmap;
+    uint32_t numBuckets = 0, numSlabs = 0, bitmapWords = 0;
+    SlabPoolView view() const { return SlabPoolView { slabs.get(), numBuckets, numSlabs, bitmap.get(), bitmapWords }; }
+
+    // A table of `buckets` heads (power of two) and `spare` allocatable slabs, all empty.
+    void create(Context& ctx, uint32_t buckets, uint32_t spare)
+    {
+        cudaStream_t s = ctx.stream;
+        numBuckets = buckets;
+        numSlabs = buckets + spare;
+        bitmapWords = (spare + 31) / 32;
+        slabs = DevBuf<unsigned long long>((size_t)numSlabs * 32, s);
+        TDAG_CUDA(cudaMemsetAsync(slabs.get(), 0xFF, (size_t)numSlabs * 32 * 8, s));
+        bitmap = DevBuf<uint32_t>(std::max<uint32_t>(bitmapWords, 1), s);
+        TDAG_CUDA(cudaMemsetAsync(bitmap.get(), 0, (size_t)std::max<uint32_t>(bitmapWords, 1) * 4, s));
+        if (spare % 32) { // bits past the pool's end count as taken
+            const uint32_t tail = ~((1u << (spare % 32)) - 1u);
+            TDAG_CUDA(cudaMemcpyAsync(bitmap.get() + bitmapWords - 1, &tail, 4, cudaMemcpyHostToDevice, s));
+            TDAG_CUDA(cudaStreamSynchronize(s));
+        }
+    }
+    // Twice the allocatable slabs, keeping every slab and its index (chains stay valid).
+    void growPool(Context& ctx)
+    {
+        cudaStream_t s = ctx.stream;
+        const uint32_t spare = numSlabs - numBuckets;
+        TDAG_CHECK((uint64_t)numBuckets + 2ull * std::max<uint32_t>(spare, 32) < 0xFFFFFFF0ull, TDAG_ERR_OOM, "slab pool exceeds 2^32 slabs");
+        SlabTable bigger;
+        bigger.create(ctx, numBuckets, 2 * std::max<uint32_t>(spare, 32));
+        TDAG_CUDA(cudaMemcpyAsync(bigger.slabs.get(), slabs.get(), (size_t)numSlabs * 32 * 8, cudaMemcpyDeviceToDevice, s));
+        if (bitmapWords) {
+            // the old tail word's padding bits were preset; they are real slabs now
+            std::vector<uint32_t> words(bitmapWords);
+            TDAG_CUDA(cudaMemcpyAsync(words.data(), bitmap.get(), (size_t)bitmapWords * 4, cudaMemcpyDeviceToHost, s));
+            TDAG_CUDA(cudaStreamSynchronize(s));
+            if (spare % 32)
+                words.back() &= (1u << (spare % 32)) - 1u;
+            TDAG_CUDA(cudaMemcpyAsync(bigger.bitmap.get(), words.data(), (size_t)bitmapWords * 4, cudaMemcpyHostToDevice, s));
+            TDAG_CUDA(cudaStreamSynchronize(s));
+        }
+        *this = std::move(bigger);
+    }
+};
+
 struct GlobalLevel {
     int words = 1;
     DevBuf<uint64_t> items; // count x words
     uint64_t count = 0;
-    DevBuf<uint64_t> slots;
-    uint64_t cap = 0;
+    SlabTable table;
+    uint32_t poolGrowths = 0, rehashes = 0;
 };
+
+// Buckets for `items` entries: about 8 per bucket (a quarter of a slab), at least 1024.
+uint32_t slabBuckets(uint64_t items)
+{
+    uint64_t b = 1024;
+    while (b * 8 < items)
+        b <<= 1;
+    TDAG_CHECK(b <= (1ull << 31), TDAG_ERR_ARG, "slab table too large");
+    return (uint32_t)b;
+}
+
+// The slab pool starts at tuning.slab_pool_slabs allocatable slabs when set (tests use a tiny pool to
+// exercise the growth path), else at one per bucket.
+uint32_t initialSpare(const Context& ctx, uint32_t buckets) { return ctx.tuning.slab_pool_slabs ? ctx.tuning.slab_pool_slabs : buckets; }
+
+template <int W>
+void rehashInto(Context& ctx, GlobalLevel& g, uint32_t buckets)
+{
+    cudaStream_t s = ctx.stream;
+    for (uint32_t attempt = 0;; ++attempt) {
+        SlabTable t;
+        t.create(ctx, buckets, std::max<uint32_t>(initialSpare(ctx, buckets), 32) << attempt);
+        if (g.count) {
+            slabRehashKernel<W><<<gridFor(g.count * 32, 256), 256, 0, s>>>(g.items.get(), g.count, t.view(), ctx.status);
+            TDAG_LAUNCHED();
+        }
+        uint32_t aux = 0;
+        const uint32_t code = ctx.takeStatus(&aux);
+        if (code == 0) {
+            g.table = std::move(t);
+            return;
+        }
+        TDAG_CHECK(code == TDAG_ERR_ALLOC && attempt < 16, (int)code, "slab table rehash: device reported error " + std::to_string(code));
+        ++g.poolGrowths;
+    }
+}
 
 void reserveGlobal(Context& ctx, GlobalLevel& g, uint64_t incoming)
 {
@@ -714,50 +774,61 @@ void reserveGlobal(Context& ctx, GlobalLevel& g, uint64_t incoming)
             TDAG_CUDA(cudaMemcpyAsync(bigger.get(), g.items.get(), g.count * g.words * 8, cudaMemcpyDeviceToDevice, s));
         g.items = std::move(bigger);
     }
-    if (need * 2 > g.cap) {
-        g.cap = pow2AtLeast(need * 4 + 64);
-        g.slots = DevBuf<uint64_t>(g.cap, s);
-        fillU64(g.slots.get(), kEmptySlot, g.cap, s);
-        if (g.count) {
-            if (g.words == 1)
-                globalRehashKernel<1><<<gridFor(g.count, 256), 256, 0, s>>>(g.items.get(), g.count, g.slots.get(), g.cap - 1, ctx.status);
-            else
-                globalRehashKernel<4><<<gridFor(g.count, 256), 256, 0, s>>>(g.items.get(), g.count, g.slots.get(), g.cap - 1, ctx.status);
-            TDAG_LAUNCHED();
-        }
+    // Chains grow by slabs as items arrive; the bucket array is rebuilt only when chains would average
+    // four slabs (more than 124 items per bucket).
+    if (g.table.numBuckets == 0 || need > (uint64_t)g.table.numBuckets * 124) {
+        const uint32_t buckets = slabBuckets(need);
+        if (g.table.numBuckets)
+            ++g.rehashes;
+        if (g.words == 1)
+            rehashInto<1>(ctx, g, buckets);
+        else
+            rehashInto<4>(ctx, g, buckets);
     }
 }
 
 // Merge n items of one chunk level (keys: n x words, in tree order) into the global level; returns
 // every item's global id.
-DevBuf<uint32_t> mergeLevel(Context& ctx, GlobalLevel& g, const uint64_t* keys, uint32_t n)
+template <int W>
+DevBuf<uint32_t> mergeLevelW(Context& ctx, GlobalLevel& g, const uint64_t* keys, uint32_t n)
 {
     cudaStream_t s = ctx.stream;
     DevBuf<uint32_t> mapping, firsts;
-    const uint32_t u = dedupLevel(ctx, keys, g.words, n, mapping, firsts); // first occurrence within the chunk
-    DevBuf<uint64_t> ukeys((size_t)u * g.words, s);
-    gatherU64Kernel<<<gridFor((size_t)u * g.words, 256), 256, 0, s>>>(keys, firsts.get(), u, g.words, ukeys.get());
+    const uint32_t u = dedupLevel(ctx, keys, W, n, mapping, firsts); // first occurrence within the chunk
+    DevBuf<uint64_t> ukeys((size_t)u * W, s);
+    gatherU64Kernel<<<gridFor((size_t)u * W, 256), 256, 0, s>>>(keys, firsts.get(), u, W, ukeys.get());
     TDAG_LAUNCHED();
     reserveGlobal(ctx, g, u);
-    DevBuf<uint32_t> uid(u, s), missing(u, s), rank(u, s);
-    if (g.words == 1)
-        globalFindKernel<1><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, g.slots.get(), g.cap - 1, g.items.get(), uid.get(), missing.get(), ctx.status);
-    else
-        globalFindKernel<4><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, g.slots.get(), g.cap - 1, g.items.get(), uid.get(), missing.get(), ctx.status);
+    DevBuf<uint32_t> uid(u, s), missing(u, s), rank(u, s), done(u, s);
+    TDAG_CUDA(cudaMemsetAsync(done.get(), 0, (size_t)u * 4, s));
+    slabFindKernel<W><<<gridFor((uint64_t)u * 32, 256), 256, 0, s>>>(ukeys.get(), u, g.table.view(), g.items.get(), uid.get(), missing.get(), ctx.status);
     TDAG_LAUNCHED();
     const uint64_t added = exclusiveScanU32Total(missing.get(), rank.get(), u, s);
-    if (g.words == 1)
-        globalAppendKernel<1><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, missing.get(), rank.get(), g.count, g.items.get(), g.slots.get(), g.cap - 1,
-            uid.get(), ctx.status);
-    else
-        globalAppendKernel<4><<<gridFor(u, 256), 256, 0, s>>>(ukeys.get(), u, missing.get(), rank.get(), g.count, g.items.get(), g.slots.get(), g.cap - 1,
-            uid.get(), ctx.status);
-    TDAG_LAUNCHED();
+    ctx.checkStatus("scene merge: lookup");
+    for (uint32_t attempt = 0;; ++attempt) {
+        slabAppendKernel<W><<<gridFor((uint64_t)u * 32, 256), 256, 0, s>>>(ukeys.get(), u, missing.get(), rank.get(), g.count, g.items.get(),
+            g.table.view(), uid.get(), done.get(), ctx.status);
+        TDAG_LAUNCHED();
+        uint32_t aux = 0;
+        const uint32_t code = ctx.takeStatus(&aux);
+        if (code == 0)
+            break;
+        // the pool ran out: grow it (chains stay valid) and insert what is left
+        TDAG_CHECK(code == TDAG_ERR_ALLOC && attempt < 16, (int)code, "scene merge: device reported error " + std::to_string(code) + " (aux " +
+                std::to_string(aux) + ")");
+        g.table.growPool(ctx);
+        ++g.poolGrowths;
+    }
     g.count += added;
     DevBuf<uint32_t> ids(n, s);
     composeIdsKernel<<<gridFor(n, 256), 256, 0, s>>>(mapping.get(), n, uid.get(), ids.get());
     TDAG_LAUNCHED();
     return ids;
+}
+
+DevBuf<uint32_t> mergeLevel(Context& ctx, GlobalLevel& g, const uint64_t* keys, uint32_t n)
+{
+    return g.words == 1 ? mergeLevelW<1>(ctx, g, keys, n) : mergeLevelW<4>(ctx, g, keys, n);
 }
 
 inline uint32_t log2u(uint32_t v) { return (uint32_t)(31 - __builtin_clz(v)); }

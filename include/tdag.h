@@ -108,7 +108,9 @@ typedef struct tdag_tuning {
                                         * rerun; above 100 the first table is certain to be too small. */
     uint32_t table_regrow_limit; /* doublings allowed per table (default 4); past them the call
                                   * returns TDAG_ERR_TABLE_FULL */
-    uint32_t reserved;
+    uint32_t slab_pool_slabs; /* initial spare slabs of each global slab hash table of the streamed
+                               * scene build (0: one per bucket); a pool that runs out
+                               * (TDAG_ERR_ALLOC on the device) is doubled and the insertion resumed */
     uint64_t device_memory_limit; /* bytes of device memory the context's calls may hold at once
                                    * (0 = no limit); an allocation past it fails with TDAG_ERR_OOM */
 } tdag_tuning;

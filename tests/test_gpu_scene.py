@@ -81,6 +81,22 @@ def test_chunked_scene_equals_single_pass(tdaglib, gpu_ctx, res, chunk, n, seed,
     assert many.voxel_count == one.voxel_count
 
 
+@pytest.mark.parametrize("slabs", [1, 40])
+def test_chunked_scene_with_a_tiny_slab_pool(tdaglib, gpu_ctx, slabs):
+    """The global slab hash tables of the chunked generator start with a pool of 1 or 40 spare slabs,
+    so their chains exhaust it again and again (TDAG_ERR_ALLOC on the device, never a spin); the host
+    doubles the pool and resumes each insertion. The SVDAG is the single-pass one all the same."""
+    base = dict(kind=tdaglib.SCENE_PRIMITIVES, resolution=512, seed=9, num_primitives=300)
+    one = tdaglib.scene_svdag(tdaglib.SceneSpec(**base), to_dag=True, ctx=gpu_ctx)
+    ctx = tdaglib.Context(tuning={"slab_pool_slabs": slabs})
+    try:
+        many = tdaglib.scene_svdag(tdaglib.SceneSpec(**base, chunk_resolution=64), to_dag=True, ctx=ctx)
+        _assert_same(many.to_host(), one.to_host())
+        assert many.voxel_count == one.voxel_count
+    finally:
+        ctx.close()
+
+
 def _covered_bricks(res, prims):
     """32^3 bricks whose 34^3 halo box lies inside one box or ball primitive and inside the grid."""
     from oracle.generator import PERMS
@@ -116,3 +132,15 @@ def test_scene_with_solid_bricks_matches_cpu_generator(oracle, tdaglib, gpu_ctx,
     got = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx)
     _assert_same(got.to_host(), _svo_struct(tdaglib, oracle, dense, True))
     assert got.voxel_count == int(dense.sum())
+
+
+def test_device_scene_equals_cpu_scene_statement(oracle, tdaglib, gpu_ctx):
+    """The device generator and the C++ CPU statement (oracle/scene_oracle.cpp, which builds the CPU
+    baseline's inputs) agree on a 512^3 primitive scene, and a CPU sub-box equals the device grid's
+    subtree at that box."""
+    spec = tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=512, seed=13, num_primitives=400)
+    got = tdaglib.scene_svdag(spec, to_dag=True, ctx=gpu_ctx).to_host()
+    dense = oracle.scene_dense(512, 13, 400)
+    _assert_same(got, _svo_struct(tdaglib, oracle, dense, True))
+    sub = oracle.scene_dense(512, 13, 400, origin=(256, 128, 0), size=128)
+    assert np.array_equal(sub, dense[0:128, 128:256, 256:384])
