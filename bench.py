@@ -74,6 +74,8 @@ def parse_args():
     ap.add_argument("--train-steps", type=int, default=1500, help="proposal: training steps")
     ap.add_argument("--grids", type=int, default=96)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--probe-bulk-copy", type=int, default=0, choices=[0, 1, 2],
+                    help="level-4 probe source staging: 1 = bulk copy (TMA) one source ahead, 0/2 = cooperative loads")
     return ap.parse_args()
 
 
@@ -521,7 +523,7 @@ def run_ours(args, world, rank, local, pg):
 
     dev = local if torch.cuda.is_available() else 0
     torch.cuda.set_device(dev)
-    ctx = tdag.Context(dev)
+    ctx = tdag.Context(dev, {"probe_bulk_copy": args.probe_bulk_copy})
     spec = scene_spec(args)
     g = tdag.scene_svdag(spec, to_dag=True, ctx=ctx)
     voxels = g.voxel_count

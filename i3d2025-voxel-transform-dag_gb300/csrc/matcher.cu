@@ -42,6 +42,40 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// ---------------------------------------------------------------------------- bulk copies (TMA)
+// A 1-D bulk copy (cp.async.bulk, the TMA unit's untiled form) from this GPU's global memory into the
+// CTA's shared memory, completed on an mbarrier: both addresses 16-byte aligned, the size a multiple
+// of 16. No multicast. Every wait is bounded.
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbarInit(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+// Orders this thread's earlier shared-memory accesses (and barrier inits) before later async-proxy ones.
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulkCopyToShared(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smemAddr(dst)), "l"(src),
+        "r"(bytes), "r"(smemAddr(bar))
+        : "memory");
+}
+// Waits until the barrier's phase with the given parity has completed; false after the bound.
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity)
+{
+    const uint32_t a = smemAddr(bar);
+    for (uint32_t i = 0; i < (1u << 20); ++i) {
+        uint32_t done = 0;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
 // The directional box hash. The reference folds every axis with hash_combine and clamps to 1 once
 // started (find_translation.cpp:210-218). Which hash is used does not change the result: a probe only
 // proposes (source, target, transform) candidates, every candidate is verified exactly, and
@@ -945,6 +979,8 @@ struct ProbeParams {
     uint16_t* srcLines; // [end - begin][3][R * R]: every source's lines, for verification
     uint32_t* workCounter;
     unsigned long long* counters; // [0] probes, [1] filter passes
+    uint32_t* status;
+    uint32_t bulkCopy; // level 4: source grids arrive by a bulk copy one source ahead (ProbeShape::TMA)
 };
 
 template <int R>
@@ -964,7 +1000,13 @@ struct ProbeShape {
     static constexpr size_t STAGE_OFF = TEAM_BYTES * TEAMS;
     static constexpr size_t COUNT_OFF = STAGE_OFF + (size_t)(kThreads / 32) * STAGE * 16; // per-warp stage counts
     static constexpr size_t BOX_OFF = COUNT_OFF + (kThreads / 32) * 4; // per team: lo x y z, hi + 1 x y z
-    static constexpr size_t SMEM = BOX_OFF + TEAMS * 24 + 16;
+    static constexpr size_t BASE_OFF = BOX_OFF + TEAMS * 24; // work base (+ 12 spare bytes)
+    // Level 4 (one team per CTA): two 512-byte source-grid buffers filled by bulk copies, and their
+    // two mbarriers, after the work base.
+    static constexpr bool TMA = R == 16;
+    static constexpr size_t PREF_OFF = (BASE_OFF + 16 + 127) & ~(size_t)127;
+    static constexpr size_t MBAR_OFF = PREF_OFF + 2 * W * 8;
+    static constexpr size_t SMEM = TMA ? MBAR_OFF + 16 : BASE_OFF + 16;
     static_assert(STAGE_OFF % 16 == 0 && TEAM_BYTES % 16 == 0, "alignment");
     static_assert(R == 4 || LINES_OFF % 16 == 0, "pass-2 rows are read as 16-byte vectors");
     static_assert(R % CHUNK == 0, "chunks tile a line");
@@ -1017,7 +1059,15 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
     ulonglong2* stage = reinterpret_cast<ulonglong2*>(smem + Sh::STAGE_OFF) + warp * STAGE;
     uint32_t* stageCnt = reinterpret_cast<uint32_t*>(smem + Sh::COUNT_OFF) + warp;
     uint32_t* box = reinterpret_cast<uint32_t*>(smem + Sh::BOX_OFF) + team * 6;
-    uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::SMEM - 16);
+    uint32_t* shBase = reinterpret_cast<uint32_t*>(smem + Sh::BASE_OFF);
+    // bulk-copy prefetch (level 4): buffer it & 1 holds the source of iteration `it`
+    uint64_t* pref = reinterpret_cast<uint64_t*>(smem + (Sh::TMA ? Sh::PREF_OFF : 0));
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + (Sh::TMA ? Sh::MBAR_OFF : 0));
+    const bool bulk = Sh::TMA && p.bulkCopy;
+    auto sourceGrid = [&](uint32_t wi) {
+        const uint32_t r = p.workList ? p.workList[wi] : wi;
+        return p.grids + (size_t)p.order[r] * W;
+    };
     // lanes of this thread's team within its warp (teams of 16 share a warp)
     const unsigned teamMask = TEAM >= 32 ? 0xffffffffu : (((1u << TEAM) - 1u) << (lane & ~(uint32_t)(TEAM - 1)));
     uint32_t cProbe = 0, cFilter = 0;
@@ -1046,8 +1096,20 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
         __syncwarp();
     };
 
-    for (;;) {
-        if (threadIdx.x == 0)
+    if (bulk) {
+        if (threadIdx.x == 0) {
+            mbarInit(&mbar[0], 1);
+            mbarInit(&mbar[1], 1);
+            fenceProxyAsync();
+            const uint32_t first = p.begin + atomicAdd(p.workCounter, 1u);
+            *shBase = first;
+            if (first < p.end)
+                bulkCopyToShared(pref, sourceGrid(first), W * 8, &mbar[0]);
+        }
+        __syncthreads();
+    }
+    for (uint32_t it = 0;; ++it) {
+        if (!bulk && threadIdx.x == 0)
             *shBase = p.begin + atomicAdd(p.workCounter, (uint32_t)TEAMS);
         __syncthreads();
         const uint32_t base = *shBase;
@@ -1055,10 +1117,37 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
         if (base >= p.end)
             break;
         const uint32_t wi = base + team;
-        const bool valid = wi < p.end;
+        bool valid = wi < p.end;
         const uint32_t wIdx = wi - p.begin;
         uint64_t salt = 0;
-        if (valid) {
+        if (bulk) {
+            // claim the next source and start its copy into the other buffer (read last iteration,
+            // before the barriers above), then wait for this source's copy
+            const int b = (int)(it & 1u);
+            bool issued = false;
+            if (threadIdx.x == 0) {
+                const uint32_t next = p.begin + atomicAdd(p.workCounter, 1u);
+                *shBase = next;
+                if (next < p.end) {
+                    fenceProxyAsync();
+                    bulkCopyToShared(pref + (b ^ 1) * W, sourceGrid(next), W * 8, &mbar[b ^ 1]);
+                    issued = true;
+                }
+            }
+            const bool arrived = mbarWait(&mbar[b], (it >> 1) & 1u);
+            if (__syncthreads_or(!arrived)) {
+                // a copy never completed: record it, let the copy just issued land (bounded), stop
+                if (threadIdx.x == 0) {
+                    setDeviceError(p.status, TDAG_ERR_CUDA, 430);
+                    if (issued)
+                        mbarWait(&mbar[b ^ 1], ((it + 1) >> 1) & 1u);
+                }
+                break;
+            }
+            srcW = pref + b * W;
+            if (SALTED)
+                salt = boxSalt(p.gridOf[p.order[p.workList ? p.workList[wi] : wi]]);
+        } else if (valid) {
             const uint32_t r = p.workList ? p.workList[wi] : wi;
             const uint32_t orig = p.order[r];
             const uint64_t* g = p.grids + (size_t)orig * W;
@@ -1741,6 +1830,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         pp.recCount = recCount.get();
         pp.workCounter = work.get();
         pp.counters = counters.get();
+        pp.status = ctx.status;
+        // 1: on, 0 (default) or 2: off; a bulk copy needs a 16-byte aligned source (caller-owned grids may not be)
+        pp.bulkCopy = (ctx.tuning.probe_bulk_copy == 1 && ((uintptr_t)grids & 15u) == 0) ? 1u : 0u;
         LookupParams lp {};
         lp.slots = table.slots.get();
         lp.homeShift = table.homeShift;

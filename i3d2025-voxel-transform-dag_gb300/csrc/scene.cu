@@ -581,11 +581,11 @@ DevPrim toDevPrim(const tdag_primitive& p)
 } // namespace
 
 // ------------------------------------------------------------------------------------------------
-// Streamed scene build for grids whose leaf array does not fit (SURVEY config 4, 16384^3): the grid
+// Streamed scene build for grids whose leaf array does not fit (16384^3 and other grids above 4096^3): the grid
 // is generated in chunks of chunkRes^3 voxels in Morton order of the chunks. Every chunk gets its own
 // SVO (levels 2..log2(chunkRes)), is deduplicated within itself (first occurrence), and its unique
-// items are merged level by level into global content tables that number items in order of first
-// appearance. The level sequences of the whole tree are the chunks' sequences concatenated in chunk
+// items are merged level by level into global content tables -- slab hash tables whose chains grow by
+// slabs from a bitmap allocator (slab_hash.cuh) -- that number items in order of first appearance. The level sequences of the whole tree are the chunks' sequences concatenated in chunk
 // Morton order (the depth-first Morton traversal visits chunks in that order), so the global
 // numbering is exactly toDAG's first-occurrence numbering of the full tree. Levels above the chunks
 // are built from the chunks' root ids on the host (at most (res/chunkRes)^3 entries).

@@ -113,6 +113,9 @@ typedef struct tdag_tuning {
                                * (TDAG_ERR_ALLOC on the device) is doubled and the insertion resumed */
     uint64_t device_memory_limit; /* bytes of device memory the context's calls may hold at once
                                    * (0 = no limit); an allocation past it fails with TDAG_ERR_OOM */
+    uint32_t probe_bulk_copy; /* level-4 probe: 1 stages the source grids by a bulk copy (TMA) one
+                               * source ahead; 0 (default) or 2 load them cooperatively */
+    uint32_t reserved2;
 } tdag_tuning;
 
 /* Library/version information. */
