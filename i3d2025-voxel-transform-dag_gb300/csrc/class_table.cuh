@@ -51,6 +51,10 @@ __global__ void __launch_bounds__(256) classInsertKernel(const uint64_t* __restr
         }
         slot = (slot + 1) & capMask;
     }
+    // Every slot is claimed (the probe visited all of them): name the home slot, whose class minimum
+    // is a valid item, so that the kernels reading slotOf before the host sees the status stay in
+    // bounds. The pass's results are discarded and it is rerun with a larger table.
+    slotOf[i] = (uint32_t)(fp & capMask);
     setDeviceError(status, TDAG_ERR_TABLE_FULL, 100);
 }
 

@@ -265,6 +265,8 @@ inline unsigned gridFor(size_t n, unsigned block) { return (unsigned)((n + block
 // Primitives (primitives.cu): exclusive scan of u32, stable LSD radix sort of (u64 key, u32 value).
 // ------------------------------------------------------------------------------------------------
 void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
+// 64 bytes of pinned host memory owned by the calling host thread, for small device-to-host readbacks.
+uint64_t* pinnedScratch();
 // Returns total (sum of in) by copying the last element; synchronises the stream.
 uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
 void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s);

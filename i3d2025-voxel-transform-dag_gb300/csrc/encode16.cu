@@ -173,21 +173,26 @@ uint32_t referenceCountOrder(const std::vector<uint32_t>& counts, std::vector<ui
 
 // The distinct child pointers of a level in the reference's order (transform_dag_encoding.cpp:276-295):
 // counted in a std::unordered_map in node order, children 0..7, then iterated and std::sort-ed by
-// count, descending. `instances` are the level's child pointers in that order (remapped to the
-// encoded child level). Node storage comes from an arena; the iteration order of libstdc++'s map
-// depends on the hash codes, the insertion sequence and its rehash policy, not on the allocator.
-std::vector<uint64_t> referencePointerOrder(const std::vector<uint64_t>& instances)
+// count, descending. The map's iteration order depends only on which keys it holds when, i.e. on the
+// sequence of first occurrences and their hash codes: a repeated key changes nothing but its count.
+// So the device hands over the distinct pointers in first-occurrence order (values, counts, run ids)
+// and the host inserts each once, into the same container with the same hash, and sorts the same
+// way; std::sort's moves depend only on its comparisons, so sorting (count, run id) pairs permutes
+// exactly as the reference's (count, pointer) pairs. Node storage comes from an arena: the iteration
+// order does not depend on the allocator. Returns the run ids in the reference's order.
+std::vector<uint32_t> referencePointerOrder(const std::vector<uint64_t>& firstValues, const std::vector<uint32_t>& firstRuns,
+    const std::vector<uint32_t>& runCount)
 {
-    std::pmr::monotonic_buffer_resource arena(instances.size() * 48 + 4096);
-    std::pmr::unordered_map<uint64_t, uint32_t, ReferencePointerHash> counts(&arena);
-    for (uint64_t tp : instances)
-        counts[tp]++;
-    std::vector<std::pair<uint32_t, uint64_t>> byCount;
-    byCount.reserve(counts.size());
-    for (const auto& [tp, n] : counts)
-        byCount.push_back({ n, tp });
+    std::pmr::monotonic_buffer_resource arena(firstValues.size() * 48 + 4096);
+    std::pmr::unordered_map<uint64_t, uint32_t, ReferencePointerHash> runOf(&arena);
+    for (size_t k = 0; k < firstValues.size(); ++k)
+        runOf[firstValues[k]] = firstRuns[k];
+    std::vector<std::pair<uint32_t, uint32_t>> byCount; // (count, run)
+    byCount.reserve(runOf.size());
+    for (const auto& [tp, run] : runOf)
+        byCount.push_back({ runCount[run], run });
     std::sort(byCount.begin(), byCount.end(), [](const auto& l, const auto& r) { return l.first > r.first; });
-    std::vector<uint64_t> out(byCount.size());
+    std::vector<uint32_t> out(byCount.size());
     for (size_t i = 0; i < byCount.size(); ++i)
         out[i] = byCount[i].second;
     return out;
@@ -508,6 +513,24 @@ __global__ void nodeWriteKernel(const uint64_t* __restrict__ nodes, uint32_t n, 
     stream[off[i]] = (uint16_t)mask;
 }
 
+// Per run (distinct pointer, runs in ascending value): the slot of its first occurrence as a sort key
+// (the stable value sort keeps equal values in slot order) and the run id as the value.
+__global__ void firstOccurrenceKeysKernel(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ runStart, uint32_t u, uint64_t* __restrict__ keys,
+    uint32_t* __restrict__ runIds)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= u)
+        return;
+    keys[r] = vals[runStart[r]];
+    runIds[r] = r;
+}
+__global__ void gatherValuesKernel(const uint64_t* __restrict__ runVal, const uint32_t* __restrict__ runIds, uint32_t u, uint64_t* __restrict__ out)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < u)
+        out[k] = runVal[runIds[k]];
+}
+
 __global__ void scatterRankKernel(const uint32_t* __restrict__ byCount, uint32_t u, uint32_t* __restrict__ rankOfRun)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -549,7 +572,7 @@ DevBuf<uint64_t> sortByReferenceCount(Context& c, const DevBuf<uint64_t>& items,
     if (referenceTies) {
         std::vector<uint32_t> hostCounts(count), order;
         if (count)
-            TDAG_CUDA(cudaMemcpyAsync(hostCounts.data(), counts.get(), count * 4, cudaMemcpyDeviceToHost, s));
+            downloadStaged(c, { { hostCounts.data(), counts.get(), (size_t)count * 4 } });
         c.checkStatus("encode16: reference counts");
         k = referenceCountOrder(hostCounts, order);
         if (k) {
@@ -664,14 +687,9 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
         DevBuf<uint32_t> vals(std::max<uint32_t>(m, 1), s), runFlag(std::max<uint32_t>(m, 1), s), runScan(std::max<uint32_t>(m, 1), s);
         DevBuf<uint32_t> slotRun(std::max<uint64_t>(slots, 1), s);
         uint32_t u = 0;
-        std::vector<uint64_t> instances; // the level's child pointers in node order (reference ties)
         if (m) {
             instanceKeysKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(nodes[l].get(), instSlots.get(), m, keys.get(), vals.get());
             TDAG_LAUNCHED();
-            if (referenceTies) {
-                instances.resize(m);
-                TDAG_CUDA(cudaMemcpyAsync(instances.data(), keys.get(), (uint64_t)m * 8, cudaMemcpyDeviceToHost, s));
-            }
             radixSortPairs(keys.get(), vals.get(), m, 0, 64, s);
             runFlagsKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(keys.get(), m, runFlag.get());
             TDAG_LAUNCHED();
@@ -687,15 +705,19 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
             runCountKeysKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(runStart.get(), u, m, m, runCount.get(), countKeys.get(), byCount.get());
             TDAG_LAUNCHED();
             if (referenceTies) {
-                // Runs are numbered in ascending pointer value; name the reference's order by run.
-                std::vector<uint64_t> values(u);
-                TDAG_CUDA(cudaMemcpyAsync(values.data(), runVal.get(), (uint64_t)u * 8, cudaMemcpyDeviceToHost, s));
+                // the distinct pointers in first-occurrence order (runs are numbered by ascending value)
+                firstOccurrenceKeysKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(vals.get(), runStart.get(), u, countKeys.get(), byCount.get());
+                TDAG_LAUNCHED();
+                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(slots)), s);
+                gatherValuesKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(runVal.get(), byCount.get(), u, countKeys.get());
+                TDAG_LAUNCHED();
+                std::vector<uint64_t> firstValues(u);
+                std::vector<uint32_t> firstRuns(u), counts(u);
+                downloadStaged(c, { { firstValues.data(), countKeys.get(), (size_t)u * 8 }, { firstRuns.data(), byCount.get(), (size_t)u * 4 },
+                                      { counts.data(), runCount.get(), (size_t)u * 4 } });
                 c.checkStatus("encode16: distinct pointers");
-                const std::vector<uint64_t> order = referencePointerOrder(instances);
-                TDAG_CHECK(order.size() == u, TDAG_ERR_CUDA, "encode16: distinct pointer counts disagree");
-                std::vector<uint32_t> runOrder(u);
-                for (uint32_t k = 0; k < u; ++k)
-                    runOrder[k] = (uint32_t)(std::lower_bound(values.begin(), values.end(), order[k]) - values.begin());
+                const std::vector<uint32_t> runOrder = referencePointerOrder(firstValues, firstRuns, counts);
+                TDAG_CHECK(runOrder.size() == u, TDAG_ERR_CUDA, "encode16: distinct pointer counts disagree");
                 TDAG_CUDA(cudaMemcpyAsync(byCount.get(), runOrder.data(), (uint64_t)u * 4, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s)); // `runOrder` is released at the end of this scope
             } else {

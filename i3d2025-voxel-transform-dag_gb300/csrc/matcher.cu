@@ -1574,8 +1574,10 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
         TDAG_LAUNCHED();
         tileMaxScanKernel<<<1, kPlaceThreads, 0, s>>>(tileMax.get(), tiles, maxAll.get());
         TDAG_LAUNCHED();
-        TDAG_CUDA(cudaMemcpyAsync(&maxHomeMinusIndex, maxAll.get(), 8, cudaMemcpyDeviceToHost, s));
+        uint64_t* h = pinnedScratch();
+        TDAG_CUDA(cudaMemcpyAsync(h, maxAll.get(), 8, cudaMemcpyDeviceToHost, s));
         TDAG_CUDA(cudaStreamSynchronize(s));
+        maxHomeMinusIndex = (long long)h[0];
     }
     // last run at runs - 1 + max(home - index); probes start at homes up to cap - 1; one empty slot after both
     const uint64_t slotCount = std::max<uint64_t>(cap, runs ? (uint64_t)((long long)runs + maxHomeMinusIndex) : 0) + 1;
@@ -1876,8 +1878,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 probe<<<blocks, kThreads, smem, s>>>(pp);
                 TDAG_LAUNCHED();
                 TDAG_CUDA(cudaEventRecord(ctx.ev[6], s));
-                TDAG_CUDA(cudaMemcpyAsync(&produced, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
+                uint64_t* hp = pinnedScratch();
+                TDAG_CUDA(cudaMemcpyAsync(hp, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
+                produced = hp[0];
                 {
                     float pm = 0; // the stream was synchronised for the record count
                     TDAG_CUDA(cudaEventElapsedTime(&pm, ctx.ev[5], ctx.ev[6]));

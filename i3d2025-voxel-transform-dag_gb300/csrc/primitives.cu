@@ -111,16 +111,26 @@ void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t 
     TDAG_LAUNCHED();
 }
 
+// 64 pinned host bytes per host thread for small readbacks (counts, totals): asynchronous copies
+// and one stream synchronisation, instead of staged pageable copies.
+uint64_t* pinnedScratch()
+{
+    thread_local uint64_t* words = nullptr;
+    if (!words)
+        TDAG_CUDA(cudaHostAlloc((void**)&words, 64, cudaHostAllocPortable));
+    return words;
+}
+
 uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s)
 {
     if (n == 0)
         return 0;
     exclusiveScanU32(in, out, n, s);
-    uint32_t lastIn = 0, lastOut = 0;
-    TDAG_CUDA(cudaMemcpyAsync(&lastIn, in + n - 1, 4, cudaMemcpyDeviceToHost, s));
-    TDAG_CUDA(cudaMemcpyAsync(&lastOut, out + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    uint32_t* pair = reinterpret_cast<uint32_t*>(pinnedScratch());
+    TDAG_CUDA(cudaMemcpyAsync(&pair[0], in + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    TDAG_CUDA(cudaMemcpyAsync(&pair[1], out + n - 1, 4, cudaMemcpyDeviceToHost, s));
     TDAG_CUDA(cudaStreamSynchronize(s));
-    return (uint64_t)lastIn + lastOut;
+    return (uint64_t)pair[0] + pair[1];
 }
 
 namespace {

@@ -43,7 +43,7 @@ def test_full_class_tables_are_regrown_with_identical_output(tdaglib, case):
     try:
         got, stats = _build(tdaglib, ctx, svo)
         assert got == ref
-        assert stats["table_regrows"] >= 2  # 400 % -> 200 % -> 100 % at least, on several levels
+        assert stats["table_regrows"] >= 1  # a table of a quarter of the items' slots cannot hold every class
         # toDAG's class tables take the same path
         sv = tdaglib.svdag_from_dense(dense, ctx=ctx)
         assert sv.to_host().to_svo_bytes() == svo
