@@ -104,37 +104,51 @@ uint64_t Context::classTableCapacity(uint64_t n) const
 }
 
 namespace {
-std::mutex g_budgetMutex;
-std::unordered_map<cudaStream_t, std::shared_ptr<MemoryBudget>> g_budgets;
-std::atomic<bool> g_anyBudget { false };
+std::mutex g_streamMutex;
+std::unordered_map<cudaStream_t, std::weak_ptr<StreamState>> g_streams;
 }
 
-std::shared_ptr<MemoryBudget> budgetOf(cudaStream_t stream)
+StreamState::~StreamState()
 {
-    if (!g_anyBudget.load(std::memory_order_acquire))
+    if (stream)
+        cudaStreamDestroy(stream);
+}
+
+std::shared_ptr<StreamState> streamStateOf(cudaStream_t stream)
+{
+    // one cached entry per host thread spares the lock on the hot path (many buffers per build)
+    thread_local cudaStream_t lastStream = nullptr;
+    thread_local std::weak_ptr<StreamState> lastState;
+    if (stream && stream == lastStream)
+        if (auto st = lastState.lock())
+            return st;
+    std::lock_guard<std::mutex> lock(g_streamMutex);
+    const auto it = g_streams.find(stream);
+    if (it == g_streams.end())
         return nullptr;
-    std::lock_guard<std::mutex> lock(g_budgetMutex);
-    const auto it = g_budgets.find(stream);
-    return it == g_budgets.end() ? nullptr : it->second;
+    auto st = it->second.lock();
+    lastStream = stream;
+    lastState = st;
+    return st;
 }
 
-void registerBudget(cudaStream_t stream, uint64_t limit)
+std::shared_ptr<StreamState> registerStream(cudaStream_t stream, uint64_t limit)
 {
-    std::lock_guard<std::mutex> lock(g_budgetMutex);
-    auto b = std::make_shared<MemoryBudget>();
-    b->limit = limit;
-    g_budgets[stream] = std::move(b);
-    g_anyBudget.store(true, std::memory_order_release);
+    auto st = std::make_shared<StreamState>();
+    st->stream = stream;
+    st->limit = limit;
+    std::lock_guard<std::mutex> lock(g_streamMutex);
+    g_streams[stream] = st;
+    return st;
 }
 
-void unregisterBudget(cudaStream_t stream)
+void unregisterStream(cudaStream_t stream)
 {
-    std::lock_guard<std::mutex> lock(g_budgetMutex);
-    g_budgets.erase(stream);
-    g_anyBudget.store(!g_budgets.empty(), std::memory_order_release);
+    std::lock_guard<std::mutex> lock(g_streamMutex);
+    g_streams.erase(stream);
 }
 
-void chargeBudget(MemoryBudget& b, uint64_t bytes)
+void chargeBudget(StreamState& b, uint64_t bytes)
 {
     const uint64_t before = b.used.fetch_add(bytes);
     if (before + bytes > b.limit) {
@@ -624,8 +638,7 @@ int tdag_ctx_create(int device, const tdag_tuning* tuning, tdag_ctx** out)
         if (tuning)
             c.tuning = *tuning;
         TDAG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-        if (c.tuning.device_memory_limit)
-            registerBudget(c.stream, c.tuning.device_memory_limit);
+        c.streamState = registerStream(c.stream, c.tuning.device_memory_limit);
         cudaMemPool_t pool;
         TDAG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
         uint64_t threshold = ~0ull;
@@ -670,8 +683,11 @@ int tdag_ctx_destroy(tdag_ctx* ctx)
     if (c.stage)
         cudaFreeHost(c.stage);
     if (c.stream) {
-        unregisterBudget(c.stream);
-        cudaStreamDestroy(c.stream);
+        // the stream goes with the last buffer allocated on it (results may outlive the context)
+        unregisterStream(c.stream);
+        if (!c.streamState)
+            cudaStreamDestroy(c.stream);
+        c.streamState.reset();
     }
     delete ctx;
     return TDAG_OK;

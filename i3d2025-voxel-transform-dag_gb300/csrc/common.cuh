@@ -184,19 +184,23 @@ struct TransformTables {
 const TransformTables& hostTables();
 
 // ------------------------------------------------------------------------------------------------
-// Device-memory budgets (tdag_tuning.device_memory_limit). A context created with a limit registers
-// its stream; every DevBuf allocated on that stream is charged to the budget until it is released,
-// and an allocation that would pass the limit throws TDAG_ERR_OOM before reaching the driver. The
-// budget is shared by the buffers charged to it, so results that outlive their context stay valid.
+// Context streams and device-memory budgets. A context's stream is owned by a StreamState that every
+// buffer allocated on the stream shares, so buffers and results that outlive their context (and free
+// themselves later) still free on a live stream; the stream is destroyed with its last user. A
+// context created with tdag_tuning.device_memory_limit also charges every such buffer to its budget
+// until the buffer is released; an allocation that would pass the limit throws TDAG_ERR_OOM before
+// reaching the driver.
 // ------------------------------------------------------------------------------------------------
-struct MemoryBudget {
-    uint64_t limit = 0;
+struct StreamState {
+    cudaStream_t stream = nullptr;
+    uint64_t limit = 0; // 0: no budget
     std::atomic<uint64_t> used { 0 };
+    ~StreamState(); // destroys the stream (its pending work completes first)
 };
-std::shared_ptr<MemoryBudget> budgetOf(cudaStream_t stream); // null: no limit on this stream
-void registerBudget(cudaStream_t stream, uint64_t limit);
-void unregisterBudget(cudaStream_t stream);
-void chargeBudget(MemoryBudget& b, uint64_t bytes); // throws TDAG_ERR_OOM past the limit
+std::shared_ptr<StreamState> streamStateOf(cudaStream_t stream); // null: a stream no context owns
+std::shared_ptr<StreamState> registerStream(cudaStream_t stream, uint64_t limit);
+void unregisterStream(cudaStream_t stream);
+void chargeBudget(StreamState& st, uint64_t bytes); // throws TDAG_ERR_OOM past the limit
 
 // ------------------------------------------------------------------------------------------------
 // Small device-memory helpers (stream-ordered allocations from the context's pool).
@@ -206,23 +210,22 @@ struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
     cudaStream_t s = 0;
-    std::shared_ptr<MemoryBudget> budget; // set when the stream has a device-memory limit
+    std::shared_ptr<StreamState> owner; // keeps the stream alive; carries the context's budget
     DevBuf() = default;
     DevBuf(size_t count, cudaStream_t stream)
         : n(count)
         , s(stream)
     {
         if (count) {
-            if (auto b = budgetOf(stream)) {
-                chargeBudget(*b, count * sizeof(T));
-                budget = std::move(b);
-            }
+            owner = streamStateOf(stream);
+            if (owner && owner->limit)
+                chargeBudget(*owner, count * sizeof(T));
             const cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), stream);
             if (e != cudaSuccess) {
                 p = nullptr;
-                if (budget)
-                    budget->used -= count * sizeof(T);
-                budget.reset();
+                if (owner && owner->limit)
+                    owner->used -= count * sizeof(T);
+                owner.reset();
                 TDAG_CUDA(e);
             }
         }
@@ -237,7 +240,7 @@ struct DevBuf {
             p = o.p;
             n = o.n;
             s = o.s;
-            budget = std::move(o.budget);
+            owner = std::move(o.owner);
             o.p = nullptr;
             o.n = 0;
         }
@@ -248,10 +251,10 @@ struct DevBuf {
     {
         if (p) {
             cudaFreeAsync(p, s);
-            if (budget)
-                budget->used -= n * sizeof(T);
+            if (owner && owner->limit)
+                owner->used -= n * sizeof(T);
         }
-        budget.reset();
+        owner.reset();
         p = nullptr;
         n = 0;
     }

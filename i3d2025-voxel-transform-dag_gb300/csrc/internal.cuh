@@ -23,6 +23,7 @@ struct Context {
 
     uint32_t tableRegrows = 0; // class-table doublings of the current build
     unsigned char* noAllocScratch = nullptr; // device address of the no-allocation matcher's array
+    std::shared_ptr<StreamState> streamState; // owns `stream` together with the buffers allocated on it
 
     // Synchronise the stream, read the device status word, throw on a recorded error.
     void checkStatus(const std::string& where);
