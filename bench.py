@@ -178,9 +178,18 @@ def run_batch(args, world, rank, local, pg):
     dev = local if torch.cuda.is_available() else 0
     torch.cuda.set_device(dev)
     ctx = tdag.Context(dev)
-    specs = batch_specs(args.grids, args.seed + rank)
+    # the batch's grids are independent: rank r builds grids r, r + N, ... of the same seeded set
+    all_specs = batch_specs(args.grids, args.seed)
+    specs = all_specs[rank::world]
     devs = [tdag.scene_svdag(sp, to_dag=True, ctx=ctx) for sp in specs]
     voxels = sum(d.voxel_count for d in devs)
+    if pg is not None:
+        import torch as _t
+        tv = _t.tensor([float(voxels)], dtype=_t.float64, device=f"cuda:{dev}")
+        pg.all_reduce(tv)
+        total_voxels = int(tv.item())
+    else:
+        total_voxels = voxels
     cfg = tdag.TransformDAGConfig()
     tuning, tune_ms, table = ({}, None, [])
     if not args.no_autotune:
@@ -216,13 +225,14 @@ def run_batch(args, world, rank, local, pg):
         single.free()
         r.free()
     dev_ms = max_over_ranks(pg, dev_ms)
-    value = replica_value(voxels, args.steps, world, dev_ms / 1e3)
+    value = total_voxels * args.steps / (dev_ms / 1e3) / 1e6  # the whole batch over the slowest rank's time
     out = {
         "metric": "TDAG batched build Mvoxels/s", "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic (device-generated primitive scenes)",
-        "config": {"workload": f"{len(specs)} independent grids, sides log-uniform 128..1024, 0.1-5% shell voxels, one batched build",
-                   "sides": sorted(sp.resolution for sp in specs), "solid_voxels": int(voxels),
+        "config": {"workload": f"{len(all_specs)} independent grids, sides log-uniform 128..1024, 0.1-5% shell voxels, one batched build "
+                               f"per GPU over its share of the grids (grid i on rank i mod {world})",
+                   "sides": sorted(sp.resolution for sp in all_specs), "solid_voxels": int(total_voxels),
                    "l2": "inputs resident; no flush (each step re-reads the whole batch)"},
         "autotune": {"chosen": tuning, "candidates": [{"tuning": t, "ms": m} for t, m in table]},
         "bit_exact_vs_per_grid": bool(exact),

@@ -1,7 +1,8 @@
 """Autotuner for batched Transform-DAG builds.
 
-Sweeps the knobs of libtdag.so's tdag_tuning — the corner-hash table load factor, the membership
-filter density (bits per distinct key) and the number of persistent search CTAs per SM — on a given
+Sweeps the knobs of libtdag.so's tdag_tuning — the corner-hash table load factor (50-85 %), the
+membership filter density (bits per distinct key), the number of persistent probe CTAs per SM and the
+level-4 probe's source staging (bulk copy or cooperative loads) — on a given
 batch, checks that every configuration gives the same result (the build is exact, so any difference
 is a bug), and returns the fastest. Timings are the library's own CUDA-event device times.
 """
@@ -14,9 +15,10 @@ from typing import Dict, List, Optional, Sequence, Tuple
 import tdag
 
 DEFAULT_SPACE = {
-    "table_load_percent": (50, 70),
+    "table_load_percent": (50, 70, 85),
     "filter_bits_per_key": (16, 32),
-    "search_ctas_per_sm": (2, 3, 4),
+    "search_ctas_per_sm": (3, 4),
+    "probe_bulk_copy": (1, 2),
 }
 
 

@@ -59,3 +59,20 @@ def test_two_gloo_replicas_agree_on_the_slowest_rank():
         assert world == 2
         assert slowest == 2.5  # max over ranks
         assert value == pytest.approx(1_000_000 * 3 * 2 / 2.5 / 1e6)  # whole-job voxels over the slowest time
+
+
+def test_batch_grids_are_partitioned_by_rank():
+    """bench.py --workload batch96 on N GPUs: rank r builds grids r, r + N, ... of one seeded set, so
+    the shares are disjoint and cover the whole batch (no data-path collective; only the timing and
+    the voxel total are reduced)."""
+    import sys
+    from conftest import REPO
+    if REPO not in sys.path:
+        sys.path.insert(0, REPO)
+    import bench
+    specs = bench.batch_specs(96, 1)
+    for world in (1, 2, 4, 8):
+        shares = [specs[r::world] for r in range(world)]
+        seeds = [sp.seed for sh in shares for sp in sh]
+        assert sorted(seeds) == sorted(sp.seed for sp in specs) and len(set(seeds)) == 96
+        assert max(len(sh) for sh in shares) - min(len(sh) for sh in shares) <= 1
