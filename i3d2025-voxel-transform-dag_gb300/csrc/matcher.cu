@@ -60,6 +60,37 @@ __device__ __forceinline__ void bulkCopyToShared(void* dst, const void* src, uin
         "r"(bytes), "r"(smemAddr(bar))
         : "memory");
 }
+// L2 eviction-priority hints (per instruction; no cache state outlives the kernel). The level-4
+// probe marks its membership-filter loads evict-last and its streamed stores (survivor records and
+// the sources' line orientations, hundreds of MB per build) evict-first, so that they do not push
+// the filter out of L2.
+__device__ __forceinline__ uint64_t l2PolicyEvictLast()
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint64_t l2PolicyEvictFirst()
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint32_t ldL2Hint(const uint32_t* p, uint64_t pol)
+{
+    uint32_t v;
+    asm volatile("ld.global.cg.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void stL2Hint(ulonglong2* p, ulonglong2 v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.v2.u64 [%0], {%1, %2}, %3;" ::"l"(p), "l"(v.x), "l"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void stL2Hint(uint16_t* p, uint16_t v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.u16 [%0], %1, %2;" ::"l"(p), "h"(v), "l"(pol) : "memory");
+}
+
 // Waits until the barrier's phase with the given parity has completed; false after the bound.
 __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity)
 {
@@ -1074,6 +1105,11 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
     if (lane == 0)
         *stageCnt = 0;
     __syncwarp();
+    uint64_t polLast = 0, polFirst = 0; // L2 hints of level 4
+    if constexpr (R == 16) {
+        polLast = l2PolicyEvictLast();
+        polFirst = l2PolicyEvictFirst();
+    }
 
     // Warp-uniform: copy the staged records (at most STAGE; reservations past it were written
     // directly by their lanes) to the record list.
@@ -1089,7 +1125,10 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
         g = __shfl_sync(0xffffffffu, g, 0);
         for (uint32_t i = lane; i < nrec; i += 32)
             if (g + i < p.recCap)
-                p.recs[g + i] = stage[i];
+                if constexpr (R == 16)
+                    stL2Hint(&p.recs[g + i], stage[i], polFirst);
+                else
+                    p.recs[g + i] = stage[i];
         __syncwarp();
         if (lane == 0)
             *stageCnt = 0;
@@ -1175,9 +1214,15 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
             }
             xLines[tl] = (uint16_t)lx;
             uint16_t* dst = p.srcLines + (size_t)wIdx * 3 * R * R; // all three orientations, for verification
-            dst[tl] = (uint16_t)lx;
-            dst[R * R + tl] = (uint16_t)ly;
-            dst[2 * R * R + tl] = (uint16_t)lz;
+            if constexpr (R == 16) { // read back only for the sources that reach a verification
+                stL2Hint(&dst[tl], (uint16_t)lx, polFirst);
+                stL2Hint(&dst[R * R + tl], (uint16_t)ly, polFirst);
+                stL2Hint(&dst[2 * R * R + tl], (uint16_t)lz, polFirst);
+            } else {
+                dst[tl] = (uint16_t)lx;
+                dst[R * R + tl] = (uint16_t)ly;
+                dst[2 * R * R + tl] = (uint16_t)lz;
+            }
             // bounding box: lowest set coordinate and highest + 1 along every axis
             const uint32_t l3[3] = { lx, ly, lz };
 #pragma unroll
@@ -1248,7 +1293,7 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
                                 // level 4: box contents rarely repeat, so filter words bypass L1; the small
                                 // boxes of levels 2-3 repeat often enough to hit in it
                                 const uint32_t* fw = &p.filter[filterWordIndex(x, p.filterShift)];
-                                word[c] = ((nonEmpty >> c) & 1u) ? (R == 16 ? __ldcg(fw) : __ldg(fw)) : 0u;
+                                word[c] = ((nonEmpty >> c) & 1u) ? (R == 16 ? ldL2Hint(fw, polLast) : __ldg(fw)) : 0u;
                             }
                             uint32_t hit = 0;
 #pragma unroll
@@ -1271,7 +1316,13 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
                                         if (o < (uint32_t)STAGE)
                                             stage[o] = rec;
                                         else if (g < p.recCap)
-                                            p.recs[g++] = rec;
+                                        {
+                                            if constexpr (R == 16)
+                                                stL2Hint(&p.recs[g], rec, polFirst);
+                                            else
+                                                p.recs[g] = rec;
+                                            ++g;
+                                        }
                                         else
                                             ++g;
                                         ++o;
