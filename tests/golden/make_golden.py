@@ -85,6 +85,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--scene2048", default="")
     ap.add_argument("--scene2048-reference", action="store_true")
+    ap.add_argument("--keep-small", action="store_true", help="keep the small cases' digests as they are")
+    ap.add_argument("--reuse-oracle", action="store_true", help="keep scene2048's oracle digests when its .svo is unchanged")
     args = ap.parse_args()
     path = os.path.join(HERE, "golden.json")
     golden = json.load(open(path)) if os.path.exists(path) else {}
@@ -95,7 +97,7 @@ def main():
         "terrain256": (generator.terrain(256, 1), "oracle/generator.py terrain(256, seed=1), SVO -> toDAG"),
         "blocky128": (blocky_grid(128, 3), "tests/helpers.py blocky_grid(128, seed=3), SVO -> toDAG"),
     }
-    for key, (dense, what) in small.items():
+    for key, (dense, what) in ([] if args.keep_small else small.items()):
         svo = orc.to_dag(orc.svo_from_dense(dense))
         g = dict(oracle_case(svo), input=what)
         if have_ref:
@@ -106,7 +108,11 @@ def main():
         golden[key] = g
     if args.scene2048:
         svo = open(args.scene2048, "rb").read()
-        g = dict(oracle_case(svo), input="tdag.scene_svdag(SceneSpec(kind=PRIMITIVES, resolution=2048, seed=1, num_primitives=4000), to_dag=True)")
+        old = golden.get("scene2048", {})
+        if args.reuse_oracle and old.get("svo_sha256") == digest(svo) and "tdag16_plain_canonical_sha256" in old:
+            g = {k: v for k, v in old.items() if k != "reference"}
+        else:
+            g = dict(oracle_case(svo), input="tdag.scene_svdag(SceneSpec(kind=PRIMITIVES, resolution=2048, seed=1, num_primitives=4000), to_dag=True)")
         if args.scene2048_reference and have_ref:
             g["reference"] = reference_case(svo, variants=())
         elif "reference" in golden.get("scene2048", {}):
