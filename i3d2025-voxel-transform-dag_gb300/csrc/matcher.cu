@@ -1599,14 +1599,16 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
     while ((1ull << log2Cap) < cap)
         ++log2Cap;
     t.homeShift = 64 - log2Cap;
-    // Filter density: 32 bits per key unless the filter would then exceed 64 MB; past that it no longer
-    // stays in L2 (126 MB over two dies, shared with the batch's grids and records), every probe
-    // becomes a DRAM access, and halving the density (down to 8 bits per key) costs less in extra
-    // false-positive lookups than it saves (8192^3 grid: 337 -> 273 ms per build).
+    // Filter density: 32 bits per key unless the filter would then exceed 32 MB; past that a share of
+    // the probes misses L2 (126 MB over two dies, each SM's die caching the lines it reads, shared with
+    // the batch's grids and records), and halving the density (down to 8 bits per key) costs less in
+    // extra false-positive lookups than the misses cost. 2048^3 grid, level-4 probe: 20.2 ms with a
+    // 64 MB filter, 17.8 ms with 32 MB (8.0 GB of DRAM reads per build with 64 MB); 8192^3 grid: 337 ->
+    // 273 ms per build at 8 bits per key.
     uint32_t bitsPerKey = ctx.tuning.filter_bits_per_key;
     if (!bitsPerKey) {
         bitsPerKey = 32;
-        while (bitsPerKey > 8 && pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey)) > (1ull << 29))
+        while (bitsPerKey > 8 && pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey)) > (1ull << 28))
             bitsPerKey /= 2;
     }
     const uint64_t filterBits = pow2AtLeast(std::max<uint64_t>(1024, runs * bitsPerKey));
