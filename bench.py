@@ -116,8 +116,7 @@ def run_proposal(args, world, rank, local, pg):
             sets.append((words, level, P.exhaustive_parents(ctx, words, level, cfg)[0]))
         g.free()
     t_labels = time.perf_counter() - t0
-    torch.manual_seed(0)
-    enc = P.ProposalEncoder().cuda()
+    enc = P.ProposalEncoder(seed=0, ctx=ctx)
     t0 = time.perf_counter()
     losses = P.train(enc, sets, steps=args.train_steps, batch=2048)
     torch.cuda.synchronize()

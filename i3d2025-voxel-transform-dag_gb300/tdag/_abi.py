@@ -133,7 +133,16 @@ EXPORTED = (
     "tdag_device_pool_usage",  # include/tdag_diag.h
     "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
     "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify", "tdag16_raycast",
+    "tdag_nn_gemm", "tdag_nn_block_masks", "tdag_nn_pool_forward", "tdag_nn_pool_backward",  # include/tdag_nn.h
+    "tdag_nn_info_nce", "tdag_nn_column_sums", "tdag_nn_adamw", "tdag_nn_topk", "tdag_nn_sync", "tdag_nn_to_bf16",
 )
+
+# include/tdag_nn.h operand modes
+NN_KMAJOR, NN_MNMAJOR, NN_BITS, NN_BITS_T = 0, 1, 2, 3
+
+
+class NnOperand(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("mode", ctypes.c_uint32), ("ld", ctypes.c_uint32)]
 
 # int (*tdag_proposal_fn)(void* user, uint32_t level, const uint64_t* d_grids, uint32_t n, uint32_t* d_sources, uint32_t* num_sources)
 PROPOSAL_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
@@ -197,6 +206,18 @@ def lib(path: str = None):
         L.tdag16_verify.argtypes = [vp, vp, ctypes.POINTER(SvdagView), ctypes.POINTER(Tdag16VerifyStats)]
         L.tdag16_huffman_code_table.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)]
+        u32, f32 = ctypes.c_uint32, ctypes.c_float
+        L.tdag_nn_gemm.argtypes = [vp, ctypes.POINTER(NnOperand), ctypes.POINTER(NnOperand), u32, u32, u32, f32, vp, ctypes.c_int, vp, u32,
+                                   vp, u32, ctypes.c_int]
+        L.tdag_nn_block_masks.argtypes = [vp, vp, u32, u32, vp]
+        L.tdag_nn_pool_forward.argtypes = [vp, vp, vp, u32, u32, vp, vp, vp, vp]
+        L.tdag_nn_pool_backward.argtypes = [vp, vp, vp, vp, vp, vp, u32, u32, vp]
+        L.tdag_nn_info_nce.argtypes = [vp, vp, u32, vp, vp]
+        L.tdag_nn_column_sums.argtypes = [vp, vp, u32, u32, u32, vp]
+        L.tdag_nn_adamw.argtypes = [vp, vp, vp, vp, vp, ctypes.c_uint64, f32, f32, f32, f32, f32, u32, vp]
+        L.tdag_nn_topk.argtypes = [vp, vp, u32, u32, vp, vp]
+        L.tdag_nn_sync.argtypes = [vp]
+        L.tdag_nn_to_bf16.argtypes = [vp, vp, ctypes.c_uint64, vp]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

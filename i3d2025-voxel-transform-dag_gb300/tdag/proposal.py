@@ -2,24 +2,30 @@
 
 The exhaustive search lets every item of a translation level search as a source. Here an encoder
 embeds every item, each target proposes the k most similar items that precede it in the popcount
-order (dot products of embeddings: bf16 GEMMs on the tensor cores through cuBLAS), and only the
-proposed items search. The library verifies every match exactly (tdag_build_device_proposed,
-tdag_find_duplicates_level_device), so the result is always a valid TDAG. Its node count can only
-grow against the exhaustive build: that growth is the "extra nodes" this mode trades for speed.
+order, and only the proposed items search. The library verifies every match exactly
+(tdag_build_device_proposed, tdag_find_duplicates_level_device), so the result is always a valid
+TDAG. Its node count can only grow against the exhaustive build: that growth is the "extra nodes"
+this mode trades for speed.
 
-Encoder: every 4^3 block of an item -- its 64-bit occupancy mask unpacked to 64 bf16 values, bit
-dx + 4 dy + 16 dz -- goes through an MLP 64 -> 256 -> 256 -> 32 (bf16 GEMMs with FP32 accumulation).
-An item's embedding is the mean over its non-empty blocks ((R/4)^3 = 1, 8, 64 blocks at levels 2, 3,
-4), L2-normalised. Training: InfoNCE over (target, exhaustive parent) pairs from the exhaustive GPU
-matcher with in-batch negatives, AdamW on FP32 master weights.
+Encoder: every 4^3 block of an item -- its 64-bit occupancy mask read as 64 bf16 inputs, bit
+dx + 4 dy + 16 dz -- goes through an MLP 64 -> 256 -> 256 -> 32. An item's embedding is the mean
+over its non-empty blocks ((R/4)^3 = 1, 8, 64 blocks at levels 2, 3, 4), L2-normalised. Training:
+symmetric InfoNCE over (target, exhaustive parent) pairs from the exhaustive GPU matcher with
+in-batch negatives, AdamW on FP32 master weights.
+
+Every arithmetic step runs in the library's own kernels (include/tdag_nn.h): the dense layers
+forward and backward, the InfoNCE logits and the candidate scoring are bf16 GEMMs on the tcgen05
+tensor cores with FP32 accumulation (bias, ReLU and the ReLU gate fused into their epilogues); block
+masks, pooling, the loss, bias gradients and AdamW are plain CUDA kernels. PyTorch only holds the
+device memory and orders the items.
 """
 from __future__ import annotations
 
 import ctypes
+import math
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import torch
-import torch.nn.functional as F
 
 from . import _abi
 from ._abi import lib
@@ -27,50 +33,177 @@ from ._abi import lib
 EMBED_DIM = 32
 HIDDEN = 256
 PTR_MASK = (1 << 37) - 1
+LAYERS = ((HIDDEN, 64), (HIDDEN, HIDDEN), (EMBED_DIM, HIDDEN))  # (out, in) of every dense layer
 
 
-# ------------------------------------------------------------------------------------------------
-# encoder
-# ------------------------------------------------------------------------------------------------
-class ProposalEncoder(torch.nn.Module):
-    """Leaf-block MLP 64 -> 256 -> 256 -> 32 with mean pooling over an item's non-empty 4^3 blocks."""
-
-    def __init__(self):
-        super().__init__()
-        self.l1 = torch.nn.Linear(64, HIDDEN)
-        self.l2 = torch.nn.Linear(HIDDEN, HIDDEN)
-        self.l3 = torch.nn.Linear(HIDDEN, EMBED_DIM)
-
-    def blocks(self, x: torch.Tensor) -> torch.Tensor:
-        return self.l3(F.relu(self.l2(F.relu(self.l1(x)))))
-
-    def forward(self, words: torch.Tensor, level: int) -> torch.Tensor:
-        x = unpack_blocks(words, level)  # (n, B, 64) in {0, 1}
-        nonempty = (x.amax(dim=-1) > 0).to(torch.float32)  # (n, B)
-        with torch.autocast(device_type=x.device.type, dtype=torch.bfloat16, enabled=x.is_cuda):
-            h = self.blocks(x.to(torch.bfloat16 if x.is_cuda else torch.float32))
-        h = h.float() * nonempty.unsqueeze(-1)
-        e = h.sum(dim=1) / nonempty.sum(dim=1).clamp(min=1.0).unsqueeze(-1)
-        return F.normalize(e, dim=-1)
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else t.data_ptr()
 
 
-def unpack_blocks(words: torch.Tensor, level: int) -> torch.Tensor:
-    """(n, R^3/64) int64 grid words (bit x + R*y + R^2*z) -> (n, (R/4)^3, 64) float blocks."""
-    R = 1 << level
+def _op(t, mode: int, ld: int = 0) -> _abi.NnOperand:
+    return _abi.NnOperand(t.data_ptr(), mode, ld)
+
+
+def _ctx(ctx):
+    if ctx is None:
+        from . import default_context
+        ctx = default_context()
+    return ctx
+
+
+def gemm(ctx, a: _abi.NnOperand, b: _abi.NnOperand, m: int, n: int, k: int, out: torch.Tensor, alpha: float = 1.0,
+         bias: Optional[torch.Tensor] = None, relu: bool = False, gate: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """out (m x n, FP32 or bf16) = epilogue(alpha * A B^T) on the tensor cores (tdag_nn_gemm)."""
+    _abi.check(lib().tdag_nn_gemm(_ctx(ctx).handle, ctypes.byref(a), ctypes.byref(b), m, n, k, alpha, _ptr(bias), int(relu), _ptr(gate),
+                                  n if gate is not None else 0, out.data_ptr(), out.stride(0), int(out.dtype == torch.bfloat16)))
+    return out
+
+
+def block_masks(ctx, words: torch.Tensor, level: int) -> torch.Tensor:
+    """(n, (R/4)^3) int64 block masks of n items (tdag_nn_block_masks)."""
     n = words.shape[0]
-    shifts = torch.arange(64, device=words.device, dtype=torch.int64)
-    bits = ((words.unsqueeze(-1) >> shifts) & 1).to(torch.float32)  # arithmetic shift: bit s is still bit s
-    b = R // 4
-    bits = bits.reshape(n, b, 4, b, 4, b, 4)  # [bz, dz, by, dy, bx, dx] from the flat index x + R y + R^2 z
-    return bits.permute(0, 1, 3, 5, 2, 4, 6).reshape(n, b * b * b, 64)
+    B = ((1 << level) // 4) ** 3
+    masks = torch.empty((n, B), dtype=torch.int64, device=words.device)
+    _abi.check(lib().tdag_nn_block_masks(_ctx(ctx).handle, words.contiguous().data_ptr(), n, level, masks.data_ptr()))
+    return masks
+
+
+class ProposalEncoder:
+    """Leaf-block MLP 64 -> 256 -> 256 -> 32 with mean pooling over an item's non-empty 4^3 blocks,
+    on the library's kernels. Parameters: FP32 master weights (out x in) and biases, their bf16
+    copies (the GEMM operands) and the AdamW moments, all on one device."""
+
+    def __init__(self, device=None, seed: int = 0, ctx=None):
+        self.ctx = _ctx(ctx)
+        self.device = torch.device("cuda", self.ctx.device) if device is None else torch.device(device)
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        params = []
+        for o, i in LAYERS:  # uniform(-1/sqrt(fan_in), 1/sqrt(fan_in))
+            bound = 1.0 / math.sqrt(i)
+            params.append((torch.rand((o, i), generator=g, dtype=torch.float64) * 2 - 1) * bound)
+            params.append((torch.rand((o,), generator=g, dtype=torch.float64) * 2 - 1) * bound)
+        self.load(params)
+
+    def load(self, params: Sequence) -> "ProposalEncoder":
+        """Set the six parameters [w1, b1, w2, b2, w3, b3] (any array type) and reset AdamW."""
+        self.params = [torch.as_tensor(p).to(device=self.device, dtype=torch.float32).contiguous() for p in params]
+        self.w16 = [self.params[2 * l].to(torch.bfloat16) for l in range(3)]
+        self.m1 = [torch.zeros_like(p) for p in self.params]
+        self.m2 = [torch.zeros_like(p) for p in self.params]
+        self.step_count = 0
+        return self
+
+    def numpy_params(self):
+        return [p.double().cpu().numpy() for p in self.params]
+
+    # ---- forward / backward
+    def forward(self, words: torch.Tensor, level: int, keep: bool = False):
+        """u (n x 32, FP32, L2-normalised) of n items; with keep, also the cache for backward()."""
+        masks = block_masks(self.ctx, words, level)
+        return self.forward_masks(masks, keep)
+
+    def forward_masks(self, masks: torch.Tensor, keep: bool = False):
+        ctx, dev = self.ctx, self.device
+        n, B = masks.shape
+        rows = n * B
+        rows_p = max(16, (rows + 15) // 16 * 16)  # the weight gradients contract over rows: a multiple of 16
+        flat = torch.zeros(rows_p, dtype=torch.int64, device=dev)
+        flat[:rows] = masks.reshape(-1)
+        h1 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
+        h2 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
+        z = torch.empty((rows_p, EMBED_DIM), dtype=torch.float32, device=dev)
+        gemm(ctx, _op(flat, _abi.NN_BITS), _op(self.w16[0], _abi.NN_KMAJOR, 64), rows_p, HIDDEN, 64, h1, bias=self.params[1], relu=True)
+        gemm(ctx, _op(h1, _abi.NN_KMAJOR, HIDDEN), _op(self.w16[1], _abi.NN_KMAJOR, HIDDEN), rows_p, HIDDEN, HIDDEN, h2, bias=self.params[3],
+             relu=True)
+        gemm(ctx, _op(h2, _abi.NN_KMAJOR, HIDDEN), _op(self.w16[2], _abi.NN_KMAJOR, HIDDEN), rows_p, EMBED_DIM, HIDDEN, z, bias=self.params[5])
+        u = torch.empty((n, EMBED_DIM), dtype=torch.float32, device=dev)
+        ub = torch.empty((n, EMBED_DIM), dtype=torch.bfloat16, device=dev)
+        norm = torch.empty(n, dtype=torch.float32, device=dev)
+        count = torch.empty(n, dtype=torch.float32, device=dev)
+        _abi.check(lib().tdag_nn_pool_forward(ctx.handle, z.data_ptr(), flat.data_ptr(), n, B, u.data_ptr(), ub.data_ptr(), norm.data_ptr(),
+                                              count.data_ptr()))
+        if not keep:
+            return u, ub
+        return u, ub, {"masks": flat, "h1": h1, "h2": h2, "u": u, "norm": norm, "count": count, "n": n, "B": B, "rows_p": rows_p}
+
+    def backward(self, cache: dict, du: torch.Tensor) -> List[torch.Tensor]:
+        """FP32 gradients [gw1, gb1, gw2, gb2, gw3, gb3] from d loss / d u (n x 32, FP32)."""
+        ctx, dev = self.ctx, self.device
+        n, B, rows_p = cache["n"], cache["B"], cache["rows_p"]
+        h1, h2, flat = cache["h1"], cache["h2"], cache["masks"]
+        dz3 = torch.zeros((rows_p, EMBED_DIM), dtype=torch.bfloat16, device=dev)
+        _abi.check(lib().tdag_nn_pool_backward(ctx.handle, du.contiguous().data_ptr(), cache["u"].data_ptr(), cache["norm"].data_ptr(),
+                                               cache["count"].data_ptr(), flat.data_ptr(), n, B, dz3.data_ptr()))
+        grads = [None] * 6
+        grads[4] = gemm(ctx, _op(dz3, _abi.NN_MNMAJOR, EMBED_DIM), _op(h2, _abi.NN_MNMAJOR, HIDDEN), EMBED_DIM, HIDDEN, rows_p,
+                        torch.empty((EMBED_DIM, HIDDEN), dtype=torch.float32, device=dev))
+        grads[5] = self._column_sums(dz3)
+        dz2 = gemm(ctx, _op(dz3, _abi.NN_KMAJOR, EMBED_DIM), _op(self.w16[2], _abi.NN_MNMAJOR, HIDDEN), rows_p, HIDDEN, EMBED_DIM,
+                   torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev), gate=h2)
+        grads[2] = gemm(ctx, _op(dz2, _abi.NN_MNMAJOR, HIDDEN), _op(h1, _abi.NN_MNMAJOR, HIDDEN), HIDDEN, HIDDEN, rows_p,
+                        torch.empty((HIDDEN, HIDDEN), dtype=torch.float32, device=dev))
+        grads[3] = self._column_sums(dz2)
+        dz1 = gemm(ctx, _op(dz2, _abi.NN_KMAJOR, HIDDEN), _op(self.w16[1], _abi.NN_MNMAJOR, HIDDEN), rows_p, HIDDEN, HIDDEN,
+                   torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev), gate=h1)
+        grads[0] = gemm(ctx, _op(dz1, _abi.NN_MNMAJOR, HIDDEN), _op(flat, _abi.NN_BITS_T), HIDDEN, 64, rows_p,
+                        torch.empty((HIDDEN, 64), dtype=torch.float32, device=dev))
+        grads[1] = self._column_sums(dz1)
+        return grads
+
+    def _column_sums(self, x: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(x.shape[1], dtype=torch.float32, device=self.device)
+        _abi.check(lib().tdag_nn_column_sums(self.ctx.handle, x.data_ptr(), x.shape[0], x.shape[1], x.stride(0), out.data_ptr()))
+        return out
+
+    # ---- training
+    def loss_and_grads(self, words_t: torch.Tensor, words_p: torch.Tensor, level: int, tau: float):
+        """(loss tensor on the device, gradients) of the symmetric InfoNCE of b (target, parent) pairs;
+        b must be a multiple of 16."""
+        b = words_t.shape[0]
+        assert b % 16 == 0 and b == words_p.shape[0]
+        dev = self.device
+        u, ub, cache = self.forward(torch.cat([words_t, words_p]), level, keep=True)
+        logits = torch.empty((b, b), dtype=torch.float32, device=dev)
+        gemm(self.ctx, _op(ub[:b], _abi.NN_KMAJOR, EMBED_DIM), _op(ub[b:], _abi.NN_KMAJOR, EMBED_DIM), b, b, EMBED_DIM, logits, alpha=1.0 / tau)
+        loss = torch.empty(1, dtype=torch.float32, device=dev)
+        dl = torch.empty((b, b), dtype=torch.bfloat16, device=dev)
+        _abi.check(lib().tdag_nn_info_nce(self.ctx.handle, logits.data_ptr(), b, loss.data_ptr(), dl.data_ptr()))
+        du = torch.empty((2 * b, EMBED_DIM), dtype=torch.float32, device=dev)
+        gemm(self.ctx, _op(dl, _abi.NN_KMAJOR, b), _op(ub[b:], _abi.NN_MNMAJOR, EMBED_DIM), b, EMBED_DIM, b, du[:b], alpha=1.0 / tau)
+        gemm(self.ctx, _op(dl, _abi.NN_MNMAJOR, b), _op(ub[:b], _abi.NN_MNMAJOR, EMBED_DIM), b, EMBED_DIM, b, du[b:], alpha=1.0 / tau)
+        return loss, self.backward(cache, du)
+
+    def adamw_step(self, grads: Sequence[torch.Tensor], lr: float, weight_decay: float = 1e-2, beta1: float = 0.9, beta2: float = 0.999,
+                   eps: float = 1e-8) -> None:
+        self.step_count += 1
+        for i, (p, g) in enumerate(zip(self.params, grads)):
+            w16 = self.w16[i // 2] if i % 2 == 0 else None
+            decay = weight_decay
+            _abi.check(lib().tdag_nn_adamw(self.ctx.handle, p.data_ptr(), g.contiguous().data_ptr(), self.m1[i].data_ptr(), self.m2[i].data_ptr(),
+                                           p.numel(), lr, beta1, beta2, eps, decay, self.step_count, _ptr(w16)))
+
+    def sync(self) -> None:
+        """Waits for the queued kernels; raises on a tensor-core wait past its bound."""
+        _abi.check(lib().tdag_nn_sync(self.ctx.handle))
+
+
+def _on_lib_stream(ctx):
+    """torch's current stream set to the library context's stream, so that allocations and the
+    kernels of both are ordered."""
+    sp = ctypes.c_void_p()
+    _abi.check(lib().tdag_ctx_stream(ctx.handle, ctypes.byref(sp)))
+    return torch.cuda.stream(torch.cuda.ExternalStream(sp.value, device=ctx.device))
 
 
 def embed(encoder: ProposalEncoder, words: torch.Tensor, level: int, chunk: int = 16384) -> torch.Tensor:
+    """(n, 32) FP32 embeddings of n items, in chunks of items."""
     out = []
-    with torch.no_grad():
+    with _on_lib_stream(encoder.ctx):
         for a in range(0, words.shape[0], chunk):
-            out.append(encoder(words[a:a + chunk], level))
-    return torch.cat(out) if out else torch.zeros((0, EMBED_DIM), device=words.device)
+            out.append(encoder.forward(words[a:a + chunk], level)[0])
+        res = torch.cat(out) if out else torch.zeros((0, EMBED_DIM), device=words.device)
+    encoder.sync()
+    return res
 
 
 # ------------------------------------------------------------------------------------------------
@@ -117,25 +250,30 @@ def subset_parents(ctx, words: torch.Tensor, level: int, config, sources: torch.
 # ------------------------------------------------------------------------------------------------
 # proposals
 # ------------------------------------------------------------------------------------------------
-def propose_lists(embeddings: torch.Tensor, positions: torch.Tensor, k: int, chunk: int = 4096) -> torch.Tensor:
+def propose_lists(embeddings: torch.Tensor, positions: torch.Tensor, k: int, encoder_ctx=None) -> torch.Tensor:
     """(n, k) original indices: for every target, the k items with the highest embedding dot product
-    among those preceding it in the source order (-1 where fewer exist)."""
+    among those preceding it in the source order (-1 where fewer exist). Scored on the tensor cores
+    with the top-k kept in registers (tdag_nn_topk; k is rounded up to 8, 16 or 32 and cut back)."""
     n = embeddings.shape[0]
     out = torch.full((n, k), -1, dtype=torch.int64, device=embeddings.device)
     if n == 0:
         return out
+    ctx = _ctx(encoder_ctx)
+    kk = 8 if k <= 8 else (16 if k <= 16 else 32)
+    assert k <= 32
     order = torch.argsort(positions)  # sorted position -> original index
-    e = embeddings[order].to(torch.bfloat16)
-    for a in range(1, n, chunk):
-        b = min(n, a + chunk)
-        scores = (e[a:b] @ e[:b].T).float()  # (targets a..b) x (sources 0..b), tensor-core GEMM
-        col = torch.arange(b, device=e.device)
-        row = torch.arange(a, b, device=e.device).unsqueeze(1)
-        scores.masked_fill_(col.unsqueeze(0) >= row, float("-inf"))  # sources strictly before the target
-        kk = min(k, b)
-        top = torch.topk(scores, kk, dim=1)
-        idx = torch.where(torch.isfinite(top.values), order[top.indices], torch.full_like(top.indices, -1))
-        out[order[a:b], :kk] = idx
+    with _on_lib_stream(ctx):
+        e = embeddings[order].to(torch.bfloat16).contiguous()
+        idx = torch.empty((n, kk), dtype=torch.int32, device=e.device)
+        score = torch.empty((n, kk), dtype=torch.float32, device=e.device)
+        _abi.check(lib().tdag_nn_topk(ctx.handle, e.data_ptr(), n, kk, idx.data_ptr(), score.data_ptr()))
+        if kk > k:  # keep the k best of the kk
+            sel = torch.topk(score, k, dim=1).indices
+            idx = torch.gather(idx, 1, sel)
+        idx = idx.long()
+        res = torch.where(idx >= 0, order[idx.clamp(min=0)], torch.full_like(idx, -1))
+        out[order] = res
+    _abi.check(lib().tdag_nn_sync(ctx.handle))
     return out
 
 
@@ -183,35 +321,31 @@ def recall_at_k(lists: torch.Tensor, parent: torch.Tensor) -> float:
 # ------------------------------------------------------------------------------------------------
 # training
 # ------------------------------------------------------------------------------------------------
-def info_nce(e_t: torch.Tensor, e_p: torch.Tensor, tau: float) -> torch.Tensor:
-    """Symmetric InfoNCE with in-batch negatives."""
-    logits = (e_t @ e_p.T) / tau
-    labels = torch.arange(e_t.shape[0], device=e_t.device)
-    return 0.5 * (F.cross_entropy(logits, labels) + F.cross_entropy(logits.T, labels))
-
-
 def train(encoder: ProposalEncoder, sets: Sequence[Tuple[torch.Tensor, int, torch.Tensor]], steps: int = 600, batch: int = 2048,
           lr: float = 2e-3, weight_decay: float = 1e-2, tau: float = 0.07, seed: int = 0) -> List[float]:
     """sets: (grid words, level, exhaustive parent per item). Each step draws a batch of positive
-    pairs from one randomly chosen set."""
+    pairs (a multiple of 16) from one randomly chosen set; forward, InfoNCE, backward and AdamW run
+    as the library's kernels."""
     g = torch.Generator(device="cpu").manual_seed(seed)
-    opt = torch.optim.AdamW(encoder.parameters(), lr=lr, weight_decay=weight_decay)  # FP32 master weights
     pairs = []
     for words, level, parent in sets:
         t = (parent != torch.arange(parent.shape[0], device=parent.device)).nonzero().squeeze(1)
-        if t.numel() >= 2:
+        if t.numel() >= 16:
             pairs.append((words, level, t, parent[t]))
     losses = []
     if not pairs:
         return losses
-    for step in range(steps):
-        words, level, t, p = pairs[int(torch.randint(len(pairs), (1,), generator=g))]
-        idx = torch.randint(t.numel(), (min(batch, t.numel()),), generator=g).to(t.device)
-        loss = info_nce(encoder(words[t[idx]], level), encoder(words[p[idx]], level), tau)
-        opt.zero_grad(set_to_none=True)
-        loss.backward()
-        opt.step()
-        losses.append(loss.item())
+    dev_losses = []
+    with _on_lib_stream(encoder.ctx):
+        for step in range(steps):
+            words, level, t, p = pairs[int(torch.randint(len(pairs), (1,), generator=g))]
+            b = min(batch, t.numel()) // 16 * 16
+            idx = torch.randint(t.numel(), (b,), generator=g).to(t.device)
+            loss, grads = encoder.loss_and_grads(words[t[idx]], words[p[idx]], level, tau)
+            encoder.adamw_step(grads, lr, weight_decay)
+            dev_losses.append(loss)
+        losses = torch.cat(dev_losses).cpu().tolist()
+    encoder.sync()
     return losses
 
 
@@ -232,7 +366,7 @@ class ProposalHook:
             W = (1 << (3 * level)) // 64
             words = torch.empty((n, W), dtype=torch.int64, device=f"cuda:{self.device}")
             _abi.check(lib().tdag_device_copy(self.ctx.handle, words.data_ptr(), d_grids, n * W * 8))
-            src = sources_of(propose_lists(embed(self.encoder, words, level), popcount_positions(words), self.k)).to(torch.int32)
+            src = sources_of(propose_lists(embed(self.encoder, words, level), popcount_positions(words), self.k, self.encoder.ctx)).to(torch.int32)
             torch.cuda.synchronize(self.device)
             if src.numel():
                 _abi.check(lib().tdag_device_copy(self.ctx.handle, d_sources, src.data_ptr(), src.numel() * 4))

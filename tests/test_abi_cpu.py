@@ -11,9 +11,9 @@ from conftest import REPO
 
 
 def header_functions():
-    """Every tdag_* function declared by the C headers (include/tdag.h, tdag_diag.h, tdag16.h)."""
+    """Every tdag_* function declared by the C headers (include/tdag.h, tdag_diag.h, tdag16.h, tdag_nn.h)."""
     names = set()
-    for h in ("tdag.h", "tdag_diag.h", "tdag16.h"):
+    for h in ("tdag.h", "tdag_diag.h", "tdag16.h", "tdag_nn.h"):
         src = open(os.path.join(REPO, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         names |= set(re.findall(r"\b(tdag(?:16)?_[a-z0-9_]+)\s*\(", src))

@@ -1,0 +1,231 @@
+"""GPU tests of the learned-proposal kernels (include/tdag_nn.h) through the C ABI.
+
+- tdag_nn_gemm (tcgen05 tensor cores, bf16 operands, FP32 accumulation) in every operand mode and
+  epilogue against a plain PyTorch FP32 product of the same bf16 values: only the summation order
+  differs, so the tolerance is a few FP32 ulps of the row's magnitude;
+- the fused causal top-k scorer against the NumPy statement;
+- block masks exactly, and pooling, InfoNCE, forward, backward and AdamW against the FP64 NumPy
+  oracle (oracle/proposal_oracle.py). The network path rounds weights and hidden activations to
+  bf16, so those comparisons use relative tolerances stated in each test.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import proposal_oracle as PO  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16(x):
+    return torch.as_tensor(x, dtype=torch.float32).to(torch.bfloat16)
+
+
+def _ref_operand(t, mode, rows, k):
+    """(rows, k) FP32 matrix an operand stands for."""
+    from tdag import _abi
+    if mode == _abi.NN_KMAJOR:
+        return t[:rows, :k].float()
+    if mode == _abi.NN_MNMAJOR:
+        return t[:k, :rows].float().T
+    bits = ((t.unsqueeze(-1) >> torch.arange(64, device=t.device)) & 1).float()  # (masks, 64)
+    if mode == _abi.NN_BITS:
+        return bits[:rows]
+    return bits[:k, :rows].T  # BITS_T
+
+
+def _make(mode, rows, k, g, dev):
+    from tdag import _abi
+    if mode == _abi.NN_KMAJOR:
+        return _bf16(torch.randn((rows, k), generator=g)).to(dev)
+    if mode == _abi.NN_MNMAJOR:
+        return _bf16(torch.randn((k, rows), generator=g)).to(dev)
+    n = rows if mode == _abi.NN_BITS else k
+    return torch.randint(-(1 << 62), 1 << 62, (n,), generator=g, dtype=torch.int64).to(dev)
+
+
+CASES = [  # (mode A, mode B, M, N, K)
+    (0, 0, 300, 256, 256),
+    (0, 0, 129, 32, 32),
+    (0, 0, 64, 100, 80),
+    (2, 0, 200, 256, 64),
+    (1, 1, 32, 256, 272),
+    (1, 3, 256, 64, 272),
+    (0, 1, 160, 256, 32),
+    (1, 1, 48, 32, 4096),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "A{}B{}_{}x{}x{}".format(*c))
+def test_gemm_modes_match_fp32_product(tdaglib, gpu_ctx, case):
+    from tdag import _abi, proposal as P
+    ma, mb, M, N, K = case
+    dev = torch.device("cuda", gpu_ctx.device)
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    a = _make(ma, M, K, g, dev)
+    b = _make(mb, N, K, g, dev)
+    lda = {0: K, 1: M}.get(ma, 0)
+    ldb = {0: K, 1: N}.get(mb, 0)
+    ref = _ref_operand(a, ma, M, K) @ _ref_operand(b, mb, N, K).T
+    bias = torch.randn(N, generator=g).to(dev)
+    gate = _bf16(torch.randn((M, N), generator=g)).to(dev)
+    for alpha, use_bias, relu, use_gate, out_bf16 in ((1.0, False, False, False, False), (0.5, True, True, False, False),
+                                                       (1.0, True, False, True, True)):
+        out = torch.full((M, N), 7.0, dtype=torch.bfloat16 if out_bf16 else torch.float32, device=dev)
+        P.gemm(gpu_ctx, _abi.NnOperand(a.data_ptr(), ma, lda), _abi.NnOperand(b.data_ptr(), mb, ldb), M, N, K, out, alpha=alpha,
+               bias=bias if use_bias else None, relu=relu, gate=gate if use_gate else None)
+        torch.cuda.synchronize()
+        want = ref * alpha
+        if use_bias:
+            want = want + bias
+        if relu:
+            want = torch.relu(want)
+        if use_gate:
+            want = torch.where(gate.float() > 0, want, torch.zeros_like(want))
+        tol = 1e-5 * (ref.abs().amax(dim=1, keepdim=True) + 1.0) * np.sqrt(K) + (1e-2 * want.abs() if out_bf16 else 0.0)
+        assert bool(((out.float() - want).abs() <= tol).all()), (alpha, use_bias, relu, use_gate, out_bf16,
+                                                                float((out.float() - want).abs().max()))
+
+
+@pytest.mark.parametrize("k", [8, 16, 32])
+def test_topk_matches_numpy(tdaglib, gpu_ctx, k):
+    from tdag import _abi
+    dev = torch.device("cuda", gpu_ctx.device)
+    n = 700
+    g = torch.Generator().manual_seed(k)
+    e = _bf16(torch.randn((n, 32), generator=g))
+    ed = e.to(dev)
+    idx = torch.full((n, k), -5, dtype=torch.int32, device=dev)
+    score = torch.empty((n, k), dtype=torch.float32, device=dev)
+    _abi.check(tdaglib.lib().tdag_nn_topk(gpu_ctx.handle, ed.data_ptr(), n, k, idx.data_ptr(), score.data_ptr()))
+    _abi.check(tdaglib.lib().tdag_nn_sync(gpu_ctx.handle))
+    idx, score = idx.cpu().numpy(), score.cpu().numpy()
+    s = e.float().numpy().astype(np.float64) @ e.float().numpy().astype(np.float64).T
+    for i in range(n):
+        got = idx[i]
+        valid = got[got >= 0]
+        assert len(valid) == min(k, i) and len(set(valid.tolist())) == len(valid)
+        assert bool((valid < i).all())
+        if i == 0:
+            continue
+        kth = np.sort(s[i, :i])[::-1][min(k, i) - 1]  # the k-th best score among the predecessors
+        assert np.all(s[i, valid] >= kth - 1e-4), i
+        assert np.allclose(score[i][got >= 0], s[i, valid], atol=1e-4)
+
+
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_block_masks_exact(tdaglib, gpu_ctx, level):
+    from tdag import proposal as P
+    rng = np.random.default_rng(level)
+    R = 1 << level
+    words = rng.integers(0, 1 << 63, (97, R ** 3 // 64), dtype=np.uint64) ^ rng.integers(0, 1 << 63, (97, R ** 3 // 64), dtype=np.uint64) << 1
+    got = P.block_masks(gpu_ctx, torch.from_numpy(words.view(np.int64)).cuda(gpu_ctx.device), level)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy().view(np.uint64), PO.block_masks(words, level))
+
+
+def _pairs(level, b, seed):
+    rng = np.random.default_rng(seed)
+    R = 1 << level
+    bits = rng.random((2 * b, R ** 3)) < 0.25
+    return np.packbits(bits, axis=-1, bitorder="little").view("<u8").reshape(2 * b, -1)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _cos(a, b):
+    a, b = a.ravel(), b.ravel()
+    return float(a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_forward_backward_match_oracle(tdaglib, gpu_ctx, level):
+    """Loss, embeddings and all six gradients of one InfoNCE batch against the FP64 oracle, with the
+    same bf16 weight copies, in two forms:
+    - the oracle rounding to bf16 where the kernels store bf16 (hidden activations, embeddings for
+      the logits, the logit gradient and the backward operands): only FP32 against FP64 summation and
+      the odd value on the other side of a bf16 rounding boundary differ, so every gradient is within
+      1.5 % relative (Frobenius) error (measured: at most 0.45 %), cosine similarity above 0.9999;
+    - the exact FP64 oracle: bf16 storage is the whole difference, every gradient within 15 %
+      relative error (the last layer's bias gradient, a sum of mostly cancelling terms, is the
+      worst: about 11 % at level 4), cosine above 0.99; embeddings within 0.02 per component; loss
+      within 2 %."""
+    from tdag import proposal as P
+    b = 48
+    words = _pairs(level, b, 10 + level)
+    enc = P.ProposalEncoder(seed=level, ctx=gpu_ctx)
+    params = enc.numpy_params()
+    for i in (0, 2, 4):  # the GEMMs read bf16 weight copies
+        params[i] = enc.w16[i // 2].float().double().cpu().numpy()
+    dw = torch.from_numpy(words.view(np.int64)).cuda(gpu_ctx.device)
+    with P._on_lib_stream(gpu_ctx):
+        loss, grads = enc.loss_and_grads(dw[:b], dw[b:], level, 0.07)
+        u, _ = enc.forward(dw, level)
+    enc.sync()
+    masks = PO.block_masks(words, level)
+    u_ref, _ = PO.forward(params, masks)
+    assert np.abs(u.cpu().numpy() - u_ref).max() < 0.02
+    u_bf, _ = PO.forward(params, masks, PO.bf16)
+    assert np.abs(u.cpu().numpy() - u_bf).max() < 2e-3
+    grads = [g.double().cpu().numpy() for g in grads]
+    loss_bf, g_bf = PO.grads_of(params, masks[:b], masks[b:], 0.07, PO.bf16)
+    assert abs(float(loss.item()) - loss_bf) <= 2e-3 * abs(loss_bf)
+    for i, (g, r) in enumerate(zip(grads, g_bf)):
+        print(f"level {level} param {i} vs bf16-storage oracle: relative error {_rel(g, r):.5f} cosine {_cos(g, r):.6f}")
+        assert _rel(g, r) < 0.015 and _cos(g, r) > 0.9999, (i, _rel(g, r), _cos(g, r))
+    loss_ref, g_ref = PO.grads_of(params, masks[:b], masks[b:], 0.07)
+    assert abs(float(loss.item()) - loss_ref) <= 0.02 * abs(loss_ref)
+    for i, (g, r) in enumerate(zip(grads, g_ref)):
+        print(f"level {level} param {i} vs exact oracle: relative error {_rel(g, r):.4f} cosine {_cos(g, r):.5f}")
+        assert _rel(g, r) < 0.15 and _cos(g, r) > 0.99, (i, _rel(g, r), _cos(g, r))
+
+
+def test_adamw_matches_oracle(tdaglib, gpu_ctx):
+    from tdag import _abi
+    rng = np.random.default_rng(9)
+    n = 5000
+    w, g = rng.normal(size=n), rng.normal(size=n)
+    m1, m2 = rng.normal(size=n) * 0.1, np.abs(rng.normal(size=n)) * 0.01
+    dev = torch.device("cuda", gpu_ctx.device)
+    t = [torch.tensor(x, dtype=torch.float32, device=dev) for x in (w, g, m1, m2)]
+    w16 = torch.empty(n, dtype=torch.bfloat16, device=dev)
+    _abi.check(tdaglib.lib().tdag_nn_adamw(gpu_ctx.handle, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), t[3].data_ptr(), n, 1e-3,
+                                           0.9, 0.999, 1e-8, 1e-2, 3, w16.data_ptr()))
+    _abi.check(tdaglib.lib().tdag_nn_sync(gpu_ctx.handle))
+    f32 = [x.astype(np.float32).astype(np.float64) for x in (w, g, m1, m2)]
+    w_ref, a_ref, v_ref = PO.adamw(*f32, 3, lr=1e-3)
+    assert np.allclose(t[0].cpu().numpy(), w_ref, rtol=1e-5, atol=1e-7)
+    assert np.allclose(t[2].cpu().numpy(), a_ref, rtol=1e-5, atol=1e-8)
+    assert np.allclose(t[3].cpu().numpy(), v_ref, rtol=1e-5, atol=1e-9)
+    assert torch.equal(w16, t[0].to(torch.bfloat16))
+
+
+def test_training_lowers_the_loss_and_gradients_stay_checked(tdaglib, gpu_ctx):
+    """Fifty kernel training steps on one fixed batch lower its loss (the optimiser is wired to
+    the gradients), and the oracle's loss at the trained weights agrees."""
+    from tdag import proposal as P
+    level, b = 3, 64
+    words = _pairs(level, b, 77)
+    words[b:] = words[:b]  # parents identical to their targets: an easy, learnable pairing
+    enc = P.ProposalEncoder(seed=5, ctx=gpu_ctx)
+    dw = torch.from_numpy(words.view(np.int64)).cuda(gpu_ctx.device)
+    losses = []
+    with P._on_lib_stream(gpu_ctx):
+        for _ in range(50):
+            loss, grads = enc.loss_and_grads(dw[:b], dw[b:], level, 0.07)
+            enc.adamw_step(grads, 2e-3)
+            losses.append(loss)
+        losses = torch.cat(losses).cpu().numpy()
+    enc.sync()
+    assert losses[-1] < 0.9 * losses[0], losses
+    params = enc.numpy_params()
+    for i in (0, 2, 4):
+        params[i] = enc.w16[i // 2].float().double().cpu().numpy()
+    masks = PO.block_masks(words, level)
+    with P._on_lib_stream(gpu_ctx):
+        loss, _ = enc.loss_and_grads(dw[:b], dw[b:], level, 0.07)
+    enc.sync()
+    assert abs(float(loss.item()) - PO.loss_of(params, masks[:b], masks[b:], 0.07, PO.bf16)) < 2e-3 * max(1.0, float(loss.item()))

@@ -37,8 +37,7 @@ def test_proposed_build_is_lossless(oracle, tdaglib, gpu_ctx):
     from tdag import proposal as P
     cfg = tdaglib.TransformDAGConfig()
     g = _scene(tdaglib, gpu_ctx, 128, 11, 150)
-    torch.manual_seed(0)
-    enc = P.ProposalEncoder().cuda()
+    enc = P.ProposalEncoder(seed=0, ctx=gpu_ctx)
     res, sources = P.construct_transform_dag_proposed(g, enc, 4, cfg, ctx=gpu_ctx)
     got = res.to_host(ctx=gpu_ctx)
     ex = tdaglib.construct_transform_dag_device(g, cfg, ctx=gpu_ctx).to_host(ctx=gpu_ctx)
@@ -58,8 +57,7 @@ def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx):
         for level, words in P.level_items(_scene(tdaglib, gpu_ctx, 256, seed), cfg, ctx=gpu_ctx).items():
             if level >= 3:
                 train_sets.append((words, level, P.exhaustive_parents(gpu_ctx, words, level, cfg)[0]))
-    torch.manual_seed(0)
-    enc = P.ProposalEncoder().cuda()
+    enc = P.ProposalEncoder(seed=0, ctx=gpu_ctx)
     losses = P.train(enc, train_sets, steps=400, batch=1024)
     assert losses[-1] < losses[0]
     held = P.level_items(_scene(tdaglib, gpu_ctx, 256, 9), cfg, ctx=gpu_ctx)
