@@ -153,8 +153,11 @@ def run_proposal(args, world, rank, local, pg):
     for k in (8, 32):
         s_k, (r, src) = timed(lambda: P.construct_transform_dag_proposed(g, enc, k, cfg, ctx=ctx))
         n_k = nodes_of(r)
+        secs = getattr(P.construct_transform_dag_proposed, "last_seconds", {})
         modes[str(k)] = {"ms": s_k * 1e3, "mvoxels_per_s": voxels / s_k / 1e6, "nodes": n_k,
                          "extra_nodes_percent": 100.0 * (n_k - ex_nodes) / ex_nodes, "speed_vs_exhaustive": ex_s / s_k,
+                         "embed_ms_per_level": {str(l): v[0] * 1e3 for l, v in secs.items()},
+                         "score_ms_per_level": {str(l): v[1] * 1e3 for l, v in secs.items()},
                          "sources_per_level": {str(l): {"items": it, "sources": sc} for l, (it, sc) in src.items()}}
     out = {"metric": "TDAG build Mvoxels/s (learned proposals, approximate)", "value": modes["8"]["mvoxels_per_s"], "unit": UNIT,
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "u64 (encoder bf16)",

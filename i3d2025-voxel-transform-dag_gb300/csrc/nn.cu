@@ -97,6 +97,24 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16])
         v[j] = __uint_as_float(r[j]);
 }
 
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmemLoad32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, "
+                 "%19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+                 "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+                 "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                 "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+        v[j] = __uint_as_float(r[j]);
+}
+
 __device__ __forceinline__ uint16_t toBf16(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float fromBf16(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
 __device__ __forceinline__ uint32_t bitPair(uint64_t m, uint32_t k) // elements k, k + 1 of a mask as bf16 1.0 / 0.0
@@ -211,7 +229,12 @@ __global__ void __launch_bounds__(kGemmThreads) tcGemmKernel(GemmParams p)
     tcFenceAfter();
     const uint32_t tmem = tmemSlot;
 
-    const uint32_t chunks = (p.K + kChunkK - 1) / kChunkK;
+    // split K (blockIdx.z of gridDim.z): this CTA's chunks are [c0, c0 + chunks); the partial tiles are
+    // summed into C by atomic adds
+    const uint32_t allChunks = (p.K + kChunkK - 1) / kChunkK;
+    const uint32_t per = (allChunks + gridDim.z - 1) / gridDim.z;
+    const uint32_t c0 = blockIdx.z * per;
+    const uint32_t chunks = c0 < allChunks ? min(per, allChunks - c0) : 0u;
     bool ok = true;
     uint32_t issued = 0; // chunks whose MMAs were committed
     for (uint32_t c = 0; c < chunks; ++c) {
@@ -225,13 +248,14 @@ __global__ void __launch_bounds__(kGemmThreads) tcGemmKernel(GemmParams p)
                 break;
             }
         }
-        stageTile(tA, p.a, 128, m0, p.M, c * kChunkK, p.K);
-        stageTile(tB, p.b, BN, n0, p.N, c * kChunkK, p.K);
+        const uint32_t k0 = (c0 + c) * kChunkK;
+        stageTile(tA, p.a, 128, m0, p.M, k0, p.K);
+        stageTile(tB, p.b, BN, n0, p.N, k0, p.K);
         fenceProxyAsync();
         __syncthreads();
         if (threadIdx.x == 0) {
             tcFenceAfter();
-            const uint32_t steps = min(4u, (p.K - c * kChunkK) / 16u);
+            const uint32_t steps = min(4u, (p.K - k0) / 16u);
             for (uint32_t s = 0; s < steps; ++s) {
                 const uint64_t da = smemDesc(smemAddr(tA) + s * 128u * 32u, kLbo, kSbo);
                 const uint64_t db = smemDesc(smemAddr(tB) + s * BN * 32u, kLbo, kSbo);
@@ -241,12 +265,12 @@ __global__ void __launch_bounds__(kGemmThreads) tcGemmKernel(GemmParams p)
         }
         issued = c + 1;
     }
-    if (ok) {
+    if (ok && chunks) {
         const uint32_t last = chunks - 1;
         ok = __syncthreads_and(mbarWait(&bar[last & 1u], (last >> 1) & 1u));
     }
     tcFenceAfter();
-    if (ok) {
+    if (ok && chunks) {
         const uint32_t row = warp * 32 + lane, gm = m0 + row;
         for (uint32_t cc = 0; cc < BN / 16; ++cc) {
             float v[16];
@@ -267,7 +291,9 @@ __global__ void __launch_bounds__(kGemmThreads) tcGemmKernel(GemmParams p)
                         if ((g & 0x8000u) || !(g & 0x7FFFu))
                             x = 0.0f;
                     }
-                    if (p.cBf16)
+                    if (gridDim.z > 1)
+                        atomicAdd(&static_cast<float*>(p.c)[(size_t)gm * p.ldc + gn], x);
+                    else if (p.cBf16)
                         static_cast<uint16_t*>(p.c)[(size_t)gm * p.ldc + gn] = toBf16(x);
                     else
                         static_cast<float*>(p.c)[(size_t)gm * p.ldc + gn] = x;
@@ -306,6 +332,7 @@ __global__ void __launch_bounds__(kGemmThreads) topkKernel(const uint16_t* __res
     const uint32_t m0 = blockIdx.x * 128;
     uint8_t* tA = smem;
     uint8_t* tB0 = smem + A_BYTES;
+    float* mine = reinterpret_cast<float*>(smem + A_BYTES + 2 * B_BYTES) + threadIdx.x * 33; // candidate scores (padded rows)
 
     if (warp == 0)
         tmemAlloc(&tmemSlot, 512);
@@ -365,19 +392,43 @@ __global__ void __launch_bounds__(kGemmThreads) topkKernel(const uint16_t* __res
             tcFenceAfter();
         }
         const uint32_t j0 = t * kTopkTile;
-        for (uint32_t cc = 0; cc < kTopkTile / 16; ++cc) {
-            float v[16];
-            tmemLoad16(tmem + ((warp * 32u) << 16) + (t & 1u) * kTopkTile + cc * 16u, v);
+        const bool diagonal = j0 + kTopkTile > m0; // the tile holds sources at or after some of the CTA's targets
+        for (uint32_t cc = 0; cc < kTopkTile / 32; ++cc) {
+            float v[32];
+            tmemLoad32(tmem + ((warp * 32u) << 16) + (t & 1u) * kTopkTile + cc * 32u, v);
+            const uint32_t jb = j0 + cc * 32;
+            if (diagonal) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const uint32_t gj = j0 + cc * 16 + j;
-                if (gj < gi && v[j] > floorV) { // sources strictly before the target
-                    // replace the current minimum, then find the new one
+                for (int j = 0; j < 32; ++j)
+                    if (jb + j >= gi) // sources strictly before the target
+                        v[j] = -__int_as_float(0x7f800000);
+            }
+            float mx = v[0];
+#pragma unroll
+            for (int j = 1; j < 32; ++j)
+                mx = fmaxf(mx, v[j]);
+            if (!__any_sync(0xffffffffu, mx > floorV)) // most chunks: no lane has a score above its k-th best
+                continue;
+            if (mx > floorV) {
+                // the rare path, one candidate at a time through shared memory (a register array
+                // indexed at run time would live in local memory)
+                uint32_t cand = 0;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    mine[j] = v[j];
+                    cand |= (v[j] > floorV ? 1u : 0u) << j;
+                }
+                while (cand) {
+                    const int j = __ffs(cand) - 1;
+                    cand &= cand - 1u;
+                    const float x = mine[j];
+                    if (x <= floorV) // the floor rose since the mask was taken
+                        continue;
 #pragma unroll
                     for (int s = 0; s < KT; ++s)
                         if (s == floorAt) {
-                            best[s] = v[j];
-                            bestIdx[s] = (int32_t)gj;
+                            best[s] = x;
+                            bestIdx[s] = (int32_t)(jb + j);
                         }
                     floorV = best[0];
                     floorAt = 0;
@@ -443,18 +494,21 @@ __device__ __forceinline__ float warpSum(float v)
 }
 
 // One warp per item, lane = embedding dimension.
-__global__ void poolForwardKernel(const float* __restrict__ z, const uint64_t* __restrict__ masks, uint32_t n, uint32_t B, float* __restrict__ u,
-    uint16_t* __restrict__ uBf16, float* __restrict__ norm, float* __restrict__ count)
+// rowOf (optional) maps block (item, b) to its row of z (the MLP runs once per distinct mask).
+__global__ void poolForwardKernel(const float* __restrict__ z, const uint32_t* __restrict__ rowOf, const uint64_t* __restrict__ masks, uint32_t n,
+    uint32_t B, float* __restrict__ u, uint16_t* __restrict__ uBf16, float* __restrict__ norm, float* __restrict__ count)
 {
     const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, d = threadIdx.x & 31;
     if (item >= n)
         return;
     float acc = 0.0f, cnt = 0.0f;
-    for (uint32_t b = 0; b < B; ++b)
-        if (masks[(size_t)item * B + b]) {
-            acc += z[((size_t)item * B + b) * 32 + d];
+    for (uint32_t b = 0; b < B; ++b) {
+        const size_t e = (size_t)item * B + b;
+        if (masks[e]) {
+            acc += z[(size_t)(rowOf ? rowOf[e] : e) * 32 + d];
             cnt += 1.0f;
         }
+    }
     cnt = fmaxf(cnt, 1.0f);
     const float e = acc / cnt;
     const float len = fmaxf(sqrtf(warpSum(e * e)), 1e-12f);
@@ -589,12 +643,25 @@ __global__ void toBf16Kernel(const float* __restrict__ x, uint64_t n, uint16_t* 
 
 unsigned gridOf(uint64_t work, unsigned threads) { return (unsigned)std::max<uint64_t>(1, (work + threads - 1) / threads); }
 
+// Few output tiles over a long K (the weight gradients: 256 x 256 outputs, K = the batch's block
+// rows) split K across CTAs until about two CTAs run per SM, each split at least 8 chunks long; the
+// partial tiles are added into the zeroed FP32 output. Only for a plain FP32 epilogue.
 template <uint32_t BN>
-void launchGemm(const GemmParams& p, cudaStream_t s)
+void launchGemm(const GemmParams& p, cudaStream_t s, int smCount)
 {
     constexpr uint32_t smem = gemmSmem<BN>();
     TDAG_CUDA(cudaFuncSetAttribute(tcGemmKernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const dim3 grid((p.M + 127) / 128, (p.N + BN - 1) / BN);
+    const uint32_t tiles = ((p.M + 127) / 128) * ((p.N + BN - 1) / BN);
+    const uint32_t chunks = (p.K + kChunkK - 1) / kChunkK;
+    uint32_t splits = 1;
+    if (!p.cBf16 && !p.bias && !p.relu && !p.gate)
+        splits = std::max<uint32_t>(1, std::min<uint32_t>(chunks / 8, (uint32_t)(2 * smCount) / std::max<uint32_t>(1, tiles)));
+    if (splits > 1) {
+        const uint32_t per = (chunks + splits - 1) / splits;
+        splits = (chunks + per - 1) / per; // no empty split
+        TDAG_CUDA(cudaMemset2DAsync(p.c, (size_t)p.ldc * 4, 0, (size_t)p.N * 4, p.M, s));
+    }
+    const dim3 grid((p.M + 127) / 128, (p.N + BN - 1) / BN, splits);
     tcGemmKernel<BN><<<grid, kGemmThreads, smem, s>>>(p);
     TDAG_LAUNCHED();
 }
@@ -602,10 +669,10 @@ void launchGemm(const GemmParams& p, cudaStream_t s)
 template <int KT>
 void launchTopk(const uint16_t* emb, uint32_t n, int32_t* idx, float* score, uint32_t* status, cudaStream_t s)
 {
-    // 40 KB are used; asking for 120 KB keeps one CTA per SM, the one whose 512 tensor-memory columns
+    // 57 KB are used; asking for 120 KB keeps one CTA per SM, the one whose 512 tensor-memory columns
     // fit (a second CTA would wait in tcgen05.alloc until the first has finished)
     constexpr uint32_t smem = 120 * 1024;
-    static_assert(smem >= 128 * 32 * 2 + 2 * kTopkTile * 32 * 2, "top-k tiles");
+    static_assert(smem >= 128 * 32 * 2 + 2 * kTopkTile * 32 * 2 + kGemmThreads * 33 * 4, "top-k tiles and candidate rows");
     TDAG_CUDA(cudaFuncSetAttribute(topkKernel<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     topkKernel<KT><<<(n + 127) / 128, kGemmThreads, smem, s>>>(emb, n, idx, score, status);
     TDAG_LAUNCHED();
@@ -670,14 +737,16 @@ int tdag_nn_gemm(tdag_ctx* ctx, const tdag_nn_operand* a, const tdag_nn_operand*
         p.ldc = ldc;
         p.cBf16 = c_bf16 ? 1u : 0u;
         p.status = cx.status;
+        int sms = 0;
+        TDAG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cx.device));
         if (n <= 32)
-            launchGemm<32>(p, cx.stream);
+            launchGemm<32>(p, cx.stream, sms);
         else if (n <= 64)
-            launchGemm<64>(p, cx.stream);
+            launchGemm<64>(p, cx.stream, sms);
         else if (n <= 128)
-            launchGemm<128>(p, cx.stream);
+            launchGemm<128>(p, cx.stream, sms);
         else
-            launchGemm<256>(p, cx.stream);
+            launchGemm<256>(p, cx.stream, sms);
     });
 }
 
@@ -698,8 +767,8 @@ int tdag_nn_block_masks(tdag_ctx* ctx, const uint64_t* words, uint32_t n, uint32
     });
 }
 
-int tdag_nn_pool_forward(tdag_ctx* ctx, const float* z, const uint64_t* masks, uint32_t n, uint32_t blocks, float* u, uint16_t* u_bf16,
-    float* norm, float* count)
+int tdag_nn_pool_forward(tdag_ctx* ctx, const float* z, const uint32_t* row_of, const uint64_t* masks, uint32_t n, uint32_t blocks, float* u,
+    uint16_t* u_bf16, float* norm, float* count)
 {
     using namespace tdag;
     if (!ctx || (n && (!z || !masks || !u || !norm || !count)) || blocks == 0)
@@ -708,7 +777,7 @@ int tdag_nn_pool_forward(tdag_ctx* ctx, const float* z, const uint64_t* masks, u
         Context& cx = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(cx.device));
         if (n) {
-            poolForwardKernel<<<gridOf((uint64_t)n * 32, 256), 256, 0, cx.stream>>>(z, masks, n, blocks, u, u_bf16, norm, count);
+            poolForwardKernel<<<gridOf((uint64_t)n * 32, 256), 256, 0, cx.stream>>>(z, row_of, masks, n, blocks, u, u_bf16, norm, count);
             TDAG_LAUNCHED();
         }
     });

@@ -210,7 +210,7 @@ def lib(path: str = None):
         L.tdag_nn_gemm.argtypes = [vp, ctypes.POINTER(NnOperand), ctypes.POINTER(NnOperand), u32, u32, u32, f32, vp, ctypes.c_int, vp, u32,
                                    vp, u32, ctypes.c_int]
         L.tdag_nn_block_masks.argtypes = [vp, vp, u32, u32, vp]
-        L.tdag_nn_pool_forward.argtypes = [vp, vp, vp, u32, u32, vp, vp, vp, vp]
+        L.tdag_nn_pool_forward.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp]
         L.tdag_nn_pool_backward.argtypes = [vp, vp, vp, vp, vp, vp, u32, u32, vp]
         L.tdag_nn_info_nce.argtypes = [vp, vp, u32, vp, vp]
         L.tdag_nn_column_sums.argtypes = [vp, vp, u32, u32, u32, vp]

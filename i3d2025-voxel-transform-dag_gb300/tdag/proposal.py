@@ -102,13 +102,10 @@ class ProposalEncoder:
         masks = block_masks(self.ctx, words, level)
         return self.forward_masks(masks, keep)
 
-    def forward_masks(self, masks: torch.Tensor, keep: bool = False):
+    def _mlp(self, flat: torch.Tensor):
+        """The block MLP over a padded column of masks: (h1, h2, z)."""
         ctx, dev = self.ctx, self.device
-        n, B = masks.shape
-        rows = n * B
-        rows_p = max(16, (rows + 15) // 16 * 16)  # the weight gradients contract over rows: a multiple of 16
-        flat = torch.zeros(rows_p, dtype=torch.int64, device=dev)
-        flat[:rows] = masks.reshape(-1)
+        rows_p = flat.shape[0]
         h1 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
         h2 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
         z = torch.empty((rows_p, EMBED_DIM), dtype=torch.float32, device=dev)
@@ -116,15 +113,38 @@ class ProposalEncoder:
         gemm(ctx, _op(h1, _abi.NN_KMAJOR, HIDDEN), _op(self.w16[1], _abi.NN_KMAJOR, HIDDEN), rows_p, HIDDEN, HIDDEN, h2, bias=self.params[3],
              relu=True)
         gemm(ctx, _op(h2, _abi.NN_KMAJOR, HIDDEN), _op(self.w16[2], _abi.NN_KMAJOR, HIDDEN), rows_p, EMBED_DIM, HIDDEN, z, bias=self.params[5])
+        return h1, h2, z
+
+    @staticmethod
+    def _padded(col: torch.Tensor) -> torch.Tensor:
+        rows_p = max(16, (col.numel() + 15) // 16 * 16)  # the weight gradients contract over rows: a multiple of 16
+        flat = torch.zeros(rows_p, dtype=torch.int64, device=col.device)
+        flat[:col.numel()] = col.reshape(-1)
+        return flat
+
+    def forward_masks(self, masks: torch.Tensor, keep: bool = False):
+        """u and its bf16 copy from (n, B) block masks. Without keep (inference) the MLP runs once per
+        distinct mask -- its output depends on the mask alone -- and pooling gathers the rows."""
+        ctx, dev = self.ctx, self.device
+        n, B = masks.shape
+        if keep:
+            flat = self._padded(masks)
+            row_of = None
+        else:
+            uniq, inv = torch.unique(masks.reshape(-1), return_inverse=True)
+            flat = self._padded(uniq)
+            row_of = inv.to(torch.int32).contiguous()
+        h1, h2, z = self._mlp(flat)
         u = torch.empty((n, EMBED_DIM), dtype=torch.float32, device=dev)
         ub = torch.empty((n, EMBED_DIM), dtype=torch.bfloat16, device=dev)
         norm = torch.empty(n, dtype=torch.float32, device=dev)
         count = torch.empty(n, dtype=torch.float32, device=dev)
-        _abi.check(lib().tdag_nn_pool_forward(ctx.handle, z.data_ptr(), flat.data_ptr(), n, B, u.data_ptr(), ub.data_ptr(), norm.data_ptr(),
-                                              count.data_ptr()))
+        mk = masks.contiguous()
+        _abi.check(lib().tdag_nn_pool_forward(ctx.handle, z.data_ptr(), _ptr(row_of), mk.data_ptr(), n, B, u.data_ptr(), ub.data_ptr(),
+                                              norm.data_ptr(), count.data_ptr()))
         if not keep:
             return u, ub
-        return u, ub, {"masks": flat, "h1": h1, "h2": h2, "u": u, "norm": norm, "count": count, "n": n, "B": B, "rows_p": rows_p}
+        return u, ub, {"masks": flat, "h1": h1, "h2": h2, "u": u, "norm": norm, "count": count, "n": n, "B": B, "rows_p": flat.shape[0]}
 
     def backward(self, cache: dict, du: torch.Tensor) -> List[torch.Tensor]:
         """FP32 gradients [gw1, gb1, gw2, gb2, gw3, gb3] from d loss / d u (n x 32, FP32)."""
@@ -198,6 +218,7 @@ def _on_lib_stream(ctx):
 def embed(encoder: ProposalEncoder, words: torch.Tensor, level: int, chunk: int = 16384) -> torch.Tensor:
     """(n, 32) FP32 embeddings of n items, in chunks of items."""
     out = []
+    torch.cuda.synchronize(words.device)  # the items may come from another stream
     with _on_lib_stream(encoder.ctx):
         for a in range(0, words.shape[0], chunk):
             out.append(encoder.forward(words[a:a + chunk], level)[0])
@@ -261,8 +282,9 @@ def propose_lists(embeddings: torch.Tensor, positions: torch.Tensor, k: int, enc
     ctx = _ctx(encoder_ctx)
     kk = 8 if k <= 8 else (16 if k <= 16 else 32)
     assert k <= 32
-    order = torch.argsort(positions)  # sorted position -> original index
+    torch.cuda.synchronize(embeddings.device)  # the inputs may come from another stream
     with _on_lib_stream(ctx):
+        order = torch.argsort(positions)  # sorted position -> original index
         e = embeddings[order].to(torch.bfloat16).contiguous()
         idx = torch.empty((n, kk), dtype=torch.int32, device=e.device)
         score = torch.empty((n, kk), dtype=torch.float32, device=e.device)
@@ -358,16 +380,22 @@ class ProposalHook:
     def __init__(self, ctx, encoder: ProposalEncoder, k: int, device: int = 0):
         self.ctx, self.encoder, self.k, self.device = ctx, encoder, k, device
         self.sources: Dict[int, Tuple[int, int]] = {}  # level -> (items, proposed sources)
+        self.seconds: Dict[int, Tuple[float, float]] = {}  # level -> (embedding, scoring) wall seconds
         self.error: Optional[BaseException] = None
         self.fn = _abi.PROPOSAL_FN(self._call)
 
     def _call(self, user, level, d_grids, n, d_sources, num_sources):
+        import time
         try:
             W = (1 << (3 * level)) // 64
             words = torch.empty((n, W), dtype=torch.int64, device=f"cuda:{self.device}")
             _abi.check(lib().tdag_device_copy(self.ctx.handle, words.data_ptr(), d_grids, n * W * 8))
-            src = sources_of(propose_lists(embed(self.encoder, words, level), popcount_positions(words), self.k, self.encoder.ctx)).to(torch.int32)
+            t0 = time.perf_counter()
+            emb = embed(self.encoder, words, level)
+            t1 = time.perf_counter()
+            src = sources_of(propose_lists(emb, popcount_positions(words), self.k, self.encoder.ctx)).to(torch.int32)
             torch.cuda.synchronize(self.device)
+            self.seconds[level] = (t1 - t0, time.perf_counter() - t1)
             if src.numel():
                 _abi.check(lib().tdag_device_copy(self.ctx.handle, d_sources, src.data_ptr(), src.numel() * 4))
             num_sources[0] = src.numel()
@@ -432,4 +460,5 @@ def construct_transform_dag_proposed(in_dag, encoder: ProposalEncoder, k: int, c
     if hook.error is not None:
         raise hook.error
     _abi.check(rc)
+    construct_transform_dag_proposed.last_seconds = dict(hook.seconds)
     return DeviceResult(rp), hook.sources

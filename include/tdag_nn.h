@@ -52,11 +52,12 @@ int tdag_nn_gemm(tdag_ctx* ctx, const tdag_nn_operand* a, const tdag_nn_operand*
  * b = bx + (R/4) by + (R/4)^2 bz, mask bit dx + 4 dy + 16 dz. */
 int tdag_nn_block_masks(tdag_ctx* ctx, const uint64_t* words, uint32_t n, uint32_t level, uint64_t* masks);
 
-/* Mean over each item's non-empty blocks (mask != 0) of the 32-wide block outputs z[(i * B + b) * 32 + d],
- * then L2 normalisation: u[i * 32 + d] (FP32) and u_bf16 (optional), norm[i] (the pre-normalisation
+/* Mean over each item's non-empty blocks (mask != 0) of the 32-wide block outputs, row r = i * B + b
+ * of z (or row row_of[i * B + b] when row_of is given: the MLP then ran once per distinct mask), then
+ * L2 normalisation: u[i * 32 + d] (FP32) and u_bf16 (optional), norm[i] (the pre-normalisation
  * length, floored at 1e-12) and count[i] (non-empty blocks, floored at 1). */
-int tdag_nn_pool_forward(tdag_ctx* ctx, const float* z, const uint64_t* masks, uint32_t n, uint32_t blocks, float* u, uint16_t* u_bf16,
-    float* norm, float* count);
+int tdag_nn_pool_forward(tdag_ctx* ctx, const float* z, const uint32_t* row_of, const uint64_t* masks, uint32_t n, uint32_t blocks, float* u,
+    uint16_t* u_bf16, float* norm, float* count);
 
 /* Gradient of pool_forward: from du (FP32, n x 32) to dz (bf16, (n * B) x 32); zero for empty blocks. */
 int tdag_nn_pool_backward(tdag_ctx* ctx, const float* du, const float* u, const float* norm, const float* count, const uint64_t* masks,
