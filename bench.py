@@ -149,6 +149,10 @@ def run_proposal(args, world, rank, local, pg):
 
     ex_s, ex = timed(lambda: tdag.construct_transform_dag_device(g, cfg, ctx=ctx))
     ex_nodes = nodes_of(ex)
+    # the ceiling of any proposal method: only the exhaustive result's parents search (no network)
+    parents = P.exhaustive_parent_sets(g, cfg, ctx=ctx)
+    best_s, (best, best_src) = timed(lambda: P.construct_transform_dag_with_sources(g, parents, cfg, ctx=ctx))
+    best_nodes = nodes_of(best)
     modes = {}
     for k in (8, 32):
         s_k, (r, src) = timed(lambda: P.construct_transform_dag_proposed(g, enc, k, cfg, ctx=ctx))
@@ -163,6 +167,9 @@ def run_proposal(args, world, rank, local, pg):
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "u64 (encoder bf16)",
            "data": "synthetic (device-generated primitive scenes; training grids seeded 100..)", "config": workload_config(args, voxels),
            "exhaustive": {"ms": ex_s * 1e3, "mvoxels_per_s": voxels / ex_s / 1e6, "nodes": ex_nodes},
+           "parents_only": {"ms": best_s * 1e3, "speed_vs_exhaustive": ex_s / best_s, "nodes": best_nodes,
+                            "sources_per_level": {str(l): {"items": it, "sources": sc} for l, (it, sc) in best_src.items()},
+                            "note": "only the exhaustive result's parents search, no network: the ceiling of any proposal method"},
            "proposal": modes,
            "training": {"grids": args.train_grids, "resolution": 1024, "steps": args.train_steps, "label_s": t_labels, "train_s": t_train,
                         "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}}

@@ -662,6 +662,7 @@ void launchGemm(const GemmParams& p, cudaStream_t s, int smCount)
         TDAG_CUDA(cudaMemset2DAsync(p.c, (size_t)p.ldc * 4, 0, (size_t)p.N * 4, p.M, s));
     }
     const dim3 grid((p.M + 127) / 128, (p.N + BN - 1) / BN, splits);
+    TDAG_CHECK(grid.y <= 65535u && grid.z <= 65535u, TDAG_ERR_ARG, "tdag_nn_gemm: N too large for one launch");
     tcGemmKernel<BN><<<grid, kGemmThreads, smem, s>>>(p);
     TDAG_LAUNCHED();
 }

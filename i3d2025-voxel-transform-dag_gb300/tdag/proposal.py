@@ -462,3 +462,56 @@ def construct_transform_dag_proposed(in_dag, encoder: ProposalEncoder, k: int, c
     _abi.check(rc)
     construct_transform_dag_proposed.last_seconds = dict(hook.seconds)
     return DeviceResult(rp), hook.sources
+
+
+class FixedSourcesHook(ProposalHook):
+    """Lets a given set of items search at every level (original indices per level)."""
+
+    def __init__(self, ctx, sources_by_level: Dict[int, torch.Tensor], device: int = 0):
+        super().__init__(ctx, None, 0, device)
+        self.fixed = {l: v.to(torch.int32).contiguous() for l, v in sources_by_level.items()}
+
+    def _call(self, user, level, d_grids, n, d_sources, num_sources):
+        try:
+            src = self.fixed.get(level)
+            if src is None:
+                src = torch.arange(n, dtype=torch.int32, device=f"cuda:{self.device}")
+            torch.cuda.synchronize(self.device)
+            if src.numel():
+                _abi.check(lib().tdag_device_copy(self.ctx.handle, d_sources, src.data_ptr(), src.numel() * 4))
+            num_sources[0] = src.numel()
+            self.sources[level] = (n, src.numel())
+            return 0
+        except BaseException as e:
+            self.error = e
+            return 1
+
+
+def exhaustive_parent_sets(in_dag, config=None, ctx=None) -> Dict[int, torch.Tensor]:
+    """Per translation level, the items that are some other item's parent in the exhaustive build."""
+    from . import TransformDAGConfig, default_context
+    ctx = ctx or default_context()
+    config = config or TransformDAGConfig()
+    out = {}
+    for level, words in level_items(in_dag, config, ctx=ctx).items():
+        parent, _ = exhaustive_parents(ctx, words, level, config)
+        dup = parent != torch.arange(parent.shape[0], device=parent.device)
+        out[level] = torch.unique(parent[dup])
+    return out
+
+
+def construct_transform_dag_with_sources(in_dag, sources_by_level: Dict[int, torch.Tensor], config=None, ctx=None):
+    """constructTransformDAG where only the given items search at each translation level. With the
+    exhaustive result's parents (exhaustive_parent_sets) it yields the exhaustive TDAG with the fewest
+    sources: the speed no proposal method can exceed."""
+    from . import DeviceResult, TransformDAGConfig, _config_struct, default_context
+    ctx = ctx or default_context()
+    config = config or TransformDAGConfig()
+    hook = FixedSourcesHook(ctx, sources_by_level, device=torch.cuda.current_device())
+    v = in_dag.view()
+    rp = ctypes.POINTER(_abi.Result)()
+    rc = lib().tdag_build_device_proposed(ctx.handle, ctypes.byref(v), ctypes.byref(_config_struct(config)), hook.fn, None, ctypes.byref(rp))
+    if hook.error is not None:
+        raise hook.error
+    _abi.check(rc)
+    return DeviceResult(rp), hook.sources

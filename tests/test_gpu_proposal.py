@@ -70,3 +70,18 @@ def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx):
         rand = P.recall_at_k(P.random_lists(pos, 8), parent)
         print(f"level {level}: recall@8 learned {learned:.3f} popcount-neighbours {neighbours:.3f} random {rand:.3f}")
         assert learned > neighbours and learned > rand
+
+
+def test_parents_as_the_only_sources_give_the_exhaustive_tdag(tdaglib, gpu_ctx):
+    """The exhaustive result's parents are the smallest source set that still finds every merge: a
+    build where only they search is byte-identical to the exhaustive build (the speed ceiling of any
+    proposal method, which bench.py --workload proposal reports)."""
+    from tdag import proposal as P
+    cfg = tdaglib.TransformDAGConfig()
+    g = _scene(tdaglib, gpu_ctx, 256, 5)
+    parents = P.exhaustive_parent_sets(g, cfg, ctx=gpu_ctx)
+    res, sources = P.construct_transform_dag_with_sources(g, parents, cfg, ctx=gpu_ctx)
+    got = tdaglib.write_tdag(res.to_host(ctx=gpu_ctx), cfg)
+    want = tdaglib.write_tdag(tdaglib.construct_transform_dag_device(g, cfg, ctx=gpu_ctx).to_host(ctx=gpu_ctx), cfg)
+    assert got == want
+    assert all(s < n for n, s in sources.values())
