@@ -79,3 +79,17 @@ def test_voxel_count(oracle, tdaglib):
     d = blocky_grid(32, 8)
     s = tdaglib.EditStructure.from_svo_bytes(oracle.to_dag(oracle.svo_from_dense(d)))
     assert s.compute_voxel_count() == int(d.sum())
+
+
+def test_nn_entry_points_reject_bad_arguments_without_a_device(tdaglib):
+    """The learned-proposal kernels' entry points validate their arguments before touching a device."""
+    import ctypes as C
+    from tdag import _abi
+    L = tdaglib.lib()
+    op = _abi.NnOperand(None, _abi.NN_KMAJOR, 0)
+    assert L.tdag_nn_gemm(None, C.byref(op), C.byref(op), 1, 1, 16, 1.0, None, 0, None, 0, None, 1, 0) == _abi.TDAG_ERR_ARG
+    assert L.tdag_nn_topk(None, None, 0, 8, None, None) == _abi.TDAG_ERR_ARG
+    assert L.tdag_nn_block_masks(None, None, 0, 4, None) == _abi.TDAG_ERR_ARG
+    assert L.tdag_nn_adamw(None, None, None, None, None, 0, 1e-3, 0.9, 0.999, 1e-8, 0.0, 1, None) == _abi.TDAG_ERR_ARG
+    assert L.tdag_nn_info_nce(None, None, 0, None, None) == _abi.TDAG_ERR_ARG
+    assert L.tdag_nn_sync(None) == _abi.TDAG_ERR_ARG
