@@ -1746,10 +1746,10 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
     const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
-    // Source batches. Single grid: ranges of sorted positions growing 8x (levels 2-3: 16x; every batch
-    // costs a table rebuild, so a few large batches beat many small ones) after a first batch of one team
-    // per SM, starting at eight teams per SM (fixed, so that the schedule does not move with the probe
-    // kernel's occupancy). Batch: the same
+    // Source batches. Single grid: ranges of sorted positions growing by the factor below (every batch
+    // costs a pruning round, so a few large batches beat many small ones) after a first batch of one
+    // team per SM, starting at eight teams per SM (fixed, so that the schedule does not move with the
+    // probe kernel's occupancy). Batch: the same
     // fractions of every grid (1/512, 1/64, 1/8, 1), as a list of sorted positions per batch, with
     // each grid's own next-batch start for the pruning keys.
     std::vector<uint32_t> bounds { 0 };
@@ -1759,7 +1759,12 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const uint32_t nSrc = sources ? numSources : n;
     if (!batched) {
         const uint32_t minBatch = std::max<uint32_t>((uint32_t)ctx.numSMs * 8 * ProbeShape<R>::TEAMS, nSrc / 256);
-        const uint64_t growth = R == 16 ? 8 : 16; // smaller grids probe faster, so their rebuilds weigh more
+        // Growth per batch. Every batch ends in a pruning round (liveness pass, filter refresh or table
+        // rebuild); smaller grids probe faster, so their rounds weigh more: 16x at levels 2-3. At level
+        // 4, up to 384 Ki sources 32x (2048^3 bench grid, 272 K sources: 49.2 -> 47.7 ms per build),
+        // above that 8x, where the lookups the rounds save outweigh them (4096^3, 492 K sources: 91.4 ms
+        // at 8x, 92.6 ms at 32x; 8192^3: 186.1 against 194.5 ms).
+        const uint64_t growth = R == 16 ? (nSrc <= (384u << 10) ? 32 : 8) : 16;
         // A first batch of one team per SM: the largest sources give most targets that many sources
         // match (small, common boxes) their parent, and the pruning after it drops them, so that the
         // next batch's sources do not enumerate their table runs again.
