@@ -566,12 +566,31 @@ __global__ void targetLiveKernel(const unsigned long long* __restrict__ parents,
         atomicAdd(count, (uint32_t)__popc(votes));
 }
 
-// flags[e] = 1 for the entries of live targets (payload of a permuted corner view: item << 6 | view).
-__global__ void entryLiveKernel(const uint32_t* __restrict__ pays, size_t m, const uint8_t* __restrict__ live, uint32_t* __restrict__ flags)
+// flags[e] = 1 for the entries of live targets (payload of a permuted corner view: item << 6 | view);
+// *count = the live entries.
+// Grid-stride over a fixed grid, one atomic per block (a per-warp atomic on one counter serialises).
+__global__ void __launch_bounds__(256) entryLiveKernel(const uint32_t* __restrict__ pays, size_t m, const uint8_t* __restrict__ live,
+    uint32_t* __restrict__ flags, uint32_t* __restrict__ count)
 {
-    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < m)
-        flags[e] = live[pays[e] >> 6];
+    __shared__ uint32_t warpCounts[8];
+    uint32_t c = 0;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t l = live[pays[e] >> 6];
+        flags[e] = l;
+        c += l;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0)
+        warpCounts[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; ++w)
+            t += warpCounts[w];
+        if (t)
+            atomicAdd(count, t);
+    }
 }
 
 // Membership filter over the keys of the flagged entries only: a pruning round that keeps the table
@@ -1826,7 +1845,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     uint32_t* sparePays = p2.get();
     size_t mCur = m;
     DevBuf<uint8_t> targetLive(n, s);
-    DevBuf<uint32_t> liveCount(1, s);
+    DevBuf<uint32_t> liveCount(2, s); // live targets, live entries
     uint32_t maxBatch = 1;
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi)
         maxBatch = std::max(maxBatch, bounds[bi + 1] - bounds[bi]);
@@ -1853,13 +1872,18 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
             }
-            TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 4, s));
+            TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 8, s));
             targetLiveKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, minKeyNext, gridOf, batched ? minKeyDev.get() : nullptr, targetLive.get(),
                 liveCount.get());
             TDAG_LAUNCHED();
-            entryLiveKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curPays, mCur, targetLive.get(), flags.get());
+            entryLiveKernel<<<(unsigned)std::min<uint64_t>(gridFor(mCur, 256), (uint64_t)ctx.numSMs * 8), 256, 0, s>>>(curPays, mCur, targetLive.get(),
+                flags.get(), liveCount.get() + 1);
             TDAG_LAUNCHED();
-            const uint64_t live = exclusiveScanU32Total(flags.get(), liveIdx.get(), mCur, s);
+            // the live entries' count decides between a filter refresh (no scan needed) and a compaction
+            uint64_t* hp = pinnedScratch();
+            TDAG_CUDA(cudaMemcpyAsync(hp, liveCount.get(), 8, cudaMemcpyDeviceToHost, s));
+            TDAG_CUDA(cudaStreamSynchronize(s));
+            const uint64_t live = hp[0] >> 32;
             if (live == 0)
                 break;
             if (2 * live >= mCur && mCur <= (1ull << 25)) {
@@ -1872,6 +1896,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 liveFilterKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, flags.get(), mCur, table.filter.get(), table.filterShift);
                 TDAG_LAUNCHED();
             } else {
+                exclusiveScanU32(flags.get(), liveIdx.get(), mCur, s);
                 compactEntriesKernel<<<gridFor(mCur, 256), 256, 0, s>>>(curKeys, curPays, flags.get(), liveIdx.get(), mCur, spareKeys, sparePays);
                 TDAG_LAUNCHED();
                 std::swap(curKeys, spareKeys);
