@@ -553,17 +553,13 @@ __global__ void gatherPositionsKernel(const uint32_t* __restrict__ sources, uint
 }
 
 // Targets that a source at or after the next batch could still give a lower parent: live[t] = 1 when
-// parent[t] > the next batch's minimum key; *count = the live targets.
+// parent[t] > the next batch's minimum key.
 __global__ void targetLiveKernel(const unsigned long long* __restrict__ parents, uint32_t n, unsigned long long minKeyNext, const uint32_t* __restrict__ gridOf,
-    const unsigned long long* __restrict__ minKeyOfGrid, uint8_t* __restrict__ live, uint32_t* __restrict__ count)
+    const unsigned long long* __restrict__ minKeyOfGrid, uint8_t* __restrict__ live)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool l = t < n && parents[t] > (gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext);
     if (t < n)
-        live[t] = l ? 1 : 0;
-    const uint32_t votes = __ballot_sync(0xffffffffu, l);
-    if ((threadIdx.x & 31) == 0 && votes)
-        atomicAdd(count, (uint32_t)__popc(votes));
+        live[t] = parents[t] > (gridOf ? minKeyOfGrid[gridOf[t]] : minKeyNext) ? 1 : 0;
 }
 
 // flags[e] = 1 for the entries of live targets (payload of a permuted corner view: item << 6 | view);
@@ -1845,7 +1841,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     uint32_t* sparePays = p2.get();
     size_t mCur = m;
     DevBuf<uint8_t> targetLive(n, s);
-    DevBuf<uint32_t> liveCount(2, s); // live targets, live entries
+    DevBuf<uint32_t> liveCount(1, s); // live entries
     uint32_t maxBatch = 1;
     for (size_t bi = 0; bi + 1 < bounds.size(); ++bi)
         maxBatch = std::max(maxBatch, bounds[bi + 1] - bounds[bi]);
@@ -1872,18 +1868,17 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s));
             }
-            TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 8, s));
-            targetLiveKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, minKeyNext, gridOf, batched ? minKeyDev.get() : nullptr, targetLive.get(),
-                liveCount.get());
+            TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 4, s));
+            targetLiveKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, minKeyNext, gridOf, batched ? minKeyDev.get() : nullptr, targetLive.get());
             TDAG_LAUNCHED();
             entryLiveKernel<<<(unsigned)std::min<uint64_t>(gridFor(mCur, 256), (uint64_t)ctx.numSMs * 8), 256, 0, s>>>(curPays, mCur, targetLive.get(),
-                flags.get(), liveCount.get() + 1);
+                flags.get(), liveCount.get());
             TDAG_LAUNCHED();
             // the live entries' count decides between a filter refresh (no scan needed) and a compaction
             uint64_t* hp = pinnedScratch();
-            TDAG_CUDA(cudaMemcpyAsync(hp, liveCount.get(), 8, cudaMemcpyDeviceToHost, s));
+            TDAG_CUDA(cudaMemcpyAsync(hp, liveCount.get(), 4, cudaMemcpyDeviceToHost, s));
             TDAG_CUDA(cudaStreamSynchronize(s));
-            const uint64_t live = hp[0] >> 32;
+            const uint64_t live = hp[0] & 0xFFFFFFFFull;
             if (live == 0)
                 break;
             if (2 * live >= mCur && mCur <= (1ull << 25)) {
