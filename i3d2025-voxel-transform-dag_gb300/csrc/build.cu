@@ -1310,7 +1310,7 @@ StaticOut buildStatic(Context& c, const tdag_static_view& in, const tdag_config&
         if (m) {
             staticChildWordsKernel<<<gridFor(n, 256), 256, 0, s>>>(words[l].get(), starts[l].get(), n, base.get(), cnt.get(), keys.get(), vals.get());
             TDAG_LAUNCHED();
-            radixSortPairs(keys.get(), vals.get(), m, 0, 32, s);
+            radixSortPairs(keys.get(), vals.get(), m, 0, 32, s, c.status);
             distinctFlagsKernel<<<gridFor(m, 256), 256, 0, s>>>(keys.get(), m, flags.get());
             TDAG_LAUNCHED();
             u = compactFlags(flags.get(), idx.get(), m, s);

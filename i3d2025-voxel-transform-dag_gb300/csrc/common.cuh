@@ -272,7 +272,10 @@ void exclusiveScanU32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t 
 uint64_t* pinnedScratch();
 // Returns total (sum of in) by copying the last element; synchronises the stream.
 uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
-void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on bits [beginBit, endBit) of the key. With a status
+// word, arrays of more than one tile take the one-sweep path (a look-back wait that gives up records
+// TDAG_ERR_CUDA there); without one, the histogram / scan / scatter passes.
+void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t* status = nullptr);
 // Compact indices i in [0, n) with flags[i] != 0 into out (ascending); returns the count.
 uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s);
 

@@ -583,7 +583,7 @@ DevBuf<uint64_t> sortByReferenceCount(Context& c, const DevBuf<uint64_t>& items,
         if (count) {
             refKeysKernel<<<gridFor(count, kBlock), kBlock, 0, s>>>(counts.get(), count, maxCount, keys.get(), vals.get(), kept.get());
             TDAG_LAUNCHED();
-            radixSortPairs(keys.get(), vals.get(), count, 0, std::max(1u, bitWidth(maxCount)), s);
+            radixSortPairs(keys.get(), vals.get(), count, 0, std::max(1u, bitWidth(maxCount)), s, c.status);
         }
         TDAG_CUDA(cudaMemcpyAsync(&k, kept.get(), 4, cudaMemcpyDeviceToHost, s));
         c.checkStatus("encode16: reference counts");
@@ -690,7 +690,7 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
         if (m) {
             instanceKeysKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(nodes[l].get(), instSlots.get(), m, keys.get(), vals.get());
             TDAG_LAUNCHED();
-            radixSortPairs(keys.get(), vals.get(), m, 0, 64, s);
+            radixSortPairs(keys.get(), vals.get(), m, 0, 64, s, c.status);
             runFlagsKernel<<<gridFor(m, kBlock), kBlock, 0, s>>>(keys.get(), m, runFlag.get());
             TDAG_LAUNCHED();
             u = (uint32_t)exclusiveScanU32Total(runFlag.get(), runScan.get(), m, s);
@@ -708,7 +708,7 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
                 // the distinct pointers in first-occurrence order (runs are numbered by ascending value)
                 firstOccurrenceKeysKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(vals.get(), runStart.get(), u, countKeys.get(), byCount.get());
                 TDAG_LAUNCHED();
-                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(slots)), s);
+                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(slots)), s, c.status);
                 gatherValuesKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(runVal.get(), byCount.get(), u, countKeys.get());
                 TDAG_LAUNCHED();
                 std::vector<uint64_t> firstValues(u);
@@ -721,7 +721,7 @@ void encodeTdag16(Context& c, const tdag_result& dag, const tdag_config& cfg, co
                 TDAG_CUDA(cudaMemcpyAsync(byCount.get(), runOrder.data(), (uint64_t)u * 4, cudaMemcpyHostToDevice, s));
                 TDAG_CUDA(cudaStreamSynchronize(s)); // `runOrder` is released at the end of this scope
             } else {
-                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(m)), s);
+                radixSortPairs(countKeys.get(), byCount.get(), u, 0, std::max(1u, bitWidth(m)), s, c.status);
             }
             scatterRankKernel<<<gridFor(u, kBlock), kBlock, 0, s>>>(byCount.get(), u, rankOfRun.get());
             TDAG_LAUNCHED();

@@ -515,7 +515,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     gatherSortInputKernel<<<gridFor(u, 256), 256, 0, s>>>(canonList.get(), u, key, sk.get(), emitOrder.get());
     TDAG_LAUNCHED();
     canonList.release();
-    radixSortPairs(sk.get(), emitOrder.get(), u, 0, 64, s);
+    radixSortPairs(sk.get(), emitOrder.get(), u, 0, 64, s, ctx.status);
     if (gridOf && numGrids > 1) {
         // batched build: grid-major emission order, (grid, key, index), by a stable pass on the grid id
         gatherGridKeysKernel<<<gridFor(u, 256), 256, 0, s>>>(emitOrder.get(), u, gridOf, sk.get());
@@ -523,7 +523,7 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
         uint32_t bits = 8;
         while ((1ull << bits) < numGrids)
             bits += 8;
-        radixSortPairs(sk.get(), emitOrder.get(), u, 0, bits, s);
+        radixSortPairs(sk.get(), emitOrder.get(), u, 0, bits, s, ctx.status);
         handleOff = countPerGrid(gridOf, emitOrder.get(), u, numGrids, s);
     } else {
         handleOff = { 0, u };

@@ -1704,7 +1704,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         uint32_t bits = 16;
         while (batched && (1ull << (bits - 13)) < numGrids)
             bits += 8;
-        radixSortPairs(key.get(), order.get(), n, 0, bits, s);
+        radixSortPairs(key.get(), order.get(), n, 0, bits, s, ctx.status);
     }
 
     // learned-proposal mode: the sorted positions of the listed sources, ascending, as the work list
@@ -1719,7 +1719,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         if (numSources) {
             gatherPositionsKernel<<<gridFor(numSources, 256), 256, 0, s>>>(sources, numSources, rank.get(), n, sk.get(), subsetDev.get(), ctx.status);
             TDAG_LAUNCHED();
-            radixSortPairs(sk.get(), subsetDev.get(), numSources, 0, 32, s);
+            radixSortPairs(sk.get(), subsetDev.get(), numSources, 0, 32, s, ctx.status);
             subsetHost.resize(numSources);
             TDAG_CUDA(cudaMemcpyAsync(subsetHost.data(), subsetDev.get(), (size_t)numSources * 4, cudaMemcpyDeviceToHost, s));
         }
@@ -1811,7 +1811,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         TDAG_CUDA(cudaMemcpyAsync(workListDev.get(), workList.data(), workList.size() * 4, cudaMemcpyHostToDevice, s));
 
     // equal view keys side by side (the sort is stable: a run keeps item order)
-    radixSortPairs(ekeys.get(), epay.get(), m, kViewKeyLowBit, 64, s);
+    radixSortPairs(ekeys.get(), epay.get(), m, kViewKeyLowBit, 64, s, ctx.status);
     mark("view sort");
     Table table;
     buildRunTable(ctx, ekeys.get(), epay.get(), m, table);

@@ -422,9 +422,149 @@ __global__ void __launch_bounds__(kSortThreads) radixSortSmallKernel(uint64_t* _
         vals[i] = vfin[i];
     }
 }
+
+// ------------------------------------------------------------------------------------------------
+// One-sweep passes (for arrays of more than one tile): every digit's global histogram comes from one
+// read of the keys, and each pass is a single scatter launch whose tiles find their digits' global
+// offsets by decoupled look-back instead of a histogram kernel and a scan of the count matrix per
+// pass. Tiles take their index from a counter in launch order, so a tile only ever waits on tiles
+// that are already running; every wait is bounded and records TDAG_ERR_CUDA when it gives up.
+// status[tile * 256 + d] = flag << 30 | count: flag 1 = the tile's own count of digit d, flag 2 = the
+// inclusive count of tiles 0..tile.
+constexpr uint32_t kFlagAgg = 1u << 30, kFlagIncl = 2u << 30, kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kLookbackSpins = 1u << 22;
+
+__global__ void __launch_bounds__(kSortThreads) allDigitHistKernel(const uint64_t* __restrict__ keys, size_t n, uint32_t beginBit, uint32_t passes,
+    uint32_t* __restrict__ ghist)
+{
+    __shared__ uint32_t h[8 * 256];
+    for (int i = threadIdx.x; i < 8 * 256; i += kSortThreads)
+        h[i] = 0;
+    __syncthreads();
+    for (size_t i = (size_t)blockIdx.x * kSortThreads + threadIdx.x; i < n; i += (size_t)gridDim.x * kSortThreads) {
+        const uint64_t k = keys[i];
+        for (uint32_t p = 0; p < passes; ++p)
+            atomicAdd(&h[p * 256 + ((uint32_t)(k >> (beginBit + 8 * p)) & 0xFF)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < passes * 256; i += kSortThreads)
+        if (h[i])
+            atomicAdd(&ghist[i], h[i]);
+}
+
+__global__ void __launch_bounds__(kSortThreads, 3) onesweepScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+    uint64_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut, size_t n, uint32_t shift, const uint32_t* __restrict__ ghist,
+    uint32_t* __restrict__ tileCounter, uint32_t* __restrict__ status, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t* sk = reinterpret_cast<uint64_t*>(smem);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kSortTile);
+    uint32_t (*warpBase)[256] = reinterpret_cast<uint32_t (*)[256]>(sv + kSortTile);
+    uint32_t* tileStart = &warpBase[kSortWarps][0];
+    uint32_t* globalBase = tileStart + 256;
+    __shared__ uint32_t tileShared;
+    __shared__ uint32_t scratch[33];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        tileShared = atomicAdd(tileCounter, 1u);
+    for (int d = threadIdx.x; d < kSortWarps * 256; d += kSortThreads)
+        (&warpBase[0][0])[d] = 0;
+    __syncthreads();
+    const uint32_t tile = tileShared;
+    const size_t tileBase = (size_t)tile * kSortTile;
+    const size_t warpItems = tileBase + (size_t)warp * (32 * kSortRounds);
+    uint64_t key[kSortRounds];
+    uint32_t rank[kSortRounds / 2];
+    const uint32_t ltMask = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const size_t i = warpItems + (size_t)r * 32 + lane;
+        const bool valid = i < n;
+        key[r] = valid ? keysIn[i] : 0;
+        const uint32_t digit = valid ? (uint32_t)(key[r] >> shift) & 0xFF : 256u;
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit) & vmask;
+        const uint32_t before = valid ? warpBase[warp][digit] : 0u;
+        __syncwarp();
+        if (valid && (peers & ltMask) == 0)
+            warpBase[warp][digit] += __popc(peers);
+        __syncwarp();
+        const uint32_t rk = before + __popc(peers & ltMask);
+        if (r & 1)
+            rank[r >> 1] |= rk << 16;
+        else
+            rank[r >> 1] = rk;
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x; // 256 threads == 256 digits
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w)
+            cnt += warpBase[w][d];
+        // publish this tile's count of digit d at once: later tiles can pass over it
+        volatile uint32_t* mine = status + (size_t)tile * 256 + d;
+        *mine = (tile == 0 ? kFlagIncl : kFlagAgg) | cnt;
+        // the digit's first position in the output: exclusive scan of the pass's global histogram
+        uint32_t total;
+        const uint32_t digitBase = blockExclusiveScan(ghist[d], scratch, total);
+        // look back over the earlier tiles' counts of digit d
+        uint32_t excl = 0;
+        if (tile > 0) {
+            uint32_t j = tile - 1, spins = 0;
+            for (;;) {
+                const uint32_t v = *reinterpret_cast<volatile const uint32_t*>(status + (size_t)j * 256 + d);
+                const uint32_t flag = v & ~kCountMask;
+                if (flag == 0) {
+                    if (++spins > kLookbackSpins) {
+                        setDeviceError(err, TDAG_ERR_CUDA, 440);
+                        break;
+                    }
+                    continue;
+                }
+                excl += v & kCountMask;
+                if (flag == kFlagIncl)
+                    break;
+                --j; // tile 0 always publishes an inclusive count, so j stays >= 0
+            }
+            *mine = kFlagIncl | (excl + cnt);
+        }
+        // the tile's own digit runs (exclusive prefix over digits) and the warps' starts within them
+        const uint32_t start = blockExclusiveScan(cnt, scratch, total);
+        tileStart[d] = start;
+        globalBase[d] = digitBase + excl;
+        uint32_t run = start;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = warpBase[w][d];
+            warpBase[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        const size_t i = warpItems + (size_t)r * 32 + lane;
+        if (i < n) {
+            const uint32_t digit = (uint32_t)(key[r] >> shift) & 0xFF;
+            const uint32_t pos = warpBase[warp][digit] + ((rank[r >> 1] >> ((r & 1) * 16)) & 0xFFFFu);
+            sk[pos] = key[r];
+            sv[pos] = valsIn[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t tileItems = (uint32_t)((n - tileBase) < (size_t)kSortTile ? (n - tileBase) : (size_t)kSortTile);
+    for (uint32_t i = threadIdx.x; i < tileItems; i += kSortThreads) {
+        const uint64_t k = sk[i];
+        const uint32_t d = (uint32_t)(k >> shift) & 0xFF;
+        const uint32_t out = globalBase[d] + (i - tileStart[d]);
+        keysOut[out] = k;
+        valsOut[out] = sv[i];
+    }
+}
 } // namespace
 
-void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s)
+void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t* status)
 {
     if (n <= 1 || beginBit >= endBit)
         return;
@@ -436,6 +576,7 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
     if (dev < 0 || dev >= 64 || !smemSet[dev]) {
         TDAG_CUDA(cudaFuncSetAttribute(radixScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
         TDAG_CUDA(cudaFuncSetAttribute(radixSortSmallKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSortSmem));
+        TDAG_CUDA(cudaFuncSetAttribute(onesweepScatterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem));
         if (dev >= 0 && dev < 64)
             smemSet[dev] = true;
     }
@@ -446,20 +587,40 @@ void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit,
     }
     DevBuf<uint64_t> k2(n, s);
     DevBuf<uint32_t> v2(n, s);
-    DevBuf<uint32_t> counts((size_t)256 * numTiles, s), offs((size_t)256 * numTiles, s);
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = k2.get();
     uint32_t* vout = v2.get();
     uint32_t passes = 0;
-    for (uint32_t shift = beginBit; shift < endBit; shift += 8, ++passes) {
-        radixHistKernel<<<numTiles, kSortThreads, 0, s>>>(kin, n, shift, counts.get(), numTiles);
+    if (status && n < (size_t)kCountMask) {
+        // one-sweep: all histograms in one read, then one look-back scatter launch per pass
+        const uint32_t numPasses = (endBit - beginBit + 7) / 8;
+        DevBuf<uint32_t> ghist((size_t)numPasses * 256, s), counters(numPasses, s), lookback((size_t)256 * numTiles, s);
+        TDAG_CUDA(cudaMemsetAsync(ghist.get(), 0, ghist.bytes(), s));
+        TDAG_CUDA(cudaMemsetAsync(counters.get(), 0, counters.bytes(), s));
+        int sms = 0;
+        TDAG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        allDigitHistKernel<<<(unsigned)std::min<uint64_t>(numTiles, (uint64_t)sms * 4), kSortThreads, 0, s>>>(kin, n, beginBit, numPasses, ghist.get());
         TDAG_LAUNCHED();
-        exclusiveScanU32(counts.get(), offs.get(), (size_t)256 * numTiles, s);
-        radixScatterKernel<<<numTiles, kSortThreads, kScatterSmem, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
-        TDAG_LAUNCHED();
-        std::swap(kin, kout);
-        std::swap(vin, vout);
+        for (uint32_t p = 0; p < numPasses; ++p, ++passes) {
+            TDAG_CUDA(cudaMemsetAsync(lookback.get(), 0, lookback.bytes(), s));
+            onesweepScatterKernel<<<numTiles, kSortThreads, kScatterSmem, s>>>(kin, vin, kout, vout, n, beginBit + 8 * p, ghist.get() + (size_t)p * 256,
+                counters.get() + p, lookback.get(), status);
+            TDAG_LAUNCHED();
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
+    } else {
+        DevBuf<uint32_t> counts((size_t)256 * numTiles, s), offs((size_t)256 * numTiles, s);
+        for (uint32_t shift = beginBit; shift < endBit; shift += 8, ++passes) {
+            radixHistKernel<<<numTiles, kSortThreads, 0, s>>>(kin, n, shift, counts.get(), numTiles);
+            TDAG_LAUNCHED();
+            exclusiveScanU32(counts.get(), offs.get(), (size_t)256 * numTiles, s);
+            radixScatterKernel<<<numTiles, kSortThreads, kScatterSmem, s>>>(kin, vin, kout, vout, n, shift, offs.get(), numTiles);
+            TDAG_LAUNCHED();
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
     }
     if (passes & 1) {
         TDAG_CUDA(cudaMemcpyAsync(keys, kin, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
