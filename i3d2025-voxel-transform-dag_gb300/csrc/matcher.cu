@@ -1879,6 +1879,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             TDAG_CUDA(cudaMemcpyAsync(hp, liveCount.get(), 4, cudaMemcpyDeviceToHost, s));
             TDAG_CUDA(cudaStreamSynchronize(s));
             const uint64_t live = hp[0] & 0xFFFFFFFFull;
+            if (trace)
+                std::fprintf(stderr, "[tdag] L%d before batch %zu: %llu of %llu entries live\n", L, bi, (unsigned long long)live, (unsigned long long)mCur);
             if (live == 0)
                 break;
             if (2 * live >= mCur && mCur <= (1ull << 25)) {
