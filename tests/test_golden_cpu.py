@@ -1,7 +1,9 @@
 """The oracle against the committed golden digests (tests/golden/golden.json, written by
-tests/golden/make_golden.py). The small cases carry digests made by the reference's own code
-(compiled from its sources into oracle/_ref); the oracle re-derives them here on every run, on every
-machine, so the restatement stays pinned to the reference where the reference cannot be built."""
+tests/golden/make_golden.py). Every case carries digests made by the reference's own code (compiled
+from its sources into oracle/_ref); the oracle re-derives the small cases here on every run, on every
+machine, so the restatement stays pinned to the reference where the reference cannot be built. For
+the 2048^3 bench grid (the reference took 8806 s on one core, the oracle two minutes on 16) the
+committed reference and oracle digests are checked to agree."""
 import hashlib
 import json
 import os
@@ -47,3 +49,14 @@ def test_oracle_reproduces_reference_digests(oracle, key):
 def test_golden_file_covers_the_bench_grid():
     g = GOLDEN.get("scene2048")
     assert g is not None and len(g["tdag_sha256"]) == 64 and g["svo_bytes"] > 0
+
+
+def test_bench_grid_reference_digests_equal_the_oracle_digests():
+    """The 2048^3 bench grid's .svo, .tdag and four .tdag16 digests as the reference's own code wrote
+    them equal the oracle's (and the GPU test compares the library with both)."""
+    g = GOLDEN["scene2048"]
+    r = g["reference"]
+    keys = [k for k, v in r.items() if k.endswith("_sha256") and isinstance(v, str)]
+    assert {"svo_sha256", "tdag_sha256", "tdag16_tables_huffman_sha256", "tdag16_plain_sha256"} <= set(keys)
+    for k in keys:
+        assert r[k] == g[k], k
