@@ -704,15 +704,18 @@ __device__ __noinline__ bool verifyCandidateWarp(const uint64_t* __restrict__ tg
     uint32_t lane)
 {
     constexpr int ROWS = R * R;
+    constexpr int STEPS = (ROWS + 31) / 32;
     const uint16_t* L = lines + a0 * R * R;
     const int lo = otherLo(a0), hi = otherHi(a0);
-    for (int r0 = 0; r0 < ROWS; r0 += 32) {
-        const int r = r0 + (int)lane;
-        const bool ok = r >= ROWS || verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, r % R, r / R);
-        if (!__all_sync(0xffffffffu, ok))
-            return false;
+    // every row's loads are issued before the first compare (one memory latency per verification
+    // instead of one per step): most verified candidates pass, so stopping early would save little
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < STEPS; ++k) {
+        const int r = k * 32 + (int)lane;
+        ok &= r >= ROWS || verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, r % R, r / R);
     }
-    return true;
+    return __all_sync(0xffffffffu, ok);
 }
 
 template <int R, int L>
@@ -1380,14 +1383,14 @@ struct LookupParams {
     const uint32_t* gridOf;
     const uint32_t* segOff;
     uint32_t allowSym, allowPerm, allowTrans;
-    unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified
+    unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified, [6] longest run
 };
 
 template <int R, int L>
 __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
 {
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t cHit = 0, cCand = 0, cVer = 0, cOk = 0;
+    uint32_t cHit = 0, cCand = 0, cVer = 0, cOk = 0, cMaxRun = 0;
 
     // every candidate (target, corner view) of the hit recorded in `m` (find_translation.cpp:820-864)
     struct Src {
@@ -1474,6 +1477,7 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
             }
         }
         cHit += cnt ? 1u : 0u;
+        cMaxRun = max(cMaxRun, cnt);
         // The warp's candidates, all hits' ranges end to end, dealt 32 at a time over the lanes: lane
         // j's hit is the first lane whose inclusive prefix of counts exceeds j (binary search by shuffles).
         uint32_t incl = cnt;
@@ -1535,6 +1539,9 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         if (lane == 0 && v)
             atomicAdd(&p.counters[2 + k], v);
     }
+    cMaxRun = __reduce_max_sync(0xffffffffu, cMaxRun);
+    if (lane == 0 && cMaxRun)
+        atomicMax(&p.counters[6], (unsigned long long)cMaxRun); // the longest run a record met (diagnostics)
 }
 
 // ---------------------------------------------------------------------------- resolve
@@ -2011,8 +2018,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             TDAG_CUDA(cudaEventElapsedTime(&ms, batchEv.back().first, batchEv.back().second));
             unsigned long long c[8];
             TDAG_CUDA(cudaMemcpy(c, counters.get(), 64, cudaMemcpyDeviceToHost));
-            std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f (probe %.3f lookup %.3f records %llu) | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu\n",
-                L, bi, b1 - b0, (unsigned long long)table.numEntries, ms, traceProbeMs, traceLookupMs, traceRecords, c[0], c[1], c[2], c[3], c[4]);
+            std::fprintf(stderr, "[tdag] L%d batch %zu sources %u table %llu ms %.3f (probe %.3f lookup %.3f records %llu) | cumulative probes %llu filter %llu hits %llu cand %llu ver %llu longest run %llu\n",
+                L, bi, b1 - b0, (unsigned long long)table.numEntries, ms, traceProbeMs, traceLookupMs, traceRecords, c[0], c[1], c[2], c[3], c[4], c[6]);
             traceProbeMs = traceLookupMs = 0;
             traceRecords = 0;
         }
