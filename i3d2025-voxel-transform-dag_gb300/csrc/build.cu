@@ -179,31 +179,45 @@ __global__ void flattenKernel(LevelPtrs lp, const uint32_t* __restrict__ indices
         return;
     const uint32_t item = (uint32_t)(gid / W), w = (uint32_t)(gid % W);
     const uint32_t orig = indices[item];
+    // A word's 64 bits touch at most four 4^3 leaves (R = 16: the four x-blocks of four rows; R = 8:
+    // 2 x 2 blocks in x and y; R = 4: one). Each is fetched once, and the walks are independent, so
+    // their loads overlap.
+    auto slotOf = [](uint32_t x, uint32_t y) -> uint32_t { return R == 16 ? (x >> 2) & 3u : (R == 8 ? ((x >> 2) & 1u) | (((y >> 2) & 1u) << 1) : 0u); };
+    uint64_t leaf[4] = { 0, 0, 0, 0 };
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+        // the first bit group of the word that falls into slot q
+        uint32_t g0 = 16;
+#pragma unroll
+        for (uint32_t g = 0; g < 16; ++g) {
+            const uint32_t b = 64 * w + 4 * g;
+            if (g0 == 16 && slotOf(b % R, (b / R) % R) == q)
+                g0 = g;
+        }
+        if (g0 == 16)
+            continue;
+        const uint32_t b = 64 * w + 4 * g0;
+        const uint32_t x = b % R, y = (b / R) % R, z = b / (R * R);
+        uint32_t idx = orig;
+        bool empty = false;
+        for (int lvl = L; lvl > 2; --lvl) {
+            const uint32_t c = ((x >> (lvl - 1)) & 1) | (((y >> (lvl - 1)) & 1) << 1) | (((z >> (lvl - 1)) & 1) << 2);
+            idx = lp.nodes[lvl][(size_t)idx * 8 + c];
+            if (idx == kEmpty32) {
+                empty = true;
+                break;
+            }
+        }
+        leaf[q] = empty ? 0 : lp.leaves[idx];
+    }
     uint64_t word = 0;
-    uint32_t cachedKey = 0xFFFFFFFFu;
-    uint64_t cachedLeaf = 0;
-#pragma unroll 4
+#pragma unroll
     for (uint32_t g = 0; g < 16; ++g) {
         const uint32_t b = 64 * w + 4 * g;
         const uint32_t x = b % R, y = (b / R) % R, z = b / (R * R);
-        const uint32_t lkey = (x >> 2) | ((y >> 2) << 4) | ((z >> 2) << 8);
-        if (lkey != cachedKey) {
-            cachedKey = lkey;
-            uint32_t idx = orig;
-            bool empty = false;
-            for (int lvl = L; lvl > 2; --lvl) {
-                const uint32_t c = ((x >> (lvl - 1)) & 1) | (((y >> (lvl - 1)) & 1) << 1) | (((z >> (lvl - 1)) & 1) << 2);
-                idx = lp.nodes[lvl][(size_t)idx * 8 + c];
-                if (idx == kEmpty32) {
-                    empty = true;
-                    break;
-                }
-            }
-            cachedLeaf = empty ? 0 : lp.leaves[idx];
-        }
         const uint32_t ly = y & 3, lz = z & 3;
         const uint32_t base = ((ly & 1) << 1) | ((lz & 1) << 2) | ((ly >> 1) << 4) | ((lz >> 1) << 5);
-        const uint64_t m = cachedLeaf;
+        const uint64_t m = leaf[slotOf(x, y)];
         const uint64_t row = ((m >> base) & 1) | (((m >> (base + 1)) & 1) << 1) | (((m >> (base + 8)) & 1) << 2) | (((m >> (base + 9)) & 1) << 3);
         word |= row << (4 * g);
     }
