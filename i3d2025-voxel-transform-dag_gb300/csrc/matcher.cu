@@ -1384,6 +1384,7 @@ struct LookupParams {
     const uint32_t* segOff;
     uint32_t allowSym, allowPerm, allowTrans;
     unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified, [6] longest run
+    unsigned long long* cursor; // set: warps claim 32 records at a time from it (zeroed before the launch)
 };
 
 template <int R, int L>
@@ -1455,9 +1456,18 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
         geo = (uint32_t)a0 | ((uint32_t)a1 << 2) | (S << 4) | ((uint32_t)(T0 + 32) << 8) | ((uint32_t)(T1 + 32) << 14) | ((uint32_t)(T2 + 32) << 20);
         return true;
     };
-    // persistent warps: each takes 32 consecutive records per step
+    // persistent warps, 32 consecutive records per step: with a cursor each warp claims its next 32
+    // (balances the few-record batches whose records differ most in verification work; one counter
+    // would serialise the claims of the large batches, which take records by a fixed stride)
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < p.count; i0 += stride) {
+    uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    if (p.cursor) {
+        unsigned long long c = 0;
+        if (lane == 0)
+            c = atomicAdd(p.cursor, 32ull);
+        i0 = __shfl_sync(0xffffffffu, c, 0);
+    }
+    for (; i0 < p.count;) {
         const uint64_t i = i0 + lane;
         uint32_t start = 0, cnt = 0;
         uint64_t meta = 0;
@@ -1528,6 +1538,14 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
                     atomicMin(&p.parents[vt], (unsigned long long)vk);
                 }
             }
+        }
+        if (p.cursor) {
+            unsigned long long c = 0;
+            if (lane == 0)
+                c = atomicAdd(p.cursor, 32ull);
+            i0 = __shfl_sync(0xffffffffu, c, 0);
+        } else {
+            i0 += stride;
         }
     }
     const uint32_t vals[4] = { cHit, cCand, cVer, cOk };
@@ -1748,6 +1766,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<unsigned long long> parents(n, s);
     fillU64(reinterpret_cast<uint64_t*>(parents.get()), sentinelKey, n, s);
     DevBuf<uint32_t> work(1, s);
+    DevBuf<unsigned long long> lookupCursor(1, s);
     DevBuf<unsigned long long> counters(8, s);
     TDAG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, s));
 
@@ -1994,6 +2013,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 lp.count = produced;
                 lp.begin = pos;
                 lp.srcLines = srcLines.get();
+                lp.cursor = nullptr;
+                if (produced < (1ull << 20)) { // few records: balance them dynamically
+                    lp.cursor = lookupCursor.get();
+                    TDAG_CUDA(cudaMemsetAsync(lp.cursor, 0, 8, s));
+                }
                 const uint64_t warpsNeeded = (produced + 31) / 32;
                 const unsigned lblocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)lookupBlocks, (warpsNeeded + kThreads / 32 - 1) / (kThreads / 32)));
                 if (trace)
