@@ -64,6 +64,7 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: 256, or the grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="batch96: skip the CUDA-graph replay of the batched build")
     ap.add_argument("--cpu-baseline", default="auto", choices=["auto", "full", "sample"],
                     help="full: the oracle on the whole grid once (auto: up to 2048^3); sample: random sub-volumes only")
     ap.add_argument("--cpu-baseline-timeout", type=float, default=900.0, help="seconds allowed to the whole-grid oracle build")
@@ -233,6 +234,37 @@ def run_batch(args, world, rank, local, pg):
         exact &= single.to_host(tctx).to_bytes() == r.to_host(tctx).to_bytes()
         single.free()
         r.free()
+    # the same build captured in one CUDA graph (tdag_batch_graph_*), against the eager call, both
+    # timed around the whole call (host round trips and result copies included)
+    graph_info = None
+    if not args.no_graph:
+        def call_ms(fn, reps):
+            ms = []
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                res, st = fn()
+                torch.cuda.synchronize()
+                ms.append((time.perf_counter() - t0) * 1e3)
+                for r in res:
+                    r.free()
+            return float(statistics.median(ms)), st
+        eager_call, _ = call_ms(lambda: tdag.construct_transform_dag_batched_device(devs, cfg, ctx=tctx), max(args.steps, 3))
+        t0 = time.perf_counter()
+        graph = tdag.BatchGraph(devs, cfg, ctx=tctx)
+        create_ms = (time.perf_counter() - t0) * 1e3
+        first, _ = graph.launch()
+        g_exact = True
+        for d, r in zip(devs, first):
+            single = tdag.construct_transform_dag_device(d, cfg, ctx=tctx)
+            g_exact &= single.to_host(tctx).to_bytes() == r.to_host(tctx).to_bytes()
+            single.free()
+            r.free()
+        graph_call, gst = call_ms(graph.launch, max(args.steps, 3))
+        graph.free()
+        graph_info = {"call_ms": graph_call, "device_ms": gst["total_ms"], "kernel_nodes": gst["kernel_launches"], "create_ms": create_ms,
+                      "eager_call_ms": eager_call, "speedup_vs_eager_call": eager_call / graph_call if graph_call > 0 else None,
+                      "bit_exact_vs_per_grid": bool(g_exact)}
     dev_ms = max_over_ranks(pg, dev_ms)
     value = total_voxels * args.steps / (dev_ms / 1e3) / 1e6  # the whole batch over the slowest rank's time
     out = {
@@ -249,6 +281,8 @@ def run_batch(args, world, rank, local, pg):
         "speedup_vs_per_grid": per_grid_ms / (dev_ms / args.steps) if dev_ms > 0 else None,
         "clocks": clk, "gpu_launches": int(launches),
     }
+    if graph_info is not None:
+        out["graph"] = graph_info
     if rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -9,6 +9,7 @@
 //      transform_dag.cpp:44-116, 417-441), run the matcher, keep the unique items (:208-221) and
 //      rewrite the parents' child pointers through the mapping (:224-233; the lower_bound lookup is
 //      a rank array here).
+#include <array>
 #include <chrono>
 #include <cstring>
 #include <memory>
@@ -73,14 +74,13 @@ const TransformTables& hostTables()
 
 uint32_t Context::takeStatus(uint32_t* aux)
 {
-    TDAG_CUDA(cudaMemcpyAsync(hostStatus, status, 16, cudaMemcpyDeviceToHost, stream));
-    TDAG_CUDA(cudaStreamSynchronize(stream));
+    readToHost({ { hostStatus, status, 16 } }, stream);
     const uint32_t code = hostStatus[0];
     if (aux)
         *aux = hostStatus[1];
     if (code != 0) {
         TDAG_CUDA(cudaMemsetAsync(status, 0, 16, stream));
-        TDAG_CUDA(cudaStreamSynchronize(stream));
+        syncHost(stream);
     }
     return code;
 }
@@ -306,8 +306,8 @@ static DevBuf<uint32_t> uploadU32(const std::vector<uint64_t>& v, cudaStream_t s
 {
     std::vector<uint32_t> h(v.begin(), v.end());
     DevBuf<uint32_t> d(h.size(), s);
-    TDAG_CUDA(cudaMemcpyAsync(d.get(), h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
-    TDAG_CUDA(cudaStreamSynchronize(s));
+    uploadToDevice(d.get(), h.data(), h.size() * 4, s);
+    syncHost(s);
     return d;
 }
 
@@ -427,10 +427,14 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
     cudaStream_t s = ctx.stream;
     ctx.tableRegrows = 0;
     const uint64_t launches0 = g_kernelLaunches.load();
-    TDAG_CUDA(cudaEventRecord(ctx.ev[2], s));
+    // stage timing (not while a batch graph captures the build: its events would not complete)
+    const bool timed = !replaying();
+    if (timed)
+        TDAG_CUDA(cudaEventRecord(ctx.ev[2], s));
     const uint32_t midLevel = cfg.max_translation_level + 1;
     HierOutput h = runHierarchical(ctx, in, cfg, cfg.translation ? midLevel : 0xFFFFFFFFu, stats);
-    TDAG_CUDA(cudaEventRecord(ctx.ev[3], s));
+    if (timed)
+        TDAG_CUDA(cudaEventRecord(ctx.ev[3], s));
     DeviceResult out;
     out.levels.resize(in.rootLevel + 1);
     out.off = h.handleOff;
@@ -457,9 +461,10 @@ static DeviceResult buildDevice(Context& ctx, const DeviceSvdag& in, const tdag_
                 translationLevel<2>(ctx, in, out, cfg, stats, hook);
         }
     }
-    TDAG_CUDA(cudaEventRecord(ctx.ev[4], s));
+    if (timed)
+        TDAG_CUDA(cudaEventRecord(ctx.ev[4], s));
     ctx.checkStatus("build");
-    if (stats) {
+    if (stats && timed) {
         TDAG_CUDA(cudaEventElapsedTime(&stats->hierarchical_ms, ctx.ev[2], ctx.ev[3]));
         TDAG_CUDA(cudaEventElapsedTime(&stats->translation_ms, ctx.ev[3], ctx.ev[4]));
         TDAG_CUDA(cudaEventElapsedTime(&stats->total_ms, ctx.ev[2], ctx.ev[4]));
@@ -995,6 +1000,298 @@ int tdag_build_batched(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count,
 int tdag_build_batched_device(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count, const tdag_config* cfg, tdag_result** out, tdag_stats* batchStats)
 {
     return buildBatched(ctx, in, count, cfg, out, batchStats, false);
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// Batch graph: the batched build recorded once, then captured into one CUDA graph and replayed.
+// ------------------------------------------------------------------------------------------------
+namespace tdag {
+namespace {
+
+// One input array of the batch: the caller's device pointer and its place in the snapshot.
+struct InputSpan {
+    const uint32_t* src;
+    uint64_t off; // in 32-bit words, into the snapshot
+    uint64_t words;
+};
+
+constexpr uint32_t kSpanBlocks = 64; // blocks per input array in the comparison
+
+// Counts the words of every input array that differ from the snapshot (block b: array b / 64).
+__global__ void compareSpansKernel(const InputSpan* __restrict__ spans, const uint32_t* __restrict__ snap, unsigned long long* __restrict__ diff)
+{
+    const InputSpan sp = spans[blockIdx.x / kSpanBlocks];
+    const uint64_t stride = (uint64_t)kSpanBlocks * blockDim.x;
+    uint32_t d = 0;
+    for (uint64_t i = (uint64_t)(blockIdx.x % kSpanBlocks) * blockDim.x + threadIdx.x; i < sp.words; i += stride)
+        d += sp.src[i] != snap[sp.off + i];
+    d = __reduce_add_sync(0xffffffffu, d);
+    if ((threadIdx.x & 31) == 0 && d)
+        atomicAdd(diff, (unsigned long long)d);
+}
+
+struct TapeScope {
+    explicit TapeScope(ControlTape* t) { setActiveTape(t); }
+    ~TapeScope() { setActiveTape(nullptr); }
+};
+
+// Offsets and counts of every grid's levels in a build's concatenated output, and the copies that
+// place them contiguously (each level 256-byte aligned) in an arena.
+struct OutputLayout {
+    std::vector<std::array<uint64_t, TDAG_MAX_LEVELS>> off, count; // per grid; off in bytes into the arena
+    uint64_t bytes = 0;
+};
+
+OutputLayout layoutOf(const DeviceResult& dr, const tdag_svdag_view* in, uint32_t count)
+{
+    OutputLayout L;
+    L.off.resize(count);
+    L.count.resize(count);
+    for (uint32_t g = 0; g < count; ++g) {
+        L.off[g].fill(0);
+        L.count[g].fill(0);
+        for (uint32_t l = 2; l <= in[g].root_level; ++l) {
+            const auto& off = dr.off[l];
+            const uint64_t cnt = off.empty() ? 0 : off[g + 1] - off[g];
+            L.off[g][l] = L.bytes;
+            L.count[g][l] = cnt;
+            L.bytes += (cnt * (l == 2 ? 1 : 8) * 8 + 255) & ~255ull;
+        }
+    }
+    return L;
+}
+
+void copyToArena(const DeviceResult& dr, const tdag_svdag_view* in, uint32_t count, const OutputLayout& L, unsigned char* arena, cudaStream_t s)
+{
+    for (uint32_t g = 0; g < count; ++g)
+        for (uint32_t l = 2; l <= in[g].root_level; ++l) {
+            const uint64_t words = (l == 2) ? 1 : 8, cnt = L.count[g][l];
+            if (!cnt)
+                continue;
+            const uint64_t* src = ((l == 2) ? dr.leaves.get() : dr.levels[l].get()) + dr.off[l][g] * words;
+            TDAG_CUDA(cudaMemcpyAsync(arena + L.off[g][l], src, cnt * words * 8, cudaMemcpyDeviceToDevice, s));
+        }
+}
+
+} // namespace
+} // namespace tdag
+
+struct tdag_batch_graph {
+    tdag_ctx* ctx = nullptr;
+    tdag_config cfg {};
+    std::vector<tdag_svdag_view> views;
+    std::vector<InputSpan> spans;
+    uint32_t* snap = nullptr; // device copy of every input array at creation
+    InputSpan* spansDev = nullptr;
+    unsigned long long* diff = nullptr; // differing input words (device)
+    ControlTape tape;
+    unsigned char* uploadsDev = nullptr;
+    uint32_t* mismatch = nullptr;
+    OutputLayout layout;
+    unsigned char* arena = nullptr; // the graph's output, grid by grid
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernelNodes = 0;
+
+    ~tdag_batch_graph()
+    {
+        if (ctx) {
+            cudaSetDevice(ctx->c.device);
+            cudaStreamSynchronize(ctx->c.stream);
+        }
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        for (void* p : { (void*)snap, (void*)spansDev, (void*)diff, (void*)uploadsDev, (void*)mismatch, (void*)arena })
+            if (p)
+                cudaFree(p);
+        if (ctx)
+            cudaDeviceGraphMemTrim(ctx->c.device);
+    }
+};
+
+extern "C" {
+
+int tdag_batch_graph_create(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t count, const tdag_config* cfg, tdag_batch_graph** out)
+{
+    if (!ctx || !cfg || !out || !in || count == 0)
+        return fail(TDAG_ERR_ARG, "null argument or empty batch");
+    *out = nullptr;
+    auto G = std::make_unique<tdag_batch_graph>();
+    const int rc = guarded([&] {
+        for (uint32_t g = 0; g < count; ++g) {
+            checkView(&in[g]);
+            TDAG_CHECK(in[g].resolution == (1u << in[g].root_level), TDAG_ERR_ARG, "resolution must equal 1 << root_level");
+            if (cfg->translation)
+                TDAG_CHECK(in[g].root_level >= cfg->max_translation_level + 1, TDAG_ERR_ARG, "root_level must exceed max_translation_level");
+        }
+        Context& c = ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        for (uint32_t g = 0; g < count; ++g)
+            requireDeviceView(c, in[g]);
+        G->ctx = ctx;
+        G->cfg = *cfg;
+        G->views.assign(in, in + count);
+
+        // snapshot of the inputs, compared with the caller's arrays before every launch
+        uint64_t words = 0;
+        for (uint32_t g = 0; g < count; ++g) {
+            auto add = [&](const void* p, uint64_t bytes) {
+                if (!bytes)
+                    return;
+                G->spans.push_back({ static_cast<const uint32_t*>(p), words, bytes / 4 });
+                words += (bytes / 4 + 63) & ~63ull;
+            };
+            add(in[g].leaves, in[g].leaf_count * 8);
+            for (uint32_t l = 3; l <= in[g].root_level; ++l)
+                add(in[g].nodes[l], in[g].node_counts[l] * 32);
+        }
+        TDAG_CUDA(cudaMalloc(&G->snap, std::max<uint64_t>(words, 1) * 4));
+        for (const InputSpan& sp : G->spans)
+            TDAG_CUDA(cudaMemcpyAsync(G->snap + sp.off, sp.src, sp.words * 4, cudaMemcpyDeviceToDevice, s));
+        TDAG_CUDA(cudaMalloc(&G->spansDev, std::max<size_t>(G->spans.size(), 1) * sizeof(InputSpan)));
+        if (!G->spans.empty())
+            TDAG_CUDA(cudaMemcpyAsync(G->spansDev, G->spans.data(), G->spans.size() * sizeof(InputSpan), cudaMemcpyHostToDevice, s));
+        TDAG_CUDA(cudaMalloc(&G->diff, 8));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+
+        // 1. the plan: an ordinary build that records every host read and upload
+        ControlTape& t = G->tape;
+        {
+            TapeScope scope(&t);
+            BatchInput b;
+            concatBatch(c, in, count, false, b);
+            DeviceResult dr = buildDevice(c, b.view, *cfg, nullptr);
+            G->layout = layoutOf(dr, in, count);
+            syncHost(s);
+        }
+        TDAG_CUDA(cudaMalloc(&G->uploadsDev, std::max<size_t>(t.uploads.size(), 1)));
+        if (!t.uploads.empty())
+            TDAG_CUDA(cudaMemcpy(G->uploadsDev, t.uploads.data(), t.uploads.size(), cudaMemcpyHostToDevice));
+        TDAG_CUDA(cudaMalloc(&G->mismatch, 4));
+        TDAG_CUDA(cudaMemset(G->mismatch, 0, 4));
+        TDAG_CUDA(cudaMalloc(&G->arena, std::max<uint64_t>(G->layout.bytes, 256)));
+        preloadTapeKernels();
+        t.replay = true;
+        t.readPos = t.uploadPos = 0;
+        t.readIndex = 0;
+        t.uploadsDev = G->uploadsDev;
+        t.mismatch = G->mismatch;
+
+        // 2. the same build captured: sizes and launch shapes come from the plan
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        TDAG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        try {
+            TapeScope scope(&t);
+            BatchInput b;
+            concatBatch(c, in, count, false, b);
+            DeviceResult dr = buildDevice(c, b.view, *cfg, nullptr);
+            copyToArena(dr, in, count, G->layout, G->arena, s);
+        } catch (...) {
+            cudaGraph_t broken = nullptr;
+            cudaStreamEndCapture(s, &broken);
+            if (broken)
+                cudaGraphDestroy(broken);
+            cudaGetLastError();
+            throw;
+        }
+        TDAG_CUDA(cudaStreamEndCapture(s, &G->graph));
+        TDAG_CHECK(t.readPos == t.reads.size() && t.uploadPos == t.uploads.size(), TDAG_ERR_CUDA,
+            "batch graph: the captured build did not replay its whole plan");
+        size_t numNodes = 0;
+        TDAG_CUDA(cudaGraphGetNodes(G->graph, nullptr, &numNodes));
+        std::vector<cudaGraphNode_t> nodes(numNodes);
+        if (numNodes)
+            TDAG_CUDA(cudaGraphGetNodes(G->graph, nodes.data(), &numNodes));
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType ty;
+            TDAG_CUDA(cudaGraphNodeGetType(nd, &ty));
+            G->kernelNodes += ty == cudaGraphNodeTypeKernel;
+        }
+        TDAG_CUDA(cudaGraphInstantiate(&G->exec, G->graph, 0));
+        TDAG_CUDA(cudaGraphUpload(G->exec, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
+    });
+    if (rc != TDAG_OK)
+        return rc;
+    *out = G.release();
+    return TDAG_OK;
+}
+
+int tdag_batch_graph_launch(tdag_batch_graph* G, tdag_result** out, tdag_stats* stats)
+{
+    if (!G || !out)
+        return fail(TDAG_ERR_ARG, "null argument");
+    const uint32_t count = (uint32_t)G->views.size();
+    for (uint32_t g = 0; g < count; ++g)
+        out[g] = nullptr;
+    return guarded([&] {
+        Context& c = G->ctx->c;
+        cudaStream_t s = c.stream;
+        TDAG_CUDA(cudaSetDevice(c.device));
+        uint64_t* hp = pinnedScratch();
+        // the batch must hold the contents the graph was planned on
+        if (!G->spans.empty()) {
+            TDAG_CUDA(cudaMemsetAsync(G->diff, 0, 8, s));
+            compareSpansKernel<<<(unsigned)(G->spans.size() * kSpanBlocks), 256, 0, s>>>(G->spansDev, G->snap, G->diff);
+            TDAG_LAUNCHED();
+            readToHost({ { hp, G->diff, 8 } }, s);
+            TDAG_CHECK(hp[0] == 0, TDAG_ERR_ARG, "the batch's arrays changed since the graph was created (" + std::to_string(hp[0]) + " words differ)");
+        }
+        TDAG_CUDA(cudaMemsetAsync(G->mismatch, 0, 4, s));
+        TDAG_CUDA(cudaEventRecord(c.ev[2], s));
+        TDAG_CUDA(cudaGraphLaunch(G->exec, s));
+        TDAG_CUDA(cudaEventRecord(c.ev[3], s));
+        readToHost({ { c.hostStatus, c.status, 16 }, { hp, G->mismatch, 4 } }, s);
+        const uint32_t code = c.hostStatus[0], aux = c.hostStatus[1];
+        const uint32_t mismatch = (uint32_t)hp[0];
+        if (code) {
+            TDAG_CUDA(cudaMemsetAsync(c.status, 0, 16, s));
+            TDAG_CUDA(cudaStreamSynchronize(s));
+            throw Error((int)code, "batch graph: device reported error " + std::to_string(code) + " (aux " + std::to_string(aux) + ")");
+        }
+        TDAG_CHECK(mismatch == 0, TDAG_ERR_CUDA, "batch graph: the replay differed from its plan at host read " + std::to_string(mismatch - 1));
+        tdag_stats st;
+        std::memset(&st, 0, sizeof(st));
+        TDAG_CUDA(cudaEventElapsedTime(&st.total_ms, c.ev[2], c.ev[3]));
+        st.kernel_launches = G->kernelNodes;
+        std::vector<std::unique_ptr<tdag_result>> res(count);
+        for (uint32_t g = 0; g < count; ++g) {
+            const tdag_svdag_view& v = G->views[g];
+            res[g].reset(newResult(v.resolution, v.root_level, true));
+            res[g]->stats = st;
+            for (uint32_t l = 2; l <= v.root_level; ++l) {
+                const uint64_t cnt = G->layout.count[g][l];
+                const size_t bytes = cnt * (l == 2 ? 1 : 8) * 8;
+                uint64_t* dst = nullptr;
+                TDAG_CUDA(cudaMalloc(&dst, bytes ? bytes : 8));
+                if (l == 2) {
+                    res[g]->leaves = dst;
+                    res[g]->leaf_count = cnt;
+                } else {
+                    res[g]->nodes[l] = dst;
+                    res[g]->node_counts[l] = cnt;
+                }
+                if (bytes)
+                    TDAG_CUDA(cudaMemcpyAsync(dst, G->arena + G->layout.off[g][l], bytes, cudaMemcpyDeviceToDevice, s));
+            }
+        }
+        TDAG_CUDA(cudaStreamSynchronize(s));
+        for (uint32_t g = 0; g < count; ++g)
+            out[g] = res[g].release();
+        if (stats)
+            *stats = st;
+    });
+}
+
+int tdag_batch_graph_free(tdag_batch_graph* G)
+{
+    delete G;
+    return TDAG_OK;
 }
 
 int tdag_build_hierarchical(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg, tdag_result** out)

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <atomic>
 #include <cstdio>
+#include <initializer_list>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -278,6 +279,52 @@ uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cuda
 void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t* status = nullptr);
 // Compact indices i in [0, n) with flags[i] != 0 into out (ascending); returns the count.
 uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s);
+
+// ------------------------------------------------------------------------------------------------
+// Host links of a build (primitives.cu). Every value a build reads back to steer itself (counts,
+// totals, status words), every stream synchronisation it waits on and every host-to-device upload
+// of host-computed data goes through these four calls. With no tape on the calling thread (the
+// default) they copy and synchronise as they always did. A batch graph (tdag_batch_graph_create)
+// builds once with a recording tape, which keeps every value read, the free device memory queried
+// and every uploaded byte, and then captures the same build into a CUDA graph with a replaying
+// tape: a read returns the recorded value and enqueues a device check that the replayed build
+// computed the same value (a difference sets the tape's mismatch word), a synchronisation is
+// dropped, and an upload comes from a device copy of the recorded bytes, so that the graph needs
+// no host memory when it runs.
+// ------------------------------------------------------------------------------------------------
+struct HostRead {
+    void* dst; // host
+    const void* src; // device
+    size_t bytes; // a multiple of 4
+};
+struct ControlTape {
+    bool replay = false;
+    std::string reads; // bytes of every read, in order
+    size_t readPos = 0;
+    std::string uploads; // bytes of every upload, in order
+    size_t uploadPos = 0;
+    const unsigned char* uploadsDev = nullptr; // device copy of `uploads` (replay)
+    uint32_t* mismatch = nullptr; // device word (replay): 1 + the index of the first read that differed
+    uint32_t readIndex = 0;
+};
+ControlTape* activeTape(); // the calling thread's tape, or null
+void setActiveTape(ControlTape* tape);
+inline bool replaying()
+{
+    const ControlTape* t = activeTape();
+    return t && t->replay;
+}
+// Copies each item to the host and waits for them (replay: the recorded values, checked on the device).
+void readToHost(std::initializer_list<HostRead> items, cudaStream_t s);
+// Waits for the stream (replay: nothing; the graph's own order holds).
+void syncHost(cudaStream_t s);
+// Stream-ordered upload of host bytes (replay: from the device copy of the recorded bytes). Like
+// cudaMemcpyAsync from pageable memory, `src` may be reused once the call returns.
+void uploadToDevice(void* dst, const void* src, size_t bytes, cudaStream_t s);
+// Free device memory (cudaMemGetInfo), recorded and replayed like a read.
+uint64_t deviceFreeBytes();
+// Loads the replay check's kernel now, so that no module loads while a stream is being captured.
+void preloadTapeKernels();
 
 // Statistics accumulated over one build (device counters for the matcher).
 struct LevelStats {

@@ -575,13 +575,13 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
         canonByte[b] = (uint8_t)best;
     }
     DevBuf<uint8_t> dCanonByte(256, s);
-    TDAG_CUDA(cudaMemcpyAsync(dCanonByte.get(), canonByte, 256, cudaMemcpyHostToDevice, s));
+    uploadToDevice(dCanonByte.get(), canonByte, 256, s);
 
     HierOutput out;
     out.levels.resize(in.rootLevel + 1);
     out.handleOff.resize(in.rootLevel + 1);
     // per-level diagnostics on stderr (TDAG_TRACE): device time, items and kept items
-    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+    const bool trace = std::getenv("TDAG_TRACE") != nullptr && !replaying();
     std::vector<cudaEvent_t> traceEv;
     std::vector<std::pair<uint64_t, uint64_t>> traceCounts;
     auto traceMark = [&](uint64_t items, uint64_t kept) {
@@ -607,8 +607,8 @@ HierOutput runHierarchical(Context& ctx, const DeviceSvdag& in, const tdag_confi
     auto uploadOffsets = [&](const std::vector<uint64_t>& off) {
         DevBuf<uint32_t> d(off.size(), s);
         std::vector<uint32_t> o32(off.begin(), off.end());
-        TDAG_CUDA(cudaMemcpyAsync(d.get(), o32.data(), o32.size() * 4, cudaMemcpyHostToDevice, s));
-        TDAG_CUDA(cudaStreamSynchronize(s));
+        uploadToDevice(d.get(), o32.data(), o32.size() * 4, s);
+        syncHost(s);
         return d;
     };
     {

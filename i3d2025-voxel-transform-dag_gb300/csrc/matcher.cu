@@ -1668,8 +1668,7 @@ void buildRunTable(Context& ctx, const uint64_t* keys, const uint32_t* pays, siz
         tileMaxScanKernel<<<1, kPlaceThreads, 0, s>>>(tileMax.get(), tiles, maxAll.get());
         TDAG_LAUNCHED();
         uint64_t* h = pinnedScratch();
-        TDAG_CUDA(cudaMemcpyAsync(h, maxAll.get(), 8, cudaMemcpyDeviceToHost, s));
-        TDAG_CUDA(cudaStreamSynchronize(s));
+        readToHost({ { h, maxAll.get(), 8 } }, s);
         maxHomeMinusIndex = (long long)h[0];
     }
     // last run at runs - 1 + max(home - index); probes start at homes up to cap - 1; one empty slot after both
@@ -1704,11 +1703,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     }
     TDAG_CHECK(n < (1u << 29), TDAG_ERR_ARG, "too many items for one matcher level");
     TDAG_CHECK(!sources || !batched, TDAG_ERR_ARG, "a source subset applies to a single grid");
+    TDAG_CHECK(!sources || !replaying(), TDAG_ERR_ARG, "a source subset cannot be captured in a batch graph");
     const uint32_t* gridOf = batched ? seg->gridOf : nullptr;
     const uint32_t* segOff = batched ? seg->offDev : nullptr;
 
     // per-stage diagnostics on stderr (TDAG_TRACE)
-    const bool trace = std::getenv("TDAG_TRACE") != nullptr;
+    const bool trace = std::getenv("TDAG_TRACE") != nullptr && !replaying();
+    // probe and batch timing (not while a batch graph captures the build: its events would not complete)
+    const bool timed = !replaying();
     std::vector<std::pair<const char*, cudaEvent_t>> marks;
     auto mark = [&](const char* name) {
         if (!trace)
@@ -1780,8 +1782,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     perSM = std::max(perSM, 1);
     const uint32_t maxBlocks = (uint32_t)ctx.numSMs * perSM;
     // survivor records: at most a quarter of the free device memory per probed range
-    size_t freeBytes = 0, totalBytes = 0;
-    TDAG_CUDA(cudaMemGetInfo(&freeBytes, &totalBytes));
+    const uint64_t freeBytes = deviceFreeBytes();
     const uint64_t maxRecords = std::max<uint64_t>(1u << 20, freeBytes / 4 / sizeof(ulonglong2));
     int lookupPerSM = 0;
     TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
@@ -1834,7 +1835,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     DevBuf<uint32_t> workListDev(workList.size(), s);
     DevBuf<unsigned long long> minKeyDev(numGrids, s);
     if (!workList.empty())
-        TDAG_CUDA(cudaMemcpyAsync(workListDev.get(), workList.data(), workList.size() * 4, cudaMemcpyHostToDevice, s));
+        uploadToDevice(workListDev.get(), workList.data(), workList.size() * 4, s);
 
     // equal view keys side by side (the sort is stable: a run keeps item order)
     radixSortPairs(ekeys.get(), epay.get(), m, kViewKeyLowBit, 64, s, ctx.status);
@@ -1891,8 +1892,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             // drop targets whose parent no source at or after this batch can lower
             const unsigned long long minKeyNext = encodeFixed64(sources ? subsetHost[b0] : b0, 0, 0, 1 - R, 1 - R, 1 - R, L);
             if (batched) {
-                TDAG_CUDA(cudaMemcpyAsync(minKeyDev.get(), minKeys[bi].data(), numGrids * 8, cudaMemcpyHostToDevice, s));
-                TDAG_CUDA(cudaStreamSynchronize(s));
+                uploadToDevice(minKeyDev.get(), minKeys[bi].data(), (size_t)numGrids * 8, s);
+                syncHost(s);
             }
             TDAG_CUDA(cudaMemsetAsync(liveCount.get(), 0, 4, s));
             targetLiveKernel<<<gridFor(n, 256), 256, 0, s>>>(parents.get(), n, minKeyNext, gridOf, batched ? minKeyDev.get() : nullptr, targetLive.get());
@@ -1902,8 +1903,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             TDAG_LAUNCHED();
             // the live entries' count decides between a filter refresh (no scan needed) and a compaction
             uint64_t* hp = pinnedScratch();
-            TDAG_CUDA(cudaMemcpyAsync(hp, liveCount.get(), 4, cudaMemcpyDeviceToHost, s));
-            TDAG_CUDA(cudaStreamSynchronize(s));
+            readToHost({ { hp, liveCount.get(), 4 } }, s);
             const uint64_t live = hp[0] & 0xFFFFFFFFull;
             if (trace)
                 std::fprintf(stderr, "[tdag] L%d before batch %zu: %llu of %llu entries live\n", L, bi, (unsigned long long)live, (unsigned long long)mCur);
@@ -1957,10 +1957,12 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
         lp.allowTrans = cfg.translation ? 1 : 0;
         lp.counters = counters.get();
         // batch timing events, read once the level has finished (no round trip per batch)
-        batchEv.emplace_back();
-        TDAG_CUDA(cudaEventCreate(&batchEv.back().first));
-        TDAG_CUDA(cudaEventCreate(&batchEv.back().second));
-        TDAG_CUDA(cudaEventRecord(batchEv.back().first, s));
+        if (timed) {
+            batchEv.emplace_back();
+            TDAG_CUDA(cudaEventCreate(&batchEv.back().first));
+            TDAG_CUDA(cudaEventCreate(&batchEv.back().second));
+            TDAG_CUDA(cudaEventRecord(batchEv.back().first, s));
+        }
         // Probe ranges of the batch sized so that their records fit; a range whose records overflow
         // the buffer is probed again after the buffer grew to the exact count (or, past the memory
         // limit, as two halves).
@@ -1980,15 +1982,16 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_CUDA(cudaMemsetAsync(recCount.get(), 0, 8, s));
                 const uint64_t groups = ((uint64_t)cs + ProbeShape<R>::TEAMS - 1) / ProbeShape<R>::TEAMS;
                 const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(maxBlocks, groups));
-                TDAG_CUDA(cudaEventRecord(ctx.ev[5], s)); // ev[2..4] time the build's stages
+                if (timed)
+                    TDAG_CUDA(cudaEventRecord(ctx.ev[5], s)); // ev[2..4] time the build's stages
                 probe<<<blocks, kThreads, smem, s>>>(pp);
                 TDAG_LAUNCHED();
-                TDAG_CUDA(cudaEventRecord(ctx.ev[6], s));
+                if (timed)
+                    TDAG_CUDA(cudaEventRecord(ctx.ev[6], s));
                 uint64_t* hp = pinnedScratch();
-                TDAG_CUDA(cudaMemcpyAsync(hp, recCount.get(), 8, cudaMemcpyDeviceToHost, s));
-                TDAG_CUDA(cudaStreamSynchronize(s));
+                readToHost({ { hp, recCount.get(), 8 } }, s);
                 produced = hp[0];
-                {
+                if (timed) {
                     float pm = 0; // the stream was synchronised for the record count
                     TDAG_CUDA(cudaEventElapsedTime(&pm, ctx.ev[5], ctx.ev[6]));
                     probeMs += pm;
@@ -1996,8 +1999,9 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 }
                 if (produced <= pp.recCap)
                     break;
-                // the discarded run's probe and filter counts are rolled back
-                TDAG_CUDA(cudaMemcpyAsync(counters.get(), probeCounts, 16, cudaMemcpyHostToDevice, s));
+                // the discarded run's probe and filter counts (diagnostics) are rolled back
+                if (timed)
+                    TDAG_CUDA(cudaMemcpyAsync(counters.get(), probeCounts, 16, cudaMemcpyHostToDevice, s));
                 if (produced <= maxRecords) {
                     recsPerSource = std::max(recsPerSource, (double)produced / cs);
                     recs = DevBuf<ulonglong2>(produced, s);
@@ -2006,7 +2010,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                     cs = (cs + 1) / 2;
                 }
             }
-            TDAG_CUDA(cudaMemcpyAsync(probeCounts, counters.get(), 16, cudaMemcpyDeviceToHost, s));
+            if (timed)
+                TDAG_CUDA(cudaMemcpyAsync(probeCounts, counters.get(), 16, cudaMemcpyDeviceToHost, s));
             recsPerSource = 0.5 * recsPerSource + 0.5 * ((double)produced / cs);
             if (produced) {
                 lp.recs = recs.get();
@@ -2035,7 +2040,8 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             }
             pos += cs;
         }
-        TDAG_CUDA(cudaEventRecord(batchEv.back().second, s));
+        if (timed)
+            TDAG_CUDA(cudaEventRecord(batchEv.back().second, s));
         if (trace) {
             TDAG_CUDA(cudaEventSynchronize(batchEv.back().second));
             float ms = 0;
@@ -2072,13 +2078,13 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     TDAG_LAUNCHED();
     out.uniqueOff = batched ? countPerGrid(gridOf, out.uniques.get(), out.numUnique, numGrids, s) : std::vector<uint64_t> { 0, out.numUnique };
 
-    TDAG_CUDA(cudaStreamSynchronize(s));
+    syncHost(s);
     for (auto& e : batchEv) {
         float ms = 0;
         TDAG_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
         searchMs += ms;
     }
-    if (stats) {
+    if (stats && timed) {
         unsigned long long c[8];
         TDAG_CUDA(cudaMemcpyAsync(c, counters.get(), 64, cudaMemcpyDeviceToHost, s));
         TDAG_CUDA(cudaStreamSynchronize(s));

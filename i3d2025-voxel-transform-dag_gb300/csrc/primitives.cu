@@ -3,6 +3,7 @@
 // The reference sorts with std::sort / std::stable_sort (find_translation.cpp:639,727;
 // transform_dag_hierarchical.cpp:378). These kernels give the same orders: a stable sort on the key,
 // with values fed in ascending index order, yields (key, index) order.
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -121,15 +122,108 @@ uint64_t* pinnedScratch()
     return words;
 }
 
+// ------------------------------------------------------------------------------------------------
+// Host links (common.cuh): plain copies and synchronisations, or a recording / replaying tape.
+// ------------------------------------------------------------------------------------------------
+namespace {
+thread_local ControlTape* t_tape = nullptr;
+
+// FNV-1a over 32-bit words, the same on both sides of a replayed read.
+__host__ __device__ __forceinline__ uint64_t fnvWords(const uint32_t* w, size_t words)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (size_t i = 0; i < words; ++i)
+        h = (h ^ w[i]) * 0x100000001b3ull;
+    return h;
+}
+
+// One thread: the replayed build's value of a read against the recorded one.
+__global__ void tapeExpectKernel(const uint32_t* __restrict__ src, size_t words, uint64_t expected, uint32_t* mismatch, uint32_t readIndex)
+{
+    if (threadIdx.x == 0 && fnvWords(src, words) != expected)
+        atomicCAS(mismatch, 0u, readIndex + 1);
+}
+} // namespace
+
+ControlTape* activeTape() { return t_tape; }
+void preloadTapeKernels()
+{
+    cudaFuncAttributes fa;
+    TDAG_CUDA(cudaFuncGetAttributes(&fa, tapeExpectKernel));
+}
+void setActiveTape(ControlTape* tape) { t_tape = tape; }
+
+void readToHost(std::initializer_list<HostRead> items, cudaStream_t s)
+{
+    ControlTape* t = t_tape;
+    if (t && t->replay) {
+        for (const HostRead& r : items) {
+            TDAG_CHECK(t->readPos + r.bytes <= t->reads.size(), TDAG_ERR_CUDA, "batch graph: the captured build reads more than its plan recorded");
+            std::memcpy(r.dst, t->reads.data() + t->readPos, r.bytes);
+            t->readPos += r.bytes;
+            TDAG_CHECK(r.bytes % 4 == 0, TDAG_ERR_ARG, "host reads are whole 32-bit words");
+            const uint64_t h = fnvWords(static_cast<const uint32_t*>(r.dst), r.bytes / 4);
+            tapeExpectKernel<<<1, 32, 0, s>>>(static_cast<const uint32_t*>(r.src), r.bytes / 4, h, t->mismatch, t->readIndex++);
+            TDAG_LAUNCHED();
+        }
+        return;
+    }
+    for (const HostRead& r : items)
+        TDAG_CUDA(cudaMemcpyAsync(r.dst, r.src, r.bytes, cudaMemcpyDeviceToHost, s));
+    TDAG_CUDA(cudaStreamSynchronize(s));
+    if (t)
+        for (const HostRead& r : items)
+            t->reads.append(static_cast<const char*>(r.dst), r.bytes);
+}
+
+void syncHost(cudaStream_t s)
+{
+    if (!replaying())
+        TDAG_CUDA(cudaStreamSynchronize(s));
+}
+
+void uploadToDevice(void* dst, const void* src, size_t bytes, cudaStream_t s)
+{
+    if (bytes == 0)
+        return;
+    ControlTape* t = t_tape;
+    if (t && t->replay) {
+        TDAG_CHECK(t->uploadPos + bytes <= t->uploads.size() && std::memcmp(t->uploads.data() + t->uploadPos, src, bytes) == 0, TDAG_ERR_CUDA,
+            "batch graph: the captured build uploads other bytes than its plan");
+        TDAG_CUDA(cudaMemcpyAsync(dst, t->uploadsDev + t->uploadPos, bytes, cudaMemcpyDeviceToDevice, s));
+        t->uploadPos += bytes;
+        return;
+    }
+    TDAG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    if (t)
+        t->uploads.append(static_cast<const char*>(src), bytes);
+}
+
+uint64_t deviceFreeBytes()
+{
+    ControlTape* t = t_tape;
+    uint64_t v = 0;
+    if (t && t->replay) {
+        TDAG_CHECK(t->readPos + 8 <= t->reads.size(), TDAG_ERR_CUDA, "batch graph: the captured build reads more than its plan recorded");
+        std::memcpy(&v, t->reads.data() + t->readPos, 8);
+        t->readPos += 8;
+        return v;
+    }
+    size_t freeBytes = 0, totalBytes = 0;
+    TDAG_CUDA(cudaMemGetInfo(&freeBytes, &totalBytes));
+    v = freeBytes;
+    if (t)
+        t->reads.append(reinterpret_cast<const char*>(&v), 8);
+    return v;
+}
+
 uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s)
 {
     if (n == 0)
         return 0;
     exclusiveScanU32(in, out, n, s);
     uint32_t* pair = reinterpret_cast<uint32_t*>(pinnedScratch());
-    TDAG_CUDA(cudaMemcpyAsync(&pair[0], in + n - 1, 4, cudaMemcpyDeviceToHost, s));
-    TDAG_CUDA(cudaMemcpyAsync(&pair[1], out + n - 1, 4, cudaMemcpyDeviceToHost, s));
-    TDAG_CUDA(cudaStreamSynchronize(s));
+    readToHost({ { &pair[0], in + n - 1, 4 }, { &pair[1], out + n - 1, 4 } }, s);
     return (uint64_t)pair[0] + pair[1];
 }
 
@@ -184,8 +278,7 @@ std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx,
         countPerGridKernel<<<gridFor(n, 256), 256, 0, s>>>(gridIds, idx, n, counts.get());
         TDAG_LAUNCHED();
         std::vector<uint32_t> c(numGrids);
-        TDAG_CUDA(cudaMemcpyAsync(c.data(), counts.get(), numGrids * 4, cudaMemcpyDeviceToHost, s));
-        TDAG_CUDA(cudaStreamSynchronize(s));
+        readToHost({ { c.data(), counts.get(), (size_t)numGrids * 4 } }, s);
         for (uint32_t g = 0; g < numGrids; ++g)
             off[g + 1] = off[g] + c[g];
     }

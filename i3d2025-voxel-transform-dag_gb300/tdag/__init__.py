@@ -527,6 +527,45 @@ def construct_transform_dag_batched_device(dags: List["DeviceSvdag"], config: Tr
     return [DeviceResult(outs[i]) for i in range(len(dags))], _abi.stats_to_dict(st, root)
 
 
+class BatchGraph:
+    """A batched build captured in one CUDA graph (tdag_batch_graph_create / _launch / _free).
+
+    Creation builds the device-resident batch once, recording every value the build reads back, and
+    captures the same build into a graph; ``launch()`` replays it in one cudaGraphLaunch and returns
+    the device results (equal to construct_transform_dag_batched_device's) and the stats. The batch's
+    arrays must keep their contents: a launch on changed arrays raises TDagError (TDAG_ERR_ARG)."""
+
+    def __init__(self, dags: List["DeviceSvdag"], config: TransformDAGConfig = TransformDAGConfig(), ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.dags = list(dags)  # the inputs stay alive with the graph
+        self.count = len(self.dags)
+        views = (_abi.SvdagView * max(1, self.count))()
+        self.root = 2
+        for i, d in enumerate(self.dags):
+            views[i] = d.view()
+            self.root = max(self.root, views[i].root_level)
+        h = ctypes.c_void_p()
+        _abi.check(lib().tdag_batch_graph_create(self.ctx.handle, views, self.count, ctypes.byref(_config_struct(config)), ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self):
+        outs = (ctypes.POINTER(_abi.Result) * max(1, self.count))()
+        st = _abi.Stats()
+        _abi.check(lib().tdag_batch_graph_launch(self.handle, outs, ctypes.byref(st)))
+        return [DeviceResult(outs[i]) for i in range(self.count)], _abi.stats_to_dict(st, self.root)
+
+    def free(self):
+        if getattr(self, "handle", None):
+            lib().tdag_batch_graph_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------------------------------------
 # .tdag16 encoding (include/tdag16.h)
 # ------------------------------------------------------------------------------------------------

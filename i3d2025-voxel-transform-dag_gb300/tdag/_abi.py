@@ -129,6 +129,7 @@ EXPORTED = (
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_build_static", "tdag_static_result_free",
+    "tdag_batch_graph_create", "tdag_batch_graph_launch", "tdag_batch_graph_free",
     "tdag_l2_probe_peak",  # include/tdag_diag.h
     "tdag_device_pool_usage",  # include/tdag_diag.h
     "tdag_encode16", "tdag16_result_free", "tdag16_huffman_code_table",  # include/tdag16.h
@@ -221,6 +222,9 @@ def lib(path: str = None):
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]
+        L.tdag_batch_graph_create.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config), ctypes.POINTER(vp)]
+        L.tdag_batch_graph_launch.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]
+        L.tdag_batch_graph_free.argtypes = [vp]
         _lib = L
     return _lib
 

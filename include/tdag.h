@@ -152,6 +152,27 @@ int tdag_build_batched(tdag_ctx* ctx, const tdag_svdag_view* in_host, uint32_t c
 int tdag_build_batched_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, uint32_t count, const tdag_config* config,
     tdag_result** out, tdag_stats* batch_stats);
 
+/* Batched build captured in one CUDA graph (no reference counterpart; the host-side batching it
+ * replaces is find_translation.cpp:661-664, 771). tdag_batch_graph_create builds the device-resident
+ * batch once as tdag_build_batched_device does, recording every value the build reads back to steer
+ * itself (compaction counts, scan totals, probe record counts, live table entries, status words),
+ * and then captures the same build -- every stage of every level, for the whole batch -- into one
+ * CUDA graph whose sizes and launch shapes are those values. The views' device arrays must stay
+ * allocated while the graph lives; the graph snapshots their contents.
+ * tdag_batch_graph_launch replays the graph: one cudaGraphLaunch, no host round trip inside the
+ * build. It first compares the views' arrays with the snapshot on the device and returns
+ * TDAG_ERR_ARG, without launching, if any word changed (a changed batch needs a new graph). Every
+ * read the replay would have made is checked on the device against the recorded value; a
+ * difference returns TDAG_ERR_CUDA. out[i] (device-resident, released with tdag_result_free) equals
+ * tdag_build_batched_device's out[i] bit for bit. stats (may be NULL) receives total_ms (the
+ * graph's device time) and kernel_launches (the graph's kernel nodes). Calls are synchronous on the
+ * context's stream. Learned-proposal hooks cannot be captured. */
+typedef struct tdag_batch_graph tdag_batch_graph;
+int tdag_batch_graph_create(tdag_ctx* ctx, const tdag_svdag_view* in_device, uint32_t count, const tdag_config* config,
+    tdag_batch_graph** out);
+int tdag_batch_graph_launch(tdag_batch_graph* graph, tdag_result** out, tdag_stats* stats);
+int tdag_batch_graph_free(tdag_batch_graph* graph);
+
 /* findDuplicatesAmongFlattenedItems_cpp2<Level>(items, grids, outPrevLevelMapping, config)
  * (transform_dag.h:307-308; tools/lib/src/voxel/find_translation.cpp:616-1000), on dense grids:
  * grids = n x (R^3 / 64) uint64 words, R = 1 << level, bit index x + R*y + R*R*z

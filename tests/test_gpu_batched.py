@@ -49,3 +49,63 @@ def test_batched_device_scenes(oracle, tdaglib, gpu_ctx):
             assert rc.node_counts[lvl] == len(rs.nodes_per_level[lvl])
         single.free()
         r.free()
+
+
+def _scene_batch(tdaglib, gpu_ctx):
+    specs = [tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=r, seed=s, num_primitives=n)
+             for r, s, n in ((64, 11, 30), (128, 12, 80), (32, 13, 8), (64, 14, 10), (128, 15, 40))]
+    return [tdaglib.scene_svdag(sp, to_dag=True, ctx=gpu_ctx) for sp in specs]
+
+
+@pytest.mark.parametrize("cfgt", [(1, 1, 1, 4), (1, 1, 0, 4), (0, 1, 1, 3)])
+def test_batch_graph_equals_eager_batch_and_oracle(oracle, tdaglib, gpu_ctx, cfgt):
+    """The batched build captured in one CUDA graph (tdag_batch_graph_*): two launches in a row, each
+    result equal bit for bit to the eager batched build's and to the oracle's."""
+    devs = _scene_batch(tdaglib, gpu_ctx)
+    cfg = tdaglib.TransformDAGConfig(*[bool(v) for v in cfgt[:3]], cfgt[3])
+    eager, _ = tdaglib.construct_transform_dag_batched_device(devs, cfg, ctx=gpu_ctx)
+    want = [tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) for r in eager]
+    for r in eager:
+        r.free()
+    for dv, w in zip(devs, want):
+        ref, _, _ = oracle.construct_tdag(dv.to_host().to_svo_bytes(), *cfgt)
+        assert w == ref
+    graph = tdaglib.BatchGraph(devs, cfg, ctx=gpu_ctx)
+    for launch in range(2):
+        results, stats = graph.launch()
+        assert stats["kernel_launches"] > 0 and stats["total_ms"] > 0, f"launch {launch}"
+        for i, r in enumerate(results):
+            assert tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) == want[i], f"launch {launch}, grid {i}"
+            r.free()
+    graph.free()
+
+
+def test_batch_graph_rejects_a_changed_batch(tdaglib, gpu_ctx):
+    """A launch on a batch whose arrays changed since the graph was made returns TDAG_ERR_ARG without
+    running the graph; with the contents restored the graph runs again."""
+    import ctypes
+    import torch
+    from tdag import _abi
+
+    devs = _scene_batch(tdaglib, gpu_ctx)[:3]
+    cfg = tdaglib.TransformDAGConfig()
+    graph = tdaglib.BatchGraph(devs, cfg, ctx=gpu_ctx)
+    first, _ = graph.launch()
+    want = [tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) for r in first]
+    L = tdaglib.lib()
+    va, vb = devs[0].view(), devs[1].view()
+    leaves_a = devs[0].to_host().sub_grids
+    leaves_b = devs[1].to_host().sub_grids
+    k = next(i for i in range(min(len(leaves_a), len(leaves_b))) if leaves_a[i] != leaves_b[i])
+    a_word = ctypes.cast(va.leaves, ctypes.c_void_p).value + 8 * k
+    b_word = ctypes.cast(vb.leaves, ctypes.c_void_p).value + 8 * k
+    saved = torch.empty(1, dtype=torch.int64, device=torch.device("cuda", gpu_ctx.device))
+    _abi.check(L.tdag_device_copy(gpu_ctx.handle, saved.data_ptr(), a_word, 8))
+    _abi.check(L.tdag_device_copy(gpu_ctx.handle, a_word, b_word, 8))  # grid 0's leaf k now differs
+    with pytest.raises(_abi.TDagError) as e:
+        graph.launch()
+    assert e.value.code == _abi.TDAG_ERR_ARG
+    _abi.check(L.tdag_device_copy(gpu_ctx.handle, a_word, saved.data_ptr(), 8))
+    again, _ = graph.launch()
+    assert [tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) for r in again] == want
+    graph.free()
