@@ -64,7 +64,7 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sample-resolution", type=int, default=0, help="CPU sample sub-volume side (0: 256, or the grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-graph", action="store_true", help="batch96: skip the CUDA-graph replay of the batched build")
+    ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph replay of the build (tdag_batch_graph_*)")
     ap.add_argument("--cpu-baseline", default="auto", choices=["auto", "full", "sample"],
                     help="full: the oracle on the whole grid once (auto: up to 2048^3); sample: random sub-volumes only")
     ap.add_argument("--cpu-baseline-timeout", type=float, default=900.0, help="seconds allowed to the whole-grid oracle build")
@@ -203,7 +203,7 @@ def run_batch(args, world, rank, local, pg):
     cfg = tdag.TransformDAGConfig()
     tuning, tune_ms, table = ({}, None, [])
     if not args.no_autotune:
-        tuning, tune_ms, table = autotune.autotune_batched(devs, cfg, device=dev)
+        tuning, tune_ms, table = autotune.autotune_batched(devs, cfg, device=dev, repeats=2)
     tctx = tdag.Context(dev, tuning)
     for _ in range(max(args.warmup, 0)):
         res, _ = tdag.construct_transform_dag_batched_device(devs, cfg, ctx=tctx)
@@ -618,6 +618,39 @@ def run_ours(args, world, rank, local, pg):
     dev_ms = max_over_ranks(pg, dev_ms)
     value = replica_value(voxels, args.steps, world, dev_ms / 1e3)
 
+    # ---- the same build replayed from one CUDA graph (tdag_batch_graph_*, a batch of one grid), timed
+    # the same way around the whole call: the input check, the graph and the result copies
+    graph_info = None
+    if not args.no_graph:
+        t0 = time.perf_counter()
+        bg = tdag.BatchGraph([g], cfg, ctx=ctx)
+        create_ms = (time.perf_counter() - t0) * 1e3
+        first, _ = bg.launch()
+        ref = tdag.construct_transform_dag_device(g, cfg, ctx=ctx)
+        g_exact = first[0].to_host(ctx).to_bytes() == ref.to_host(ctx).to_bytes()
+        ref.free()
+        first[0].free()
+        gms, gdev = [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(lib_stream)
+            res, gst = bg.launch()
+            e1.record(lib_stream)
+            e1.synchronize()
+            gms.append(e0.elapsed_time(e1))
+            gdev.append(gst["total_ms"])
+            for r in res:
+                r.free()
+        bg.free()
+        gms_mean = max_over_ranks(pg, sum(gms)) / args.steps
+        graph_info = {"ms_per_step": gms_mean, "value": replica_value(voxels, args.steps, world, gms_mean * args.steps / 1e3),
+                      "graph_device_ms": sum(gdev) / len(gdev), "kernel_nodes": gst["kernel_launches"], "create_ms": create_ms,
+                      "bit_exact_vs_eager": bool(g_exact),
+                      "note": "tdag_batch_graph_launch per step: device check of the input against the graph's snapshot, one cudaGraphLaunch, result copies"}
+
     # ---- e2e through tdag_build with pinned host buffers
     host = g.to_host()
     keep = []
@@ -740,6 +773,8 @@ def run_ours(args, world, rank, local, pg):
                      "search_L4": lvl_times[4], "search_L3": lvl_times[3], "search_L2": lvl_times[2],
                      "probe_L4": probe_times[4], "probe_L3": probe_times[3], "probe_L2": probe_times[2]},
     }
+    if graph_info is not None:
+        out["graph"] = graph_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
         orc.build()

@@ -718,6 +718,34 @@ __device__ __noinline__ bool verifyCandidateWarp(const uint64_t* __restrict__ tg
     return __all_sync(0xffffffffu, ok);
 }
 
+// This lane's share of a verification by a group of V lanes (V < 32): rows sub, sub + V, ... of the
+// R * R rows. Short shares issue every row's loads before the first compare, like the warp version;
+// long ones stop at the first mismatch.
+template <int R, int V>
+__device__ __forceinline__ bool verifyRowsOfLane(const uint64_t* __restrict__ tgrid, const uint16_t* lines, int a0, int a1, uint32_t S, int T0, int T1, int T2,
+    uint32_t sub)
+{
+    constexpr int ROWS = R * R;
+    constexpr int STEPS = (ROWS + V - 1) / V;
+    const uint16_t* L = lines + a0 * R * R;
+    const int lo = otherLo(a0), hi = otherHi(a0);
+    bool ok = true;
+    if constexpr (STEPS <= 8) {
+#pragma unroll
+        for (int k = 0; k < STEPS; ++k) {
+            const int r = k * V + (int)sub;
+            ok &= r >= ROWS || verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, r % R, r / R);
+        }
+    } else {
+        for (int k = 0; k < STEPS && ok; ++k) {
+            const int r = k * V + (int)sub;
+            if (r < ROWS)
+                ok = verifyRow<R>(tgrid, L, lo, hi, a1, S, T0, T1, T2, r % R, r / R);
+        }
+    }
+    return ok;
+}
+
 template <int R, int L>
 __global__ void __launch_bounds__(kThreads, 2) searchKernel(SearchParams p)
 {
@@ -1384,12 +1412,17 @@ struct LookupParams {
     const uint32_t* segOff;
     uint32_t allowSym, allowPerm, allowTrans;
     unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified, [6] longest run
-    unsigned long long* cursor; // set: warps claim 32 records at a time from it (zeroed before the launch)
+    unsigned long long* cursor; // set: warps claim `tile` records at a time from it (zeroed before the launch)
+    uint32_t tile; // records per claim (a multiple of 32)
 };
 
-template <int R, int L>
+// V: lanes per candidate verification (32: the whole warp verifies one candidate at a time; 1, 4 or
+// 8: the warp's 32 / V groups verify as many candidates side by side). The parent keys and so the
+// result do not depend on V: a target keeps the smallest verified key whatever the order.
+template <int R, int L, int V>
 __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
 {
+    static_assert(V == 1 || V == 4 || V == 8 || V == 32, "lanes per verification");
     const uint32_t lane = threadIdx.x & 31;
     uint32_t cHit = 0, cCand = 0, cVer = 0, cOk = 0, cMaxRun = 0;
 
@@ -1461,11 +1494,13 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
     // would serialise the claims of the large batches, which take records by a fixed stride)
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    uint64_t claimEnd = 0;
     if (p.cursor) {
         unsigned long long c = 0;
         if (lane == 0)
-            c = atomicAdd(p.cursor, 32ull);
+            c = atomicAdd(p.cursor, (unsigned long long)p.tile);
         i0 = __shfl_sync(0xffffffffu, c, 0);
+        claimEnd = i0 + p.tile;
     }
     for (; i0 < p.count;) {
         const uint64_t i = i0 + lane;
@@ -1513,6 +1548,44 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
             uint32_t tgt = 0, geo = 0;
             uint64_t key = 0;
             const bool need = j < total && prepare(__ldg(&p.entries[hs + (j - hx)]), hm, tgt, key, geo);
+            if constexpr (V < 32) {
+                // The verifications of this step, 32 / V at a time: group g of V lanes takes the
+                // g-th pending candidate of each round.
+                constexpr uint32_t G = 32 / V;
+                const uint32_t grp = lane / V, sub = lane % V;
+                const uint32_t gmask = ((V == 32) ? 0xFFFFFFFFu : ((1u << V) - 1u)) << (grp * V);
+                for (unsigned pending = __ballot_sync(0xffffffffu, need); pending;) {
+                    unsigned mine = pending;
+                    for (uint32_t k = 0; k < grp && mine; ++k)
+                        mine &= mine - 1;
+                    const bool have = mine != 0;
+                    const int src = have ? __ffs(mine) - 1 : (int)lane;
+                    for (uint32_t k = 0; k < G && pending; ++k)
+                        pending &= pending - 1;
+                    const uint32_t vt = __shfl_sync(0xffffffffu, tgt, src);
+                    const uint64_t vk = __shfl_sync(0xffffffffu, key, src);
+                    const uint32_t vg = __shfl_sync(0xffffffffu, geo, src);
+                    const uint32_t vw = (uint32_t)__shfl_sync(0xffffffffu, hm, src);
+                    unsigned long long cur = 0;
+                    if (have && sub == 0)
+                        cur = *((volatile unsigned long long*)&p.parents[vt]);
+                    cur = __shfl_sync(0xffffffffu, cur, (int)(grp * V));
+                    const bool go = have && vk < cur;
+                    if (go && sub == 0)
+                        ++cVer;
+                    bool rowsOk = true;
+                    if (go) {
+                        const int T0 = (int)((vg >> 8) & 63u) - 32, T1 = (int)((vg >> 14) & 63u) - 32, T2 = (int)((vg >> 20) & 63u) - 32;
+                        rowsOk = verifyRowsOfLane<R, V>(p.grids + (size_t)vt * (R * R * R / 64), p.srcLines + (size_t)vw * 3 * R * R, (int)(vg & 3u),
+                            (int)((vg >> 2) & 3u), (vg >> 4) & 7u, T0, T1, T2, sub);
+                    }
+                    const uint32_t okMask = __ballot_sync(0xffffffffu, rowsOk);
+                    if (go && sub == 0 && (okMask & gmask) == gmask) {
+                        ++cOk;
+                        atomicMin(&p.parents[vt], (unsigned long long)vk);
+                    }
+                }
+            } else {
             // The verifications of this step, one candidate at a time by the whole warp (a lane alone
             // would run all R * R rows while the rest of the warp waits).
             for (unsigned pending = __ballot_sync(0xffffffffu, need); pending; pending &= pending - 1) {
@@ -1538,12 +1611,17 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
                     atomicMin(&p.parents[vt], (unsigned long long)vk);
                 }
             }
+            }
         }
         if (p.cursor) {
-            unsigned long long c = 0;
-            if (lane == 0)
-                c = atomicAdd(p.cursor, 32ull);
-            i0 = __shfl_sync(0xffffffffu, c, 0);
+            i0 += 32;
+            if (i0 >= claimEnd) {
+                unsigned long long c = 0;
+                if (lane == 0)
+                    c = atomicAdd(p.cursor, (unsigned long long)p.tile);
+                i0 = __shfl_sync(0xffffffffu, c, 0);
+                claimEnd = i0 + p.tile;
+            }
         } else {
             i0 += stride;
         }
@@ -1785,7 +1863,14 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
     const uint64_t freeBytes = deviceFreeBytes();
     const uint64_t maxRecords = std::max<uint64_t>(1u << 20, freeBytes / 4 / sizeof(ulonglong2));
     int lookupPerSM = 0;
-    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookupKernel<R, L>, kThreads, 0));
+    // lanes per candidate verification (tuning.verify_lanes: 1, 4, 8 or 32 (default)) and records per
+    // dynamic claim (tuning.lookup_tile: 32 (default) .. 1024)
+    const uint32_t vLanes = ctx.tuning.verify_lanes ? ctx.tuning.verify_lanes : 32u;
+    TDAG_CHECK(vLanes == 1 || vLanes == 4 || vLanes == 8 || vLanes == 32, TDAG_ERR_ARG, "verify_lanes must be 1, 4, 8 or 32");
+    auto lookup = vLanes == 1 ? lookupKernel<R, L, 1> : (vLanes == 4 ? lookupKernel<R, L, 4> : (vLanes == 8 ? lookupKernel<R, L, 8> : lookupKernel<R, L, 32>));
+    const uint32_t lookupTile = ctx.tuning.lookup_tile ? ctx.tuning.lookup_tile : 32u;
+    TDAG_CHECK(lookupTile >= 32 && lookupTile <= 1024 && lookupTile % 32 == 0, TDAG_ERR_ARG, "lookup_tile must be a multiple of 32 in 32..1024");
+    TDAG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lookupPerSM, lookup, kThreads, 0));
     const uint32_t lookupBlocks = (uint32_t)ctx.numSMs * (uint32_t)std::max(lookupPerSM, 1);
 
     // Source batches. Single grid: ranges of sorted positions growing by the factor below (every batch
@@ -2019,6 +2104,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 lp.begin = pos;
                 lp.srcLines = srcLines.get();
                 lp.cursor = nullptr;
+                lp.tile = lookupTile;
                 if (produced < (1ull << 20)) { // few records: balance them dynamically
                     lp.cursor = lookupCursor.get();
                     TDAG_CUDA(cudaMemsetAsync(lp.cursor, 0, 8, s));
@@ -2027,7 +2113,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 const unsigned lblocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)lookupBlocks, (warpsNeeded + kThreads / 32 - 1) / (kThreads / 32)));
                 if (trace)
                     TDAG_CUDA(cudaEventRecord(traceEv[0], s));
-                lookupKernel<R, L><<<lblocks, kThreads, 0, s>>>(lp);
+                lookup<<<lblocks, kThreads, 0, s>>>(lp);
                 TDAG_LAUNCHED();
                 if (trace) {
                     TDAG_CUDA(cudaEventRecord(traceEv[1], s));

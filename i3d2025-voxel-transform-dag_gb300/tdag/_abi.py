@@ -95,7 +95,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("filter_bits_per_key", ctypes.c_uint32), ("table_load_percent", ctypes.c_uint32),
                 ("search_ctas_per_sm", ctypes.c_uint32), ("class_table_load_percent", ctypes.c_uint32),
                 ("table_regrow_limit", ctypes.c_uint32), ("slab_pool_slabs", ctypes.c_uint32), ("device_memory_limit", ctypes.c_uint64),
-                ("probe_bulk_copy", ctypes.c_uint32), ("reserved2", ctypes.c_uint32)]
+                ("probe_bulk_copy", ctypes.c_uint32), ("verify_lanes", ctypes.c_uint32), ("lookup_tile", ctypes.c_uint32),
+                ("reserved3", ctypes.c_uint32)]
 
 
 class EncodingConfig(ctypes.Structure):

@@ -115,7 +115,13 @@ typedef struct tdag_tuning {
                                    * (0 = no limit); an allocation past it fails with TDAG_ERR_OOM */
     uint32_t probe_bulk_copy; /* level-4 probe: 1 stages the source grids by a bulk copy (TMA) one
                                * source ahead; 0 (default) or 2 load them cooperatively */
-    uint32_t reserved2;
+    uint32_t verify_lanes; /* threads per exact subgrid verification in the lookup: 1, 4, 8 or 32
+                            * (0 = 32, the whole warp); smaller groups verify 32 / lanes candidates
+                            * side by side */
+    uint32_t lookup_tile; /* probe records a lookup warp claims at a time when the records are
+                           * balanced dynamically (fewer than 2^20): a multiple of 32 in 32..1024
+                           * (0 = 32) */
+    uint32_t reserved3;
 } tdag_tuning;
 
 /* Library/version information. */

@@ -109,3 +109,24 @@ def test_batch_graph_rejects_a_changed_batch(tdaglib, gpu_ctx):
     again, _ = graph.launch()
     assert [tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) for r in again] == want
     graph.free()
+
+
+def test_autotune_on_a_small_batch(oracle, tdaglib, gpu_ctx):
+    """The autotuner times every configuration it tries on the device (each one's bytes checked
+    against the first's) and its choice builds the oracle's bytes."""
+    from tdag import autotune
+
+    devs = _scene_batch(tdaglib, gpu_ctx)[:3]
+    cfg = tdaglib.TransformDAGConfig()
+    space = {"table_load_percent": (50, 85), "verify_lanes": (1, 4, 8, 32), "lookup_tile": (32, 256, 1024)}
+    best, ms, table = autotune.autotune_batched(devs, cfg, device=gpu_ctx.device, space=space)
+    assert set(best) == set(space) and ms > 0 and len(table) >= 6
+    ctx = tdaglib.Context(gpu_ctx.device, best)
+    try:
+        results, _ = tdaglib.construct_transform_dag_batched_device(devs, cfg, ctx=ctx)
+        for dv, r in zip(devs, results):
+            ref, _, _ = oracle.construct_tdag(dv.to_host().to_svo_bytes())
+            assert tdaglib.write_tdag(r.to_host(ctx), cfg) == ref
+            r.free()
+    finally:
+        ctx.close()

@@ -78,3 +78,51 @@ def test_find_duplicates_level(oracle, tdaglib, gpu_ctx, level):
     u_got, m_got = tdaglib.find_duplicates_among_flattened_items(level, grids, ctx=gpu_ctx)
     assert np.array_equal(u_ref, u_got)
     assert np.array_equal(m_ref, m_got)
+
+
+def _level_grids(level, n=300, seed=None):
+    rng = np.random.default_rng(level if seed is None else seed)
+    R = 1 << level
+    W = R ** 3 // 64
+    dense = (rng.random((n, R, R, R)) < 0.15)
+    for i in range(60, n):
+        src = dense[rng.integers(0, 60)]
+        cp = np.roll(src, tuple(rng.integers(-2, 3, size=3)), axis=(0, 1, 2))
+        if rng.random() < 0.5:
+            cp = cp[::-1]
+        if rng.random() < 0.5:
+            cp = np.transpose(cp, (1, 0, 2))
+        dense[i] = cp
+    bits = np.packbits(dense.reshape(n, -1).astype(np.uint8), axis=1, bitorder="little")
+    return bits.view(np.uint64).reshape(n, W)
+
+
+@pytest.mark.parametrize("lanes,tile", [(1, 32), (4, 64), (8, 256), (32, 1024), (4, 1024)])
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_verify_lanes_and_lookup_tile(oracle, tdaglib, level, lanes, tile):
+    """Every verification width (threads per subgrid) and lookup claim size gives the oracle's result."""
+    grids = _level_grids(level, seed=100 + level)
+    m_ref, u_ref, _ = oracle.find_duplicates(level, grids)
+    ctx = tdaglib.Context(0, {"verify_lanes": lanes, "lookup_tile": tile})
+    try:
+        u_got, m_got = tdaglib.find_duplicates_among_flattened_items(level, grids, ctx=ctx)
+        assert np.array_equal(u_ref, u_got) and np.array_equal(m_ref, m_got)
+        # and a whole build through the same context
+        dense = blocky_grid(64, 9)
+        svo = dag_svo_bytes(oracle, dense)
+        ref, _, _ = oracle.construct_tdag(svo)
+        assert _gpu_tdag_bytes(tdaglib, ctx, svo, tdaglib.TransformDAGConfig()) == ref
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("knob,value", [("verify_lanes", 2), ("verify_lanes", 64), ("lookup_tile", 48), ("lookup_tile", 2048)])
+def test_bad_lookup_knobs_are_rejected(tdaglib, knob, value):
+    grids = _level_grids(3, n=100)
+    ctx = tdaglib.Context(0, {knob: value})
+    try:
+        with pytest.raises(tdaglib.TDagError) as e:
+            tdaglib.find_duplicates_among_flattened_items(3, grids, ctx=ctx)
+        assert e.value.code == 1  # TDAG_ERR_ARG
+    finally:
+        ctx.close()
