@@ -130,3 +130,23 @@ def test_autotune_on_a_small_batch(oracle, tdaglib, gpu_ctx):
             r.free()
     finally:
         ctx.close()
+
+
+def test_batch_graph_replays_class_table_regrows(oracle, tdaglib):
+    """Class tables started far too small (400 % load) fill up, report TDAG_ERR_TABLE_FULL and are
+    regrown; whether a table is full depends only on its number of distinct classes, so the graph
+    replays the same failed attempts and retries as its plan and still builds the oracle's bytes."""
+    ctx = tdaglib.Context(tuning={"class_table_load_percent": 400})
+    try:
+        devs = _scene_batch(tdaglib, ctx)[:3]
+        cfg = tdaglib.TransformDAGConfig()
+        graph = tdaglib.BatchGraph(devs, cfg, ctx=ctx)
+        for _ in range(2):
+            results, _ = graph.launch()
+            for dv, r in zip(devs, results):
+                ref, _, _ = oracle.construct_tdag(dv.to_host().to_svo_bytes())
+                assert tdaglib.write_tdag(r.to_host(ctx), cfg) == ref
+                r.free()
+        graph.free()
+    finally:
+        ctx.close()
