@@ -154,6 +154,14 @@ def run_proposal(args, world, rank, local, pg):
     parents = P.exhaustive_parent_sets(g, cfg, ctx=ctx)
     best_s, (best, best_src) = timed(lambda: P.construct_transform_dag_with_sources(g, parents, cfg, ctx=ctx))
     best_nodes = nodes_of(best)
+    # no-network selectors: a fraction of the items searches (the first in the source order, or random)
+    fractions = []
+    for rule in ("popcount", "random"):
+        for rho in (0.2, 0.5, 0.7):
+            s_f, (r, src) = timed(lambda: P.construct_transform_dag_by_fraction(g, rule, rho, cfg, ctx=ctx))
+            n_f = nodes_of(r)
+            fractions.append({"rule": rule, "fraction": rho, "ms": s_f * 1e3, "speed_vs_exhaustive": ex_s / s_f,
+                              "extra_nodes_percent": 100.0 * (n_f - ex_nodes) / ex_nodes})
     modes = {}
     for k in (8, 32):
         s_k, (r, src) = timed(lambda: P.construct_transform_dag_proposed(g, enc, k, cfg, ctx=ctx))
@@ -172,6 +180,7 @@ def run_proposal(args, world, rank, local, pg):
                             "sources_per_level": {str(l): {"items": it, "sources": sc} for l, (it, sc) in best_src.items()},
                             "note": "only the exhaustive result's parents search, no network: the ceiling of any proposal method"},
            "proposal": modes,
+           "fraction_baselines": fractions,
            "training": {"grids": args.train_grids, "resolution": 1024, "steps": args.train_steps, "label_s": t_labels, "train_s": t_train,
                         "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}}
     if rank == 0:

@@ -1079,7 +1079,9 @@ void copyToArena(const DeviceResult& dr, const tdag_svdag_view* in, uint32_t cou
 } // namespace tdag
 
 struct tdag_batch_graph {
-    tdag_ctx* ctx = nullptr;
+    tdag_ctx* ctx = nullptr; // launches run on its stream; the context must outlive them
+    int device = 0;
+    std::shared_ptr<StreamState> stream; // keeps the stream alive for the destructor
     tdag_config cfg {};
     std::vector<tdag_svdag_view> views;
     std::vector<InputSpan> spans;
@@ -1097,9 +1099,9 @@ struct tdag_batch_graph {
 
     ~tdag_batch_graph()
     {
-        if (ctx) {
-            cudaSetDevice(ctx->c.device);
-            cudaStreamSynchronize(ctx->c.stream);
+        if (stream) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(stream->stream);
         }
         if (exec)
             cudaGraphExecDestroy(exec);
@@ -1108,8 +1110,8 @@ struct tdag_batch_graph {
         for (void* p : { (void*)snap, (void*)spansDev, (void*)diff, (void*)uploadsDev, (void*)mismatch, (void*)arena })
             if (p)
                 cudaFree(p);
-        if (ctx)
-            cudaDeviceGraphMemTrim(ctx->c.device);
+        if (stream)
+            cudaDeviceGraphMemTrim(device);
     }
 };
 
@@ -1134,6 +1136,8 @@ int tdag_batch_graph_create(tdag_ctx* ctx, const tdag_svdag_view* in, uint32_t c
         for (uint32_t g = 0; g < count; ++g)
             requireDeviceView(c, in[g]);
         G->ctx = ctx;
+        G->device = c.device;
+        G->stream = c.streamState;
         G->cfg = *cfg;
         G->views.assign(in, in + count);
 

@@ -487,6 +487,55 @@ class FixedSourcesHook(ProposalHook):
             return 1
 
 
+class FractionHook(ProposalHook):
+    """No-network selectors: a fraction `rho` of every level's items searches, either the first ones
+    in the source order ("popcount": the items with the most voxels) or a seeded random draw
+    ("random"). They bound what any selector gains from the number of sources alone."""
+
+    def __init__(self, ctx, rule: str, rho: float, device: int = 0, seed: int = 0):
+        super().__init__(ctx, None, 0, device)
+        if rule not in ("popcount", "random"):
+            raise ValueError(f"unknown selection rule {rule!r}")
+        self.rule, self.rho, self.seed = rule, rho, seed
+
+    def _call(self, user, level, d_grids, n, d_sources, num_sources):
+        try:
+            W = (1 << (3 * level)) // 64
+            words = torch.empty((n, W), dtype=torch.int64, device=f"cuda:{self.device}")
+            _abi.check(lib().tdag_device_copy(self.ctx.handle, words.data_ptr(), d_grids, n * W * 8))
+            m = int(self.rho * n)
+            if self.rule == "popcount":
+                src = (popcount_positions(words) < m).nonzero().squeeze(1).to(torch.int32)
+            else:
+                g = torch.Generator(device="cpu").manual_seed(self.seed + level)
+                src = torch.randperm(n, generator=g)[:m].to(words.device).to(torch.int32)
+            torch.cuda.synchronize(self.device)
+            if src.numel():
+                _abi.check(lib().tdag_device_copy(self.ctx.handle, d_sources, src.data_ptr(), src.numel() * 4))
+            num_sources[0] = src.numel()
+            self.sources[level] = (n, src.numel())
+            return 0
+        except BaseException as e:
+            self.error = e
+            return 1
+
+
+def construct_transform_dag_by_fraction(in_dag, rule: str, rho: float, config=None, ctx=None):
+    """constructTransformDAG where a fraction of the items searches at every translation level, chosen
+    without a network (FractionHook). Returns (DeviceResult, per-level (items, sources))."""
+    from . import DeviceResult, TransformDAGConfig, _config_struct, default_context
+    ctx = ctx or default_context()
+    config = config or TransformDAGConfig()
+    hook = FractionHook(ctx, rule, rho, device=torch.cuda.current_device())
+    v = in_dag.view()
+    rp = ctypes.POINTER(_abi.Result)()
+    rc = lib().tdag_build_device_proposed(ctx.handle, ctypes.byref(v), ctypes.byref(_config_struct(config)), hook.fn, None, ctypes.byref(rp))
+    if hook.error is not None:
+        raise hook.error
+    _abi.check(rc)
+    return DeviceResult(rp), hook.sources
+
+
 def exhaustive_parent_sets(in_dag, config=None, ctx=None) -> Dict[int, torch.Tensor]:
     """Per translation level, the items that are some other item's parent in the exhaustive build."""
     from . import TransformDAGConfig, default_context

@@ -172,7 +172,8 @@ int tdag_build_batched_device(tdag_ctx* ctx, const tdag_svdag_view* in_device, u
  * difference returns TDAG_ERR_CUDA. out[i] (device-resident, released with tdag_result_free) equals
  * tdag_build_batched_device's out[i] bit for bit. stats (may be NULL) receives total_ms (the
  * graph's device time) and kernel_launches (the graph's kernel nodes). Calls are synchronous on the
- * context's stream. Learned-proposal hooks cannot be captured. */
+ * context's stream; launches need the context alive, tdag_batch_graph_free does not. Learned-proposal
+ * hooks cannot be captured. */
 typedef struct tdag_batch_graph tdag_batch_graph;
 int tdag_batch_graph_create(tdag_ctx* ctx, const tdag_svdag_view* in_device, uint32_t count, const tdag_config* config,
     tdag_batch_graph** out);

@@ -85,3 +85,21 @@ def test_parents_as_the_only_sources_give_the_exhaustive_tdag(tdaglib, gpu_ctx):
     want = tdaglib.write_tdag(tdaglib.construct_transform_dag_device(g, cfg, ctx=gpu_ctx).to_host(ctx=gpu_ctx), cfg)
     assert got == want
     assert all(s < n for n, s in sources.values())
+
+
+def test_fraction_selectors(tdaglib, gpu_ctx):
+    """The no-network selectors: the whole fraction is the exhaustive build byte for byte, a smaller
+    one searches with that share of the items and still yields a TDAG no smaller than the exhaustive."""
+    from tdag import proposal as P
+    cfg = tdaglib.TransformDAGConfig()
+    g = _scene(tdaglib, gpu_ctx, 256, 5)
+    ex = tdaglib.construct_transform_dag_device(g, cfg, ctx=gpu_ctx).to_host(gpu_ctx)
+    want = tdaglib.write_tdag(ex, cfg)
+    nodes = lambda s: sum(len(a) for a in s.nodes_per_level) + len(s.sub_grids)
+    for rule in ("popcount", "random"):
+        r, src = P.construct_transform_dag_by_fraction(g, rule, 1.0, cfg, ctx=gpu_ctx)
+        assert tdaglib.write_tdag(r.to_host(gpu_ctx), cfg) == want
+        assert all(items == s for items, s in src.values())
+        r, src = P.construct_transform_dag_by_fraction(g, rule, 0.3, cfg, ctx=gpu_ctx)
+        assert all(s == int(0.3 * items) for items, s in src.values())
+        assert nodes(r.to_host(gpu_ctx)) >= nodes(ex)
