@@ -776,6 +776,12 @@ def run_ours(args, world, rank, local, pg):
         "clocks": clk,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats_list)),
         "subgrids_matched_per_s": sum(last["translation"][L]["items"] for L in (2, 3, 4)) / (dev_ms / args.steps / 1e3),
+        # the reference's own search throughput figure (find_translation.cpp:879-885): sources x R^3 voxels
+        # x 8 fold directions x 6 axis permutations x 8-byte hashes per second of search, per level
+        "search_permuted_voxel_mib_s": {str(L): (last["translation"][L]["items"] * (1 << (3 * L)) * 8 * 6 * 8 / (lvl_times[L] / 1e3) / 2 ** 20
+                                                 if lvl_times[L] > 0 else None) for L in (2, 3, 4)},
+        "dense_gvoxels_per_s": {"value": args.resolution ** 3 / (dev_ms / args.steps / 1e3) / 1e9,
+                                "note": "resolution^3 cells (empty included) per second of build"},
         "pipeline": pipeline,
         "tdag16": tdag16,
         "stage_ms": {"hierarchical": last["hierarchical_ms"], "translation": last["translation_ms"],

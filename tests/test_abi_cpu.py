@@ -93,3 +93,19 @@ def test_nn_entry_points_reject_bad_arguments_without_a_device(tdaglib):
     assert L.tdag_nn_adamw(None, None, None, None, None, 0, 1e-3, 0.9, 0.999, 1e-8, 0.0, 1, None) == _abi.TDAG_ERR_ARG
     assert L.tdag_nn_info_nce(None, None, 0, None, None) == _abi.TDAG_ERR_ARG
     assert L.tdag_nn_sync(None) == _abi.TDAG_ERR_ARG
+
+
+def test_batch_graph_entry_points_reject_bad_arguments_without_a_device(tdaglib):
+    """tdag_batch_graph_*: null arguments and an empty batch are refused before any CUDA call, and
+    freeing a null graph is a no-op."""
+    import ctypes
+    from tdag import _abi
+    L = tdaglib.lib()
+    out = ctypes.c_void_p()
+    cfg = tdaglib._config_struct(tdaglib.TransformDAGConfig())
+    views = (_abi.SvdagView * 1)()
+    assert L.tdag_batch_graph_create(None, views, 1, ctypes.byref(cfg), ctypes.byref(out)) == _abi.TDAG_ERR_ARG
+    assert L.tdag_batch_graph_create(None, views, 0, ctypes.byref(cfg), ctypes.byref(out)) == _abi.TDAG_ERR_ARG
+    res = (ctypes.POINTER(_abi.Result) * 1)()
+    assert L.tdag_batch_graph_launch(None, res, None) == _abi.TDAG_ERR_ARG
+    assert L.tdag_batch_graph_free(None) == _abi.TDAG_OK
