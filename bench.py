@@ -71,8 +71,12 @@ def parse_args():
     ap.add_argument("--workload", default="single", choices=["single", "batch96", "proposal"],
                     help="single: one 2048^3 grid (headline); batch96: 96 grids of 128^3..1024^3 in one batched build; "
                          "proposal: learned source proposals (approximate) against the exhaustive build of the same grid")
-    ap.add_argument("--train-grids", type=int, default=8, help="proposal: seeded 1024^3 training grids")
-    ap.add_argument("--train-steps", type=int, default=1500, help="proposal: training steps")
+    ap.add_argument("--encoder", default="hierarchical", choices=["hierarchical", "block"],
+                    help="proposal: children in canonical octant order with an MLP per level (the configured encoder), or the "
+                         "mean-pooled block MLP")
+    ap.add_argument("--train-grids", type=int, default=20, help="proposal: seeded 1024^3 training grids")
+    ap.add_argument("--train-steps", type=int, default=10000,
+                    help="proposal: training steps of 2048 positive pairs each (10000: 2.05e7 positive pairs)")
     ap.add_argument("--grids", type=int, default=96)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--probe-bulk-copy", type=int, default=0, choices=[0, 1, 2],
@@ -117,7 +121,7 @@ def run_proposal(args, world, rank, local, pg):
             sets.append((words, level, P.exhaustive_parents(ctx, words, level, cfg)[0]))
         g.free()
     t_labels = time.perf_counter() - t0
-    enc = P.ProposalEncoder(seed=0, ctx=ctx)
+    enc = (P.HierarchicalEncoder if args.encoder == "hierarchical" else P.ProposalEncoder)(seed=0, ctx=ctx)
     t0 = time.perf_counter()
     losses = P.train(enc, sets, steps=args.train_steps, batch=2048)
     torch.cuda.synchronize()
@@ -154,6 +158,14 @@ def run_proposal(args, world, rank, local, pg):
     parents = P.exhaustive_parent_sets(g, cfg, ctx=ctx)
     best_s, (best, best_src) = timed(lambda: P.construct_transform_dag_with_sources(g, parents, cfg, ctx=ctx))
     best_nodes = nodes_of(best)
+    # recall@8 of the exhaustive parents: learned lists against the no-network lists
+    recall = {}
+    for level, words in P.level_items(g, cfg, ctx=ctx).items():
+        parent, _ = P.exhaustive_parents(ctx, words, level, cfg)
+        pos = P.popcount_positions(words)
+        recall[str(level)] = {"learned": P.recall_at_k(P.propose_lists(P.embed(enc, words, level), pos, 8, ctx), parent),
+                              "popcount_neighbours": P.recall_at_k(P.popcount_neighbour_lists(pos, 8), parent),
+                              "random": P.recall_at_k(P.random_lists(pos, 8), parent)}
     # no-network selectors: a fraction of the items searches (the first in the source order, or random)
     fractions = []
     for rule in ("popcount", "random"):
@@ -181,7 +193,9 @@ def run_proposal(args, world, rank, local, pg):
                             "note": "only the exhaustive result's parents search, no network: the ceiling of any proposal method"},
            "proposal": modes,
            "fraction_baselines": fractions,
-           "training": {"grids": args.train_grids, "resolution": 1024, "steps": args.train_steps, "label_s": t_labels, "train_s": t_train,
+           "recall_at_8": recall,
+           "training": {"encoder": args.encoder, "grids": args.train_grids, "resolution": 1024, "steps": args.train_steps, "label_s": t_labels, "train_s": t_train,
+                        "positive_pairs_max": args.train_steps * 2048, "in_batch_negative_pairs_max": args.train_steps * 2048 * 2047,
                         "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None}}
     if rank == 0:
         print(json.dumps(out), flush=True)

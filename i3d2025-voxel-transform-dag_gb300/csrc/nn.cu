@@ -634,6 +634,74 @@ __global__ void adamwKernel(float* __restrict__ w, const float* __restrict__ g, 
         wBf16[i] = toBf16(x);
 }
 
+// Canonical octant order of an item's eight children: with b the child occupancy byte, the first
+// transform t (ID sym | perm << 3) whose image byteMap[t][b] is the smallest; child o goes to slot
+// pos[t][o]. One warp per item, lane = embedding dimension.
+__device__ __forceinline__ uint32_t canonTransform(const TransformTables* __restrict__ tt, uint32_t b)
+{
+    uint32_t best = 0, bestByte = 256;
+    for (uint32_t t = 0; t < 48; ++t) {
+        const uint32_t v = tt->byteMap[t][b];
+        if (v < bestByte) {
+            bestByte = v;
+            best = t;
+        }
+    }
+    return best;
+}
+
+// A child row at or past childRows is recorded as TDAG_ERR_ARG and read as an empty child.
+__global__ void canonGatherKernel(const float* __restrict__ child, uint32_t childRows, const int32_t* __restrict__ childRow, uint32_t n,
+    const TransformTables* __restrict__ tt, uint16_t* __restrict__ x, uint8_t* __restrict__ slotOf, uint32_t* status)
+{
+    const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, d = threadIdx.x & 31;
+    if (item >= n)
+        return;
+    int32_t rows[8];
+    uint32_t b = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+        rows[o] = childRow[(size_t)item * 8 + o];
+        if (rows[o] >= 0 && (uint32_t)rows[o] >= childRows) {
+            if (d == 0)
+                setDeviceError(status, TDAG_ERR_ARG, 700);
+            rows[o] = -1;
+        }
+        b |= (rows[o] >= 0 ? 1u : 0u) << o;
+    }
+    const uint32_t t = canonTransform(tt, b);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+        const uint32_t slot = tt->pos[t][o];
+        const float v = rows[o] >= 0 ? child[(size_t)rows[o] * 32 + d] : 0.0f;
+        x[(size_t)item * 256 + 32 * slot + d] = toBf16(v);
+        if (d == 0)
+            slotOf[(size_t)item * 8 + o] = (uint8_t)slot;
+    }
+}
+
+__global__ void canonScatterKernel(const void* __restrict__ dx, int dxBf16, const int32_t* __restrict__ childRow, const uint8_t* __restrict__ slotOf,
+    uint32_t n, float* __restrict__ dchild, uint32_t childRows, uint32_t* status)
+{
+    const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, d = threadIdx.x & 31;
+    if (item >= n)
+        return;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+        const int32_t row = childRow[(size_t)item * 8 + o];
+        if (row < 0)
+            continue;
+        if ((uint32_t)row >= childRows) {
+            if (d == 0)
+                setDeviceError(status, TDAG_ERR_ARG, 701);
+            continue;
+        }
+        const size_t at = (size_t)item * 256 + 32 * slotOf[(size_t)item * 8 + o] + d;
+        const float g = dxBf16 ? __bfloat162float(__ushort_as_bfloat16(static_cast<const uint16_t*>(dx)[at])) : static_cast<const float*>(dx)[at];
+        atomicAdd(&dchild[(size_t)row * 32 + d], g);
+    }
+}
+
 __global__ void toBf16Kernel(const float* __restrict__ x, uint64_t n, uint16_t* __restrict__ out)
 {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -886,6 +954,37 @@ int tdag_nn_to_bf16(tdag_ctx* ctx, const float* x, uint64_t n, uint16_t* out)
         TDAG_CUDA(cudaSetDevice(cx.device));
         if (n) {
             toBf16Kernel<<<gridOf(n, 256), 256, 0, cx.stream>>>(x, n, out);
+            TDAG_LAUNCHED();
+        }
+    });
+}
+
+int tdag_nn_canon_gather(tdag_ctx* ctx, const float* child, uint32_t child_rows, const int32_t* child_row, uint32_t n, uint16_t* x, uint8_t* slot_of)
+{
+    using namespace tdag;
+    if (!ctx || (n && (!child_row || !x || !slot_of || (child_rows && !child))))
+        return failWith(TDAG_ERR_ARG, "tdag_nn_canon_gather: null pointer");
+    return guardedCall([&] {
+        Context& cx = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(cx.device));
+        if (n) {
+            canonGatherKernel<<<gridOf((uint64_t)n * 32, 256), 256, 0, cx.stream>>>(child, child_rows, child_row, n, cx.tables, x, slot_of, cx.status);
+            TDAG_LAUNCHED();
+        }
+    });
+}
+
+int tdag_nn_canon_scatter(tdag_ctx* ctx, const void* dx, int dx_bf16, const int32_t* child_row, const uint8_t* slot_of, uint32_t n, float* dchild,
+    uint32_t child_rows)
+{
+    using namespace tdag;
+    if (!ctx || (n && (!dx || !child_row || !slot_of || (child_rows && !dchild))))
+        return failWith(TDAG_ERR_ARG, "tdag_nn_canon_scatter: null pointer");
+    return guardedCall([&] {
+        Context& cx = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(cx.device));
+        if (n) {
+            canonScatterKernel<<<gridOf((uint64_t)n * 32, 256), 256, 0, cx.stream>>>(dx, dx_bf16, child_row, slot_of, n, dchild, child_rows, cx.status);
             TDAG_LAUNCHED();
         }
     });

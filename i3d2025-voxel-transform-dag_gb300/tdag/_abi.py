@@ -137,6 +137,7 @@ EXPORTED = (
     "tdag16_upload", "tdag16_device_free", "tdag16_get", "tdag16_verify", "tdag16_raycast",
     "tdag_nn_gemm", "tdag_nn_block_masks", "tdag_nn_pool_forward", "tdag_nn_pool_backward",  # include/tdag_nn.h
     "tdag_nn_info_nce", "tdag_nn_column_sums", "tdag_nn_adamw", "tdag_nn_topk", "tdag_nn_sync", "tdag_nn_to_bf16",
+    "tdag_nn_canon_gather", "tdag_nn_canon_scatter",
 )
 
 # include/tdag_nn.h operand modes
@@ -220,6 +221,8 @@ def lib(path: str = None):
         L.tdag_nn_topk.argtypes = [vp, vp, u32, u32, vp, vp]
         L.tdag_nn_sync.argtypes = [vp]
         L.tdag_nn_to_bf16.argtypes = [vp, vp, ctypes.c_uint64, vp]
+        L.tdag_nn_canon_gather.argtypes = [vp, vp, u32, vp, u32, vp, vp]
+        L.tdag_nn_canon_scatter.argtypes = [vp, vp, ctypes.c_int, vp, vp, u32, vp, u32]
         for fn in (L.tdag_build_batched, L.tdag_build_batched_device):
             fn.argtypes = [vp, ctypes.POINTER(SvdagView), ctypes.c_uint32, ctypes.POINTER(Config),
                            ctypes.POINTER(ctypes.POINTER(Result)), ctypes.POINTER(Stats)]

@@ -207,6 +207,219 @@ class ProposalEncoder:
         _abi.check(lib().tdag_nn_sync(self.ctx.handle))
 
 
+UP_LAYERS = ((HIDDEN, 8 * EMBED_DIM), (HIDDEN, HIDDEN), (EMBED_DIM, HIDDEN))  # the upper levels' MLPs
+GROUPS = (("leaf", LAYERS), ("up3", UP_LAYERS), ("up4", UP_LAYERS))
+
+
+def _octant_blocks(device) -> torch.Tensor:
+    """(8, 8): the 4^3 block (bx + 4 by + 16 bz) of sub-octant o of octant q of a 16^3 item."""
+    blk = torch.empty((8, 8), dtype=torch.int64)
+    for q in range(8):
+        for o in range(8):
+            bx, by, bz = 2 * (q & 1) + (o & 1), 2 * ((q >> 1) & 1) + ((o >> 1) & 1), 2 * ((q >> 2) & 1) + ((o >> 2) & 1)
+            blk[q, o] = bx + 4 * by + 16 * bz
+    return blk.to(device)
+
+
+class HierarchicalEncoder:
+    """The configured encoder: a 4^3 item (level 2) is embedded by the leaf MLP 64 -> 256 -> 256 -> 32
+    over its occupancy mask; an 8^3 or 16^3 item by an MLP 256 -> 256 -> 256 -> 32 of its level
+    ('up3', 'up4') over its eight children's vectors in a canonical octant order
+    (tdag_nn_canon_gather): the children of an 8^3 item are its 4^3 blocks (leaf MLP outputs), those of
+    a 16^3 item its 8^3 octants (outputs of the 8^3 MLP). The embedding is L2-normalised. Same kernels,
+    training loop and interface as ProposalEncoder; gradients of all three MLPs flow through the
+    canonical gathers (tdag_nn_canon_scatter)."""
+
+    def __init__(self, device=None, seed: int = 0, ctx=None):
+        self.ctx = _ctx(ctx)
+        self.device = torch.device("cuda", self.ctx.device) if device is None else torch.device(device)
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        params = {}
+        for name, layers in GROUPS:
+            ps = []
+            for o, i in layers:
+                bound = 1.0 / math.sqrt(i)
+                ps.append((torch.rand((o, i), generator=g, dtype=torch.float64) * 2 - 1) * bound)
+                ps.append((torch.rand((o,), generator=g, dtype=torch.float64) * 2 - 1) * bound)
+            params[name] = ps
+        self.load(params)
+        self._blk = _octant_blocks(self.device)
+
+    def load(self, params: Dict[str, Sequence]) -> "HierarchicalEncoder":
+        """Set every group's six parameters [w1, b1, w2, b2, w3, b3] and reset AdamW."""
+        self.params = {g: [torch.as_tensor(p).to(device=self.device, dtype=torch.float32).contiguous() for p in ps] for g, ps in params.items()}
+        self.w16 = {g: [ps[2 * l].to(torch.bfloat16) for l in range(3)] for g, ps in self.params.items()}
+        self.m1 = {g: [torch.zeros_like(p) for p in ps] for g, ps in self.params.items()}
+        self.m2 = {g: [torch.zeros_like(p) for p in ps] for g, ps in self.params.items()}
+        self.step_count = 0
+        return self
+
+    def numpy_params(self):
+        return {g: [p.double().cpu().numpy() for p in ps] for g, ps in self.params.items()}
+
+    # ---- pieces
+    def _mlp(self, g: str, op_in: _abi.NnOperand, rows_p: int, k_in: int):
+        ctx, dev, P, W = self.ctx, self.device, self.params[g], self.w16[g]
+        h1 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
+        h2 = torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev)
+        z = torch.empty((rows_p, EMBED_DIM), dtype=torch.float32, device=dev)
+        gemm(ctx, op_in, _op(W[0], _abi.NN_KMAJOR, k_in), rows_p, HIDDEN, k_in, h1, bias=P[1], relu=True)
+        gemm(ctx, _op(h1, _abi.NN_KMAJOR, HIDDEN), _op(W[1], _abi.NN_KMAJOR, HIDDEN), rows_p, HIDDEN, HIDDEN, h2, bias=P[3], relu=True)
+        gemm(ctx, _op(h2, _abi.NN_KMAJOR, HIDDEN), _op(W[2], _abi.NN_KMAJOR, HIDDEN), rows_p, EMBED_DIM, HIDDEN, z, bias=P[5])
+        return h1, h2, z
+
+    def _mlp_backward(self, g: str, x_in: torch.Tensor, h1, h2, dz: torch.Tensor, rows_p: int, want_dx: bool):
+        """Gradients of group g from dz (bf16, rows_p x 32); x_in: the masks (leaf) or the bf16 input
+        rows (upper). With want_dx also d loss / d input (FP32, rows_p x 256)."""
+        ctx, dev, W = self.ctx, self.device, self.w16[g]
+        grads = [None] * 6
+        grads[4] = gemm(ctx, _op(dz, _abi.NN_MNMAJOR, EMBED_DIM), _op(h2, _abi.NN_MNMAJOR, HIDDEN), EMBED_DIM, HIDDEN, rows_p,
+                        torch.empty((EMBED_DIM, HIDDEN), dtype=torch.float32, device=dev))
+        grads[5] = self._column_sums(dz)
+        dz2 = gemm(ctx, _op(dz, _abi.NN_KMAJOR, EMBED_DIM), _op(W[2], _abi.NN_MNMAJOR, HIDDEN), rows_p, HIDDEN, EMBED_DIM,
+                   torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev), gate=h2)
+        grads[2] = gemm(ctx, _op(dz2, _abi.NN_MNMAJOR, HIDDEN), _op(h1, _abi.NN_MNMAJOR, HIDDEN), HIDDEN, HIDDEN, rows_p,
+                        torch.empty((HIDDEN, HIDDEN), dtype=torch.float32, device=dev))
+        grads[3] = self._column_sums(dz2)
+        dz1 = gemm(ctx, _op(dz2, _abi.NN_KMAJOR, HIDDEN), _op(W[1], _abi.NN_MNMAJOR, HIDDEN), rows_p, HIDDEN, HIDDEN,
+                   torch.empty((rows_p, HIDDEN), dtype=torch.bfloat16, device=dev), gate=h1)
+        if g == "leaf":
+            grads[0] = gemm(ctx, _op(dz1, _abi.NN_MNMAJOR, HIDDEN), _op(x_in, _abi.NN_BITS_T), HIDDEN, 64, rows_p,
+                            torch.empty((HIDDEN, 64), dtype=torch.float32, device=dev))
+        else:
+            grads[0] = gemm(ctx, _op(dz1, _abi.NN_MNMAJOR, HIDDEN), _op(x_in, _abi.NN_MNMAJOR, 8 * EMBED_DIM), HIDDEN, 8 * EMBED_DIM, rows_p,
+                            torch.empty((HIDDEN, 8 * EMBED_DIM), dtype=torch.float32, device=dev))
+        grads[1] = self._column_sums(dz1)
+        dx = None
+        if want_dx:
+            dx = gemm(ctx, _op(dz1, _abi.NN_KMAJOR, HIDDEN), _op(W[0], _abi.NN_MNMAJOR, 8 * EMBED_DIM), rows_p, 8 * EMBED_DIM, HIDDEN,
+                      torch.empty((rows_p, 8 * EMBED_DIM), dtype=torch.float32, device=dev))
+        return grads, dx
+
+    def _column_sums(self, x: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(x.shape[1], dtype=torch.float32, device=self.device)
+        _abi.check(lib().tdag_nn_column_sums(self.ctx.handle, x.data_ptr(), x.shape[0], x.shape[1], x.stride(0), out.data_ptr()))
+        return out
+
+    def _gather(self, child: torch.Tensor, child_row: torch.Tensor, m: int):
+        """(pad16(m) x 256) bf16 canonical rows (zero padding) and the (m x 8) slots."""
+        x = torch.zeros((max(16, (m + 15) // 16 * 16), 8 * EMBED_DIM), dtype=torch.bfloat16, device=self.device)
+        slot = torch.empty((max(m, 1), 8), dtype=torch.uint8, device=self.device)
+        cr = child_row.to(torch.int32).contiguous()
+        _abi.check(lib().tdag_nn_canon_gather(self.ctx.handle, child.data_ptr(), child.shape[0], cr.data_ptr(), m, x.data_ptr(), slot.data_ptr()))
+        return x, slot, cr
+
+    def _scatter(self, dx: torch.Tensor, cr: torch.Tensor, slot: torch.Tensor, m: int, rows: int) -> torch.Tensor:
+        """d loss / d child rows (bf16, rows x 32) from d loss / d canonical rows."""
+        dchild = torch.zeros((rows, EMBED_DIM), dtype=torch.float32, device=self.device)
+        _abi.check(lib().tdag_nn_canon_scatter(self.ctx.handle, dx.data_ptr(), 0, cr.data_ptr(), slot.data_ptr(), m, dchild.data_ptr(), rows))
+        out = torch.empty((rows, EMBED_DIM), dtype=torch.bfloat16, device=self.device)
+        _abi.check(lib().tdag_nn_to_bf16(self.ctx.handle, dchild.data_ptr(), dchild.numel(), out.data_ptr()))
+        return out
+
+    # ---- forward / backward
+    def forward(self, words: torch.Tensor, level: int, keep: bool = False):
+        """u (n x 32, FP32, L2-normalised) of n items of `level`; with keep, also the cache for backward()."""
+        ctx, dev = self.ctx, self.device
+        masks = block_masks(ctx, words, level)
+        n, B = masks.shape
+        if keep:  # one leaf row per block
+            flat = ProposalEncoder._padded(masks)
+            leaf_row = torch.arange(n * B, device=dev)
+        else:  # the leaf MLP once per distinct mask
+            uniq, inv = torch.unique(masks.reshape(-1), return_inverse=True)
+            flat = ProposalEncoder._padded(uniq)
+            leaf_row = inv
+        h1, h2, z0 = self._mlp("leaf", _op(flat, _abi.NN_BITS), flat.shape[0], 64)
+        cache = {"level": level, "n": n, "leaf": (flat, h1, h2)}
+        present = (masks != 0).reshape(-1)
+        child_row = torch.where(present, leaf_row, torch.full_like(leaf_row, -1))
+        if level == 2:
+            top = z0
+            top_row = child_row.to(torch.int32)
+        elif level == 3:
+            x3, slot3, cr3 = self._gather(z0, child_row.reshape(n, 8), n)
+            a1, a2, top = self._mlp("up3", _op(x3, _abi.NN_KMAJOR, 8 * EMBED_DIM), x3.shape[0], 8 * EMBED_DIM)
+            cache.update(up3=(x3, a1, a2), g3=(cr3, slot3, n, z0.shape[0]))
+            top_row = None
+        else:
+            cr = child_row.reshape(n, 64)[:, self._blk].reshape(n * 8, 8)  # sub-item (i, q), child o
+            x3, slot3, cr3 = self._gather(z0, cr, n * 8)
+            a1, a2, z3 = self._mlp("up3", _op(x3, _abi.NN_KMAJOR, 8 * EMBED_DIM), x3.shape[0], 8 * EMBED_DIM)
+            sub = torch.arange(n * 8, device=dev)
+            cr4 = torch.where((cr >= 0).any(dim=1), sub, torch.full_like(sub, -1)).reshape(n, 8)
+            x4, slot4, cr4 = self._gather(z3, cr4, n)
+            b1, b2, top = self._mlp("up4", _op(x4, _abi.NN_KMAJOR, 8 * EMBED_DIM), x4.shape[0], 8 * EMBED_DIM)
+            cache.update(up3=(x3, a1, a2), g3=(cr3, slot3, n * 8, z0.shape[0]), up4=(x4, b1, b2), g4=(cr4, slot4, n, z3.shape[0]))
+            top_row = None
+        # L2 normalisation: a one-block pool over the top output's rows
+        ones = torch.ones(n, dtype=torch.int64, device=dev) if top_row is None else masks.reshape(n).contiguous()
+        u = torch.empty((n, EMBED_DIM), dtype=torch.float32, device=dev)
+        ub = torch.empty((n, EMBED_DIM), dtype=torch.bfloat16, device=dev)
+        norm = torch.empty(n, dtype=torch.float32, device=dev)
+        count = torch.empty(n, dtype=torch.float32, device=dev)
+        ro = None if top_row is None else top_row.clamp(min=0).contiguous()
+        _abi.check(lib().tdag_nn_pool_forward(ctx.handle, top.data_ptr(), _ptr(ro), ones.data_ptr(), n, 1, u.data_ptr(), ub.data_ptr(),
+                                              norm.data_ptr(), count.data_ptr()))
+        if not keep:
+            return u, ub
+        cache.update(u=u, norm=norm, count=count, ones=ones, top_rows=top.shape[0])
+        return u, ub, cache
+
+    def backward(self, cache: dict, du: torch.Tensor) -> Dict[str, Optional[List[torch.Tensor]]]:
+        """FP32 gradients per group from d loss / d u (n x 32, FP32); None for groups the level does not use."""
+        ctx, dev, n, level = self.ctx, self.device, cache["n"], cache["level"]
+        dz = torch.zeros((cache["top_rows"], EMBED_DIM), dtype=torch.bfloat16, device=dev)
+        _abi.check(lib().tdag_nn_pool_backward(ctx.handle, du.contiguous().data_ptr(), cache["u"].data_ptr(), cache["norm"].data_ptr(),
+                                               cache["count"].data_ptr(), cache["ones"].data_ptr(), n, 1, dz.data_ptr()))
+        out = {"leaf": None, "up3": None, "up4": None}
+        if level == 4:
+            x4, b1, b2 = cache["up4"]
+            out["up4"], dx4 = self._mlp_backward("up4", x4, b1, b2, dz, x4.shape[0], True)
+            cr4, slot4, m4, rows4 = cache["g4"]
+            dz = self._scatter(dx4, cr4, slot4, m4, rows4)
+        if level >= 3:
+            x3, a1, a2 = cache["up3"]
+            out["up3"], dx3 = self._mlp_backward("up3", x3, a1, a2, dz, x3.shape[0], True)
+            cr3, slot3, m3, rows3 = cache["g3"]
+            dz = self._scatter(dx3, cr3, slot3, m3, rows3)
+        flat, h1, h2 = cache["leaf"]
+        out["leaf"], _ = self._mlp_backward("leaf", flat, h1, h2, dz, flat.shape[0], False)
+        return out
+
+    # ---- training (the interface of ProposalEncoder)
+    def loss_and_grads(self, words_t: torch.Tensor, words_p: torch.Tensor, level: int, tau: float):
+        b = words_t.shape[0]
+        assert b % 16 == 0 and b == words_p.shape[0]
+        dev = self.device
+        u, ub, cache = self.forward(torch.cat([words_t, words_p]), level, keep=True)
+        logits = torch.empty((b, b), dtype=torch.float32, device=dev)
+        gemm(self.ctx, _op(ub[:b], _abi.NN_KMAJOR, EMBED_DIM), _op(ub[b:], _abi.NN_KMAJOR, EMBED_DIM), b, b, EMBED_DIM, logits, alpha=1.0 / tau)
+        loss = torch.empty(1, dtype=torch.float32, device=dev)
+        dl = torch.empty((b, b), dtype=torch.bfloat16, device=dev)
+        _abi.check(lib().tdag_nn_info_nce(self.ctx.handle, logits.data_ptr(), b, loss.data_ptr(), dl.data_ptr()))
+        du = torch.empty((2 * b, EMBED_DIM), dtype=torch.float32, device=dev)
+        gemm(self.ctx, _op(dl, _abi.NN_KMAJOR, b), _op(ub[b:], _abi.NN_MNMAJOR, EMBED_DIM), b, EMBED_DIM, b, du[:b], alpha=1.0 / tau)
+        gemm(self.ctx, _op(dl, _abi.NN_MNMAJOR, b), _op(ub[:b], _abi.NN_MNMAJOR, EMBED_DIM), b, EMBED_DIM, b, du[b:], alpha=1.0 / tau)
+        return loss, self.backward(cache, du)
+
+    def adamw_step(self, grads: Dict[str, Optional[Sequence[torch.Tensor]]], lr: float, weight_decay: float = 1e-2, beta1: float = 0.9,
+                   beta2: float = 0.999, eps: float = 1e-8) -> None:
+        """One AdamW step of the groups that have gradients (the others are left as they are)."""
+        self.step_count += 1
+        for gname, gs in grads.items():
+            if gs is None:
+                continue
+            for i, (p, gr) in enumerate(zip(self.params[gname], gs)):
+                w16 = self.w16[gname][i // 2] if i % 2 == 0 else None
+                _abi.check(lib().tdag_nn_adamw(self.ctx.handle, p.data_ptr(), gr.contiguous().data_ptr(), self.m1[gname][i].data_ptr(),
+                                               self.m2[gname][i].data_ptr(), p.numel(), lr, beta1, beta2, eps, weight_decay, self.step_count,
+                                               _ptr(w16)))
+
+    def sync(self) -> None:
+        _abi.check(lib().tdag_nn_sync(self.ctx.handle))
+
+
 def _on_lib_stream(ctx):
     """torch's current stream set to the library context's stream, so that allocations and the
     kernels of both are ordered."""

@@ -2,8 +2,11 @@
  * in the reference; every match it proposes is verified exactly by the matcher, see tdag.h's
  * tdag_build_device_proposed and tdag_find_duplicates_level_device).
  *
- * The encoder is an MLP 64 -> 256 -> 256 -> 32 over the 64-bit occupancy masks of an item's 4^3
- * blocks, mean-pooled over the item's non-empty blocks and L2-normalised; it is trained with a
+ * Two encoders share the kernels. The block encoder is an MLP 64 -> 256 -> 256 -> 32 over the 64-bit
+ * occupancy masks of an item's 4^3 blocks, mean-pooled over the item's non-empty blocks and
+ * L2-normalised. The hierarchical encoder embeds a 4^3 item by the same leaf MLP, and an 8^3 or 16^3
+ * item by an MLP 256 -> 256 -> 256 -> 32 of its level over its eight children's vectors placed in a
+ * canonical octant order (tdag_nn_canon_gather). Both are trained with a
  * symmetric InfoNCE loss and AdamW on FP32 master weights. Its dense layers, the InfoNCE logits and
  * the candidate-scoring dot products run as bf16 GEMMs on the tcgen05 tensor cores (operands staged
  * in shared memory, FP32 accumulators in tensor memory); everything else is plain CUDA.
@@ -81,6 +84,23 @@ int tdag_nn_adamw(tdag_ctx* ctx, float* w, const float* grad, float* m1, float* 
  * idx[i * k + s] (j, or -1 where fewer than k exist) and score[i * k + s] (optional), in no
  * particular order; k is 8, 16 or 32. */
 int tdag_nn_topk(tdag_ctx* ctx, const uint16_t* emb, uint32_t n, uint32_t k, int32_t* idx, float* score);
+
+/* The upper levels' encoder input: each item's eight children pooled under a canonical axis order.
+ * Item i has children o = ox + 2 oy + 4 oz (its octants); child o's 32-wide vector is row
+ * child_row[i * 8 + o] of child (FP32, child_rows rows; -1: an empty child, a zero vector). With b
+ * the item's child occupancy byte (bit o set for a non-empty child) and t the first of the 48
+ * transforms (ID sym | perm << 3) whose image of b is the smallest, child o goes to slot pos_t(o),
+ * its octant under t: x[i * 256 + 32 * slot + d] (bf16) = child[row * 32 + d], zeros for empty
+ * children; slot_of[i * 8 + o] receives each child's slot. A row >= child_rows is recorded as
+ * TDAG_ERR_ARG (reported by tdag_nn_sync) and read as an empty child. */
+int tdag_nn_canon_gather(tdag_ctx* ctx, const float* child, uint32_t child_rows, const int32_t* child_row, uint32_t n, uint16_t* x,
+    uint8_t* slot_of);
+
+/* Gradient of tdag_nn_canon_gather: dchild[row * 32 + d] += dx[i * 256 + 32 * slot_of[i * 8 + o] + d]
+ * for every non-empty child o of every item i (FP32 atomics, so rows may be shared); dx is FP32, or
+ * bf16 when dx_bf16 != 0. dchild (child_rows rows) is accumulated into, not overwritten. */
+int tdag_nn_canon_scatter(tdag_ctx* ctx, const void* dx, int dx_bf16, const int32_t* child_row, const uint8_t* slot_of, uint32_t n,
+    float* dchild, uint32_t child_rows);
 
 /* Synchronises the context's stream and returns the first error a kernel of this header recorded
  * (a tensor-core wait past its bound: TDAG_ERR_CUDA), clearing it. */

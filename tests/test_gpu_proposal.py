@@ -49,7 +49,8 @@ def test_proposed_build_is_lossless(oracle, tdaglib, gpu_ctx):
     assert (dense_got == dense_ex).all()
 
 
-def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx):
+@pytest.mark.parametrize("encoder", ["block", "hierarchical"])
+def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx, encoder):
     from tdag import proposal as P
     cfg = tdaglib.TransformDAGConfig()
     train_sets = []
@@ -57,7 +58,7 @@ def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx):
         for level, words in P.level_items(_scene(tdaglib, gpu_ctx, 256, seed), cfg, ctx=gpu_ctx).items():
             if level >= 3:
                 train_sets.append((words, level, P.exhaustive_parents(gpu_ctx, words, level, cfg)[0]))
-    enc = P.ProposalEncoder(seed=0, ctx=gpu_ctx)
+    enc = (P.ProposalEncoder if encoder == "block" else P.HierarchicalEncoder)(seed=0, ctx=gpu_ctx)
     losses = P.train(enc, train_sets, steps=400, batch=1024)
     assert losses[-1] < losses[0]
     held = P.level_items(_scene(tdaglib, gpu_ctx, 256, 9), cfg, ctx=gpu_ctx)
@@ -68,7 +69,7 @@ def test_learned_proposals_beat_no_network_baselines(tdaglib, gpu_ctx):
         learned = P.recall_at_k(P.propose_lists(P.embed(enc, words, level), pos, 8), parent)
         neighbours = P.recall_at_k(P.popcount_neighbour_lists(pos, 8), parent)
         rand = P.recall_at_k(P.random_lists(pos, 8), parent)
-        print(f"level {level}: recall@8 learned {learned:.3f} popcount-neighbours {neighbours:.3f} random {rand:.3f}")
+        print(f"{encoder} encoder, level {level}: recall@8 learned {learned:.3f} popcount-neighbours {neighbours:.3f} random {rand:.3f}")
         assert learned > neighbours and learned > rand
 
 

@@ -114,3 +114,58 @@ def test_baseline_lists_only_propose_predecessors():
         src = lists.clamp(min=0)
         assert bool((pos[src][ok] < pos.unsqueeze(1).expand_as(lists)[ok]).all())
     assert P.sources_of(P.popcount_neighbour_lists(pos, 1)).numel() == 299  # every item but the last one
+
+
+def test_transform_tables_match_the_library_layout():
+    """The oracle's octant tables: transform 0 is the identity, the 48 transforms of a byte's orbit
+    are distinct permutations of the octants, and canon_slots picks the first smallest image."""
+    pos, byte_map = PO.transform_tables()
+    assert list(pos[0]) == list(range(8))
+    assert all(sorted(pos[t]) == list(range(8)) for t in range(48))
+    assert len({tuple(pos[t]) for t in range(48)}) == 48
+    occ = np.arange(256)
+    slots = PO.canon_slots(occ)
+    for b in (0, 1, 0x80, 0x5A, 0xFF, 0x37):
+        t = min(range(48), key=lambda k: (byte_map[k, b], k))
+        assert list(slots[b]) == list(pos[t])
+        assert sum(1 << int(slots[b][o]) for o in range(8) if (b >> o) & 1) == byte_map[:, b].min()
+
+
+def test_canonical_slots_are_transform_invariant():
+    """Two items whose child occupancies are transforms of each other get the same canonical byte."""
+    pos, byte_map = PO.transform_tables()
+    rng = np.random.default_rng(2)
+    for _ in range(30):
+        b = int(rng.integers(1, 256))
+        t = int(rng.integers(48))
+        bt = int(byte_map[t, b])
+        sb, st = PO.canon_slots(np.array([b, bt]))
+        img = lambda byte, s: sum(1 << int(s[o]) for o in range(8) if (byte >> o) & 1)  # noqa: E731
+        assert img(b, sb) == img(bt, st)
+
+
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_hierarchical_gradients_match_finite_differences_fp64(level):
+    P = PO.init_hier_params(3)
+    n = 5
+    words, _ = random_words(2 * n, level, 10 + level, density=0.2 if level < 4 else 0.05)
+    masks = PO.block_masks(words, level)
+    mt, mp = masks[:n], masks[n:]
+    tau = 0.1
+    loss, grads = PO.hier_grads_of(P, mt, mp, level, tau)
+    assert np.isfinite(loss)
+    used = {2: ["leaf"], 3: ["leaf", "up3"], 4: ["leaf", "up3", "up4"]}[level]
+    assert all(grads[g] is not None for g in used) and all(grads[g] is None for g in grads if g not in used)
+    rng = np.random.default_rng(level)
+    eps = 1e-6
+    for g in used:
+        for pi in range(6):
+            p = P[g][pi]
+            for _ in range(2):
+                idx = tuple(int(rng.integers(s)) for s in p.shape)
+                plus = {k: [q.copy() for q in v] for k, v in P.items()}
+                minus = {k: [q.copy() for q in v] for k, v in P.items()}
+                plus[g][pi][idx] += eps
+                minus[g][pi][idx] -= eps
+                fd = (PO.hier_loss_of(plus, mt, mp, level, tau) - PO.hier_loss_of(minus, mt, mp, level, tau)) / (2 * eps)
+                assert abs(grads[g][pi][idx] - fd) <= 1e-6 + 1e-5 * abs(fd), (g, pi, idx, grads[g][pi][idx], fd)
