@@ -768,6 +768,75 @@ void requireDeviceView(Context& c, const tdag_svdag_view& v)
 // D2H copy into pinned memory runs at link speed; one straight into freshly allocated pageable pages
 // goes page by page through the driver and took ~20 ms for a 32 MB result. The host copies out of
 // the stage run on a few threads for large results.
+// Pinned host blocks for the arrays of host results (tdag_build): the device writes them directly,
+// with no staging copy, and tdag_result_free returns them here. Blocks are powers of two from 64 KiB;
+// freed ones are kept for reuse up to 2 GiB in all (past that they are released). Process-wide, as
+// results outlive their contexts; deliberately never destroyed (results may be freed at exit).
+namespace {
+struct HostPool {
+    std::mutex m;
+    std::unordered_map<void*, size_t> owned; // block -> capacity, for every block of the pool
+    std::unordered_multimap<size_t, void*> spare; // capacity -> cached free block
+    size_t spareBytes = 0;
+    static constexpr size_t kSpareLimit = size_t(2) << 30;
+};
+HostPool& hostPool()
+{
+    static HostPool* pool = new HostPool;
+    return *pool;
+}
+} // namespace
+
+void* hostResultAlloc(size_t bytes)
+{
+    if (bytes == 0)
+        return std::malloc(1);
+    size_t cap = size_t(64) << 10;
+    while (cap < bytes)
+        cap <<= 1;
+    HostPool& P = hostPool();
+    {
+        std::lock_guard<std::mutex> lk(P.m);
+        auto it = P.spare.find(cap);
+        if (it != P.spare.end()) {
+            void* p = it->second;
+            P.spare.erase(it);
+            P.spareBytes -= cap;
+            return p;
+        }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, cap, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(TDAG_ERR_OOM, "pinned host allocation failed");
+    }
+    std::lock_guard<std::mutex> lk(P.m);
+    P.owned[p] = cap;
+    return p;
+}
+
+void hostResultFree(void* p)
+{
+    if (!p)
+        return;
+    HostPool& P = hostPool();
+    {
+        std::lock_guard<std::mutex> lk(P.m);
+        auto it = P.owned.find(p);
+        if (it == P.owned.end()) {
+            std::free(p); // a plain allocation (empty arrays)
+            return;
+        }
+        if (P.spareBytes + it->second <= HostPool::kSpareLimit) {
+            P.spare.emplace(it->second, p);
+            P.spareBytes += it->second;
+            return;
+        }
+        P.owned.erase(it);
+    }
+    cudaFreeHost(p);
+}
+
 void downloadStaged(Context& c, const std::vector<Download>& items)
 {
     size_t total = 0;
@@ -902,19 +971,21 @@ int tdag_build(tdag_ctx* ctx, const tdag_svdag_view* in, const tdag_config* cfg,
         const auto t1 = std::chrono::steady_clock::now();
         DeviceResult dr = buildDevice(c, viewToDevice(&dv), *cfg, &r->stats);
         const auto t2 = std::chrono::steady_clock::now();
-        std::vector<Download> dl;
+        // the result arrays are pinned blocks of the host pool: the device writes them directly
         for (uint32_t l = 3; l <= in->root_level; ++l) {
             const size_t cnt = dr.levels[l].n / 8;
             r->node_counts[l] = cnt;
-            r->nodes[l] = (uint64_t*)std::malloc(cnt ? cnt * 64 : 1);
+            r->nodes[l] = (uint64_t*)hostResultAlloc(cnt * 64);
             TDAG_CHECK(r->nodes[l] != nullptr, TDAG_ERR_OOM, "host allocation failed");
-            dl.push_back({ r->nodes[l], dr.levels[l].get(), cnt * 64 });
+            if (cnt)
+                TDAG_CUDA(cudaMemcpyAsync(r->nodes[l], dr.levels[l].get(), cnt * 64, cudaMemcpyDeviceToHost, s));
         }
         r->leaf_count = dr.leaves.n;
-        r->leaves = (uint64_t*)std::malloc(dr.leaves.n ? dr.leaves.n * 8 : 1);
+        r->leaves = (uint64_t*)hostResultAlloc(dr.leaves.n * 8);
         TDAG_CHECK(r->leaves != nullptr, TDAG_ERR_OOM, "host allocation failed");
-        dl.push_back({ r->leaves, dr.leaves.get(), dr.leaves.n * 8 });
-        downloadStaged(c, dl);
+        if (dr.leaves.n)
+            TDAG_CUDA(cudaMemcpyAsync(r->leaves, dr.leaves.get(), dr.leaves.n * 8, cudaMemcpyDeviceToHost, s));
+        TDAG_CUDA(cudaStreamSynchronize(s));
         if (trace) { // host-side phases: upload enqueue, build (to its return), download
             const auto t3 = std::chrono::steady_clock::now();
             auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
@@ -1340,19 +1411,20 @@ int tdag_result_free(tdag_result* r)
 {
     if (!r)
         return TDAG_OK;
+    // host arrays: pinned pool blocks (tdag_build) or plain allocations (the other host results)
     for (uint32_t l = 0; l < TDAG_MAX_LEVELS; ++l) {
         if (!r->nodes[l])
             continue;
         if (r->on_device)
             cudaFree(r->nodes[l]);
         else
-            std::free(r->nodes[l]);
+            hostResultFree(r->nodes[l]);
     }
     if (r->leaves) {
         if (r->on_device)
             cudaFree(r->leaves);
         else
-            std::free(r->leaves);
+            hostResultFree(r->leaves);
     }
     delete r;
     return TDAG_OK;

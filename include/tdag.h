@@ -84,7 +84,9 @@ typedef struct tdag_stats {
 } tdag_stats;
 
 /* EditStructure<void, TransformPointer> result. Arrays are owned by the library: host memory from
- * tdag_build(), device memory from tdag_build_device(). Release with tdag_result_free(). */
+ * tdag_build() (page-locked blocks the device writes directly; tdag_result_free keeps up to 2 GiB
+ * of them for reuse by later calls), device memory from tdag_build_device(). Release with
+ * tdag_result_free(), never with free(). */
 typedef struct tdag_result {
     uint32_t resolution;
     uint32_t root_level;
