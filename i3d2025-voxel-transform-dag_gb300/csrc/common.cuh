@@ -279,6 +279,9 @@ uint64_t exclusiveScanU32Total(const uint32_t* in, uint32_t* out, size_t n, cuda
 void radixSortPairs(uint64_t* keys, uint32_t* vals, size_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t* status = nullptr);
 // Compact indices i in [0, n) with flags[i] != 0 into out (ascending); returns the count.
 uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s);
+// The same with the device status word read in the same round trip (into hostStatus, 16 bytes):
+// returns its error code; only when it is 0 are the indices compacted and *count set.
+uint32_t compactFlagsChecked(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s, uint32_t* status, uint32_t* hostStatus, uint32_t* count);
 
 // ------------------------------------------------------------------------------------------------
 // Host links of a build (primitives.cu). Every value a build reads back to steer itself (counts,

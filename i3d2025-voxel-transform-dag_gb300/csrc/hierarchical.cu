@@ -489,7 +489,9 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
     DevBuf<uint32_t> canonOf(n, s), isCanon(n, s);
     DevBuf<uint8_t> tOf(n, s);
     DevBuf<uint64_t> invOf(n, s);
-    withClassTable(ctx, n, "hierarchical level " + std::to_string(level), [&](uint64_t cap) {
+    // The class table's status and the number of canonical nodes come back in one round trip; a
+    // table whose bounded probes ran out is doubled and the attempt rerun, as withClassTable does.
+    auto attempt = [&](uint64_t cap) {
         DevBuf<uint64_t> slots(cap, s);
         DevBuf<uint32_t> minIdx(cap, s), slotOf(n, s);
         fillU64(slots.get(), kEmptySlot, cap, s);
@@ -505,10 +507,26 @@ static uint32_t canonicaliseLevel(Context& ctx, uint32_t level, uint32_t n, cons
         TDAG_LAUNCHED();
         slots.release();
         resolve(slotOf.get(), minIdx.get(), canonOf.get(), tOf.get(), invOf.get(), isCanon.get());
-    });
-
+    };
     DevBuf<uint32_t> canonList(n, s);
-    const uint32_t u = compactFlags(isCanon.get(), canonList.get(), n, s);
+    uint32_t u = 0;
+    uint64_t cap = ctx.classTableCapacity(n);
+    for (uint32_t regrows = 0;; ++regrows) {
+        attempt(cap);
+        const uint32_t code = compactFlagsChecked(isCanon.get(), canonList.get(), n, s, ctx.status, ctx.hostStatus, &u);
+        if (code == 0)
+            break;
+        const uint32_t aux = ctx.hostStatus[1];
+        TDAG_CUDA(cudaMemsetAsync(ctx.status, 0, 16, s));
+        syncHost(s);
+        if (code == TDAG_ERR_TABLE_FULL && regrows < ctx.tableRegrowLimit()) {
+            cap *= 2;
+            ++ctx.tableRegrows;
+            continue;
+        }
+        throw Error((int)code, "hierarchical level " + std::to_string(level) + ": device reported error " + std::to_string(code) + " (aux " + std::to_string(aux) +
+                ")" + (code == TDAG_ERR_TABLE_FULL ? " after " + std::to_string(regrows) + " table regrows" : std::string()));
+    }
     isCanon.release();
     DevBuf<uint64_t> sk(u, s);
     emitOrder = DevBuf<uint32_t>(u, s);

@@ -1397,7 +1397,9 @@ __global__ void __launch_bounds__(kThreads, 4) probeKernel(ProbeParams p)
 
 struct LookupParams {
     const ulonglong2* recs;
-    unsigned long long count;
+    const unsigned long long* countDev; // records the probe produced (device): past recCap the launch does nothing
+    unsigned long long recCap;
+    unsigned long long dynamicBelow; // fewer records than this: warps claim them from `cursor`
     const ulonglong2* slots; // run table: home slot = key >> homeShift, slotCount slots
     uint32_t homeShift;
     unsigned long long slotCount;
@@ -1412,7 +1414,7 @@ struct LookupParams {
     const uint32_t* segOff;
     uint32_t allowSym, allowPerm, allowTrans;
     unsigned long long* counters; // [2] hits, [3] candidates, [4] verifications, [5] verified, [6] longest run
-    unsigned long long* cursor; // set: warps claim `tile` records at a time from it (zeroed before the launch)
+    unsigned long long* cursor; // warps claim `tile` records at a time from it when dynamic (zeroed before the launch)
     uint32_t tile; // records per claim (a multiple of 32)
 };
 
@@ -1492,21 +1494,27 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
     // persistent warps, 32 consecutive records per step: with a cursor each warp claims its next 32
     // (balances the few-record batches whose records differ most in verification work; one counter
     // would serialise the claims of the large batches, which take records by a fixed stride)
+    // the range's record count, read on the device: a range whose records overflowed their buffer
+    // is probed again by the host with a larger one, so this launch leaves it alone
+    const unsigned long long count = *p.countDev;
+    if (count > p.recCap)
+        return;
+    const bool dynamic = count < p.dynamicBelow;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
     uint64_t claimEnd = 0;
-    if (p.cursor) {
+    if (dynamic) {
         unsigned long long c = 0;
         if (lane == 0)
             c = atomicAdd(p.cursor, (unsigned long long)p.tile);
         i0 = __shfl_sync(0xffffffffu, c, 0);
         claimEnd = i0 + p.tile;
     }
-    for (; i0 < p.count;) {
+    for (; i0 < count;) {
         const uint64_t i = i0 + lane;
         uint32_t start = 0, cnt = 0;
         uint64_t meta = 0;
-        if (i < p.count) {
+        if (i < count) {
             const ulonglong2 rec = p.recs[i];
             meta = rec.y;
             // from the home slot up to the key or an empty slot (the array ends with one)
@@ -1613,7 +1621,7 @@ __global__ void __launch_bounds__(kThreads) lookupKernel(LookupParams p)
             }
             }
         }
-        if (p.cursor) {
+        if (dynamic) {
             i0 += 32;
             if (i0 >= claimEnd) {
                 unsigned long long c = 0;
@@ -2073,6 +2081,23 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                 TDAG_LAUNCHED();
                 if (timed)
                     TDAG_CUDA(cudaEventRecord(ctx.ev[6], s));
+                // The range's lookup follows at once, with no round trip: it reads the record count
+                // on the device and returns without work if the records overflowed their buffer.
+                lp.recs = recs.get();
+                lp.countDev = recCount.get();
+                lp.recCap = recs.n;
+                lp.dynamicBelow = 1ull << 20; // few records: balance them dynamically
+                lp.begin = pos;
+                lp.srcLines = srcLines.get();
+                lp.cursor = lookupCursor.get();
+                lp.tile = lookupTile;
+                TDAG_CUDA(cudaMemsetAsync(lp.cursor, 0, 8, s));
+                if (trace)
+                    TDAG_CUDA(cudaEventRecord(traceEv[0], s));
+                lookup<<<lookupBlocks, kThreads, 0, s>>>(lp);
+                TDAG_LAUNCHED();
+                if (trace)
+                    TDAG_CUDA(cudaEventRecord(traceEv[1], s));
                 uint64_t* hp = pinnedScratch();
                 readToHost({ { hp, recCount.get(), 8 } }, s);
                 produced = hp[0];
@@ -2081,6 +2106,11 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
                     TDAG_CUDA(cudaEventElapsedTime(&pm, ctx.ev[5], ctx.ev[6]));
                     probeMs += pm;
                     traceProbeMs += pm;
+                }
+                if (trace) {
+                    float lm = 0;
+                    TDAG_CUDA(cudaEventElapsedTime(&lm, traceEv[0], traceEv[1]));
+                    traceLookupMs += lm;
                 }
                 if (produced <= pp.recCap)
                     break;
@@ -2098,32 +2128,7 @@ MatchOutput runMatcherL(Context& ctx, const uint64_t* grids, uint32_t n, const t
             if (timed)
                 TDAG_CUDA(cudaMemcpyAsync(probeCounts, counters.get(), 16, cudaMemcpyDeviceToHost, s));
             recsPerSource = 0.5 * recsPerSource + 0.5 * ((double)produced / cs);
-            if (produced) {
-                lp.recs = recs.get();
-                lp.count = produced;
-                lp.begin = pos;
-                lp.srcLines = srcLines.get();
-                lp.cursor = nullptr;
-                lp.tile = lookupTile;
-                if (produced < (1ull << 20)) { // few records: balance them dynamically
-                    lp.cursor = lookupCursor.get();
-                    TDAG_CUDA(cudaMemsetAsync(lp.cursor, 0, 8, s));
-                }
-                const uint64_t warpsNeeded = (produced + 31) / 32;
-                const unsigned lblocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)lookupBlocks, (warpsNeeded + kThreads / 32 - 1) / (kThreads / 32)));
-                if (trace)
-                    TDAG_CUDA(cudaEventRecord(traceEv[0], s));
-                lookup<<<lblocks, kThreads, 0, s>>>(lp);
-                TDAG_LAUNCHED();
-                if (trace) {
-                    TDAG_CUDA(cudaEventRecord(traceEv[1], s));
-                    TDAG_CUDA(cudaEventSynchronize(traceEv[1]));
-                    float lm = 0;
-                    TDAG_CUDA(cudaEventElapsedTime(&lm, traceEv[0], traceEv[1]));
-                    traceLookupMs += lm;
-                    traceRecords += produced;
-                }
-            }
+            traceRecords += produced;
             pos += cs;
         }
         if (timed)

@@ -285,6 +285,26 @@ std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx,
     return off;
 }
 
+uint32_t compactFlagsChecked(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s, uint32_t* status, uint32_t* hostStatus, uint32_t* count)
+{
+    *count = 0;
+    if (n == 0) {
+        readToHost({ { hostStatus, status, 16 } }, s);
+        return hostStatus[0];
+    }
+    DevBuf<uint32_t> offs(n, s);
+    exclusiveScanU32(flags, offs.get(), n, s);
+    uint32_t* pair = reinterpret_cast<uint32_t*>(pinnedScratch());
+    readToHost({ { &pair[0], flags + n - 1, 4 }, { &pair[1], offs.get() + n - 1, 4 }, { hostStatus, status, 16 } }, s);
+    const uint32_t code = hostStatus[0];
+    if (code == 0) {
+        scatterFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(flags, offs.get(), out, n);
+        TDAG_LAUNCHED();
+        *count = pair[0] + pair[1];
+    }
+    return code;
+}
+
 uint32_t compactFlags(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s)
 {
     if (n == 0)
