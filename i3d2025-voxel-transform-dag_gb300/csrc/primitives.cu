@@ -285,22 +285,37 @@ std::vector<uint64_t> countPerGrid(const uint32_t* gridIds, const uint32_t* idx,
     return off;
 }
 
+namespace {
+// The status words and, when they hold no error, the flag total: what a checked compaction reads
+// back (a failed attempt's flags are not read, so the values read depend on the input alone).
+__global__ void statusAndTotalKernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ offs, size_t n, const uint32_t* __restrict__ status,
+    uint32_t* __restrict__ out)
+{
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 4; ++k)
+            out[k] = status[k];
+        out[4] = status[0] == 0 && n ? flags[n - 1] + offs[n - 1] : 0u;
+    }
+}
+} // namespace
+
 uint32_t compactFlagsChecked(const uint32_t* flags, uint32_t* out, size_t n, cudaStream_t s, uint32_t* status, uint32_t* hostStatus, uint32_t* count)
 {
     *count = 0;
-    if (n == 0) {
-        readToHost({ { hostStatus, status, 16 } }, s);
-        return hostStatus[0];
-    }
-    DevBuf<uint32_t> offs(n, s);
-    exclusiveScanU32(flags, offs.get(), n, s);
-    uint32_t* pair = reinterpret_cast<uint32_t*>(pinnedScratch());
-    readToHost({ { &pair[0], flags + n - 1, 4 }, { &pair[1], offs.get() + n - 1, 4 }, { hostStatus, status, 16 } }, s);
-    const uint32_t code = hostStatus[0];
-    if (code == 0) {
+    DevBuf<uint32_t> offs(std::max<size_t>(n, 1), s), both(8, s);
+    if (n)
+        exclusiveScanU32(flags, offs.get(), n, s);
+    statusAndTotalKernel<<<1, 32, 0, s>>>(flags, offs.get(), n, status, both.get());
+    TDAG_LAUNCHED();
+    uint32_t* words = reinterpret_cast<uint32_t*>(pinnedScratch());
+    readToHost({ { words, both.get(), 20 } }, s);
+    for (int k = 0; k < 4; ++k)
+        hostStatus[k] = words[k];
+    const uint32_t code = words[0];
+    if (code == 0 && n) {
         scatterFlagsKernel<<<gridFor(n, 256), 256, 0, s>>>(flags, offs.get(), out, n);
         TDAG_LAUNCHED();
-        *count = pair[0] + pair[1];
+        *count = words[4];
     }
     return code;
 }
