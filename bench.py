@@ -699,6 +699,7 @@ def run_ours(args, world, rank, local, pg):
     cfg_c = tdag._config_struct(cfg)
     d2h = 0
     e2e_s = 0.0
+    e2e_steps = []
     for i in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -711,6 +712,7 @@ def run_ours(args, world, rank, local, pg):
         tdag.lib().tdag_result_free(rp)
         if i >= args.warmup:
             e2e_s += dt
+            e2e_steps.append(dt * 1e3)
     e2e_s = max_over_ranks(pg, e2e_s)
     e2e_value = replica_value(voxels, args.steps, world, e2e_s)
 
@@ -786,7 +788,8 @@ def run_ours(args, world, rank, local, pg):
         "dtype": "u64", "data": "synthetic (device-generated primitive scene; no public dataset)",
         "config": workload_config(args, voxels),
         "roofline": roof,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step_ms": [round(x, 3) for x in e2e_steps]},
         "clocks": clk,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats_list)),
         "subgrids_matched_per_s": sum(last["translation"][L]["items"] for L in (2, 3, 4)) / (dev_ms / args.steps / 1e3),
