@@ -25,6 +25,15 @@
 
 namespace tdag {
 
+// Checkpointing of the streamed scene build (tdag_scene_svdag_checkpointed): the file, a checkpoint
+// every `every` finished chunks (0: none), and a stop after `stop_after` chunks of this call (0: none;
+// the build then writes its checkpoint and fails with TDAG_ERR_INTERRUPTED).
+struct StreamCheckpoint {
+    const char* path;
+    uint32_t every;
+    uint32_t stop_after;
+};
+
 struct SvdagOwned {
     uint32_t resolution = 0, rootLevel = 0, structureType = 0;
     std::vector<DevBuf<uint32_t>> nodes;
@@ -833,9 +842,103 @@ DevBuf<uint32_t> mergeLevel(Context& ctx, GlobalLevel& g, const uint64_t* keys, 
 
 inline uint32_t log2u(uint32_t v) { return (uint32_t)(31 - __builtin_clz(v)); }
 
+// ------------------------------------------------------------------------------------------------
+// Checkpoints of the streamed build: after a chunk, the state that the rest of the build depends on
+// is the global levels' unique items (in first-occurrence order), every finished chunk's root id,
+// the voxel count and the next chunk. The slab tables are not stored: they are rebuilt from the
+// items on resume, and since a new item's id is its place in that order, the resumed build assigns
+// the same ids as an uninterrupted one. Layout (little-endian): "TDAGCKP1", the scene fields and the
+// chunk resolution (validated on resume), the next chunk, the voxel count, the number of levels,
+// per level (2 .. chunk root) its words per item, item count and items, then every chunk's root id.
+// Written to `path`.tmp and renamed over `path`, so a checkpoint on disk is always complete.
+// ------------------------------------------------------------------------------------------------
+constexpr char kCkptMagic[8] = { 'T', 'D', 'A', 'G', 'C', 'K', 'P', '1' };
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t kind, resolution, seed, numPrimitives, copyPercent, shell, chunkRes, levels;
+    uint64_t nextChunk, voxels, numChunks;
+};
+
+bool sameScene(const CkptHeader& h, const tdag_scene& sc, uint32_t chunkRes, uint64_t numChunks, uint32_t levels)
+{
+    return std::memcmp(h.magic, kCkptMagic, 8) == 0 && h.kind == sc.kind && h.resolution == sc.resolution && h.seed == sc.seed &&
+        h.numPrimitives == sc.num_primitives && h.copyPercent == sc.copy_percent && h.shell == sc.shell && h.chunkRes == chunkRes &&
+        h.numChunks == numChunks && h.levels == levels;
+}
+
+void writeCheckpoint(Context& ctx, const std::string& path, const tdag_scene& sc, uint32_t chunkRes, uint64_t nextChunk, uint64_t voxels,
+    const std::vector<GlobalLevel>& glv, const std::vector<uint32_t>& chunkRoot)
+{
+    CkptHeader h {};
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.kind = sc.kind;
+    h.resolution = sc.resolution;
+    h.seed = sc.seed;
+    h.numPrimitives = sc.num_primitives;
+    h.copyPercent = sc.copy_percent;
+    h.shell = sc.shell;
+    h.chunkRes = chunkRes;
+    h.levels = (uint32_t)glv.size();
+    h.nextChunk = nextChunk;
+    h.voxels = voxels;
+    h.numChunks = chunkRoot.size();
+    const std::string tmp = path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    TDAG_CHECK(f != nullptr, TDAG_ERR_ARG, "cannot write the checkpoint " + tmp);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+    std::vector<uint64_t> host;
+    for (uint32_t l = 2; ok && l < glv.size(); ++l) {
+        const uint64_t meta[2] = { (uint64_t)glv[l].words, glv[l].count };
+        host.resize(glv[l].count * glv[l].words);
+        if (!host.empty()) {
+            TDAG_CUDA(cudaMemcpyAsync(host.data(), glv[l].items.get(), host.size() * 8, cudaMemcpyDeviceToHost, ctx.stream));
+            TDAG_CUDA(cudaStreamSynchronize(ctx.stream));
+        }
+        ok = std::fwrite(meta, sizeof meta, 1, f) == 1 && (host.empty() || std::fwrite(host.data(), 8, host.size(), f) == host.size());
+    }
+    ok = ok && std::fwrite(chunkRoot.data(), 4, chunkRoot.size(), f) == chunkRoot.size();
+    ok = (std::fclose(f) == 0) && ok;
+    TDAG_CHECK(ok, TDAG_ERR_ARG, "writing the checkpoint " + tmp + " failed");
+    TDAG_CHECK(std::rename(tmp.c_str(), path.c_str()) == 0, TDAG_ERR_ARG, "cannot move the checkpoint to " + path);
+}
+
+// Restores a checkpoint of the same scene into glv / chunkRoot; returns the next chunk (0 when the
+// file does not exist). A file of another scene or a damaged one is an error (TDAG_ERR_CORRUPT).
+uint64_t readCheckpoint(Context& ctx, const std::string& path, const tdag_scene& sc, uint32_t chunkRes, uint64_t& voxels, std::vector<GlobalLevel>& glv,
+    std::vector<uint32_t>& chunkRoot)
+{
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f)
+        return 0;
+    std::unique_ptr<FILE, int (*)(FILE*)> guard(f, &std::fclose);
+    CkptHeader h {};
+    TDAG_CHECK(std::fread(&h, sizeof h, 1, f) == 1, TDAG_ERR_CORRUPT, "checkpoint " + path + ": truncated header");
+    TDAG_CHECK(sameScene(h, sc, chunkRes, chunkRoot.size(), (uint32_t)glv.size()), TDAG_ERR_CORRUPT, "checkpoint " + path + " is of another scene");
+    TDAG_CHECK(h.nextChunk <= h.numChunks, TDAG_ERR_CORRUPT, "checkpoint " + path + ": chunk cursor out of range");
+    for (uint32_t l = 2; l < glv.size(); ++l) {
+        uint64_t meta[2];
+        TDAG_CHECK(std::fread(meta, sizeof meta, 1, f) == 1, TDAG_ERR_CORRUPT, "checkpoint " + path + ": truncated level");
+        TDAG_CHECK(meta[0] == (uint64_t)glv[l].words && meta[1] < 0xFFFFFFF0ull, TDAG_ERR_CORRUPT, "checkpoint " + path + ": bad level header");
+        std::vector<uint64_t> host(meta[1] * meta[0]);
+        TDAG_CHECK(host.empty() || std::fread(host.data(), 8, host.size(), f) == host.size(), TDAG_ERR_CORRUPT, "checkpoint " + path + ": truncated items");
+        GlobalLevel& g = glv[l];
+        g.items = DevBuf<uint64_t>(std::max<size_t>(host.size(), 1), ctx.stream);
+        if (!host.empty()) {
+            TDAG_CUDA(cudaMemcpyAsync(g.items.get(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, ctx.stream));
+            TDAG_CUDA(cudaStreamSynchronize(ctx.stream));
+        }
+        g.count = meta[1];
+        reserveGlobal(ctx, g, 0); // the slab table, rebuilt from the items
+    }
+    TDAG_CHECK(std::fread(chunkRoot.data(), 4, chunkRoot.size(), f) == chunkRoot.size(), TDAG_ERR_CORRUPT, "checkpoint " + path + ": truncated roots");
+    voxels = h.voxels;
+    return h.nextChunk;
+}
+
 } // namespace
 
-std::unique_ptr<SvdagOwned> sceneSvdagStreamed(Context& ctx, const tdag_scene& sc, uint32_t chunkRes)
+std::unique_ptr<SvdagOwned> sceneSvdagStreamed(Context& ctx, const tdag_scene& sc, uint32_t chunkRes, const StreamCheckpoint* ckpt)
 {
     cudaStream_t s = ctx.stream;
     const uint32_t res = sc.resolution, root = log2u(res), lc = log2u(chunkRes);
@@ -880,7 +983,18 @@ std::unique_ptr<SvdagOwned> sceneSvdagStreamed(Context& ctx, const tdag_scene& s
     uint64_t voxels = 0;
     const uint32_t bpa = chunkRes / kBrick;
     const uint64_t cells = (uint64_t)(chunkRes / 4) * (chunkRes / 4) * (chunkRes / 4);
-    for (uint64_t m = 0; m < numChunks; ++m) {
+    const bool saving = ckpt && ckpt->path && ckpt->path[0];
+    const uint64_t firstChunk = saving ? readCheckpoint(ctx, ckpt->path, sc, chunkRes, voxels, glv, chunkRoot) : 0;
+    uint64_t processed = 0; // chunks finished by this call
+    auto chunkDone = [&](uint64_t m) {
+        ++processed;
+        const bool stop = ckpt && ckpt->stop_after && processed == ckpt->stop_after && m + 1 < numChunks;
+        if (saving && (stop || (ckpt->every && processed % ckpt->every == 0 && m + 1 < numChunks)))
+            writeCheckpoint(ctx, ckpt->path, sc, chunkRes, m + 1, voxels, glv, chunkRoot);
+        TDAG_CHECK(!stop, TDAG_ERR_INTERRUPTED, "streamed scene build stopped after " + std::to_string(processed) + " chunks as requested (next chunk " +
+                std::to_string(m + 1) + ")");
+    };
+    for (uint64_t m = firstChunk; m < numChunks; chunkDone(m), ++m) {
         const uint32_t nc = candOff[m + 1] - candOff[m];
         if (sc.kind == TDAG_SCENE_PRIMITIVES && nc == 0)
             continue; // nothing reaches this chunk: empty
@@ -954,7 +1068,7 @@ std::unique_ptr<SvdagOwned> sceneSvdagStreamed(Context& ctx, const tdag_scene& s
     return out;
 }
 
-std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool toDag)
+std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool toDag, const StreamCheckpoint* ckpt)
 {
     TDAG_CHECK(sc.kind == TDAG_SCENE_TERRAIN || sc.kind == TDAG_SCENE_PRIMITIVES, TDAG_ERR_ARG, "unknown scene kind");
     TDAG_CHECK(sc.resolution >= 32 && sc.resolution <= 16384 && (sc.resolution & (sc.resolution - 1)) == 0, TDAG_ERR_ARG,
@@ -965,8 +1079,9 @@ std::unique_ptr<SvdagOwned> sceneSvdag(Context& ctx, const tdag_scene& sc, bool 
     const uint32_t chunk = sc.chunk_resolution ? sc.chunk_resolution : (res > 4096 ? 2048u : 0u);
     if (chunk) {
         TDAG_CHECK(toDag, TDAG_ERR_ARG, "a streamed scene build always deduplicates (to_dag = 1)");
-        return sceneSvdagStreamed(ctx, sc, chunk);
+        return sceneSvdagStreamed(ctx, sc, chunk, ckpt);
     }
+    TDAG_CHECK(!ckpt, TDAG_ERR_ARG, "checkpoints apply to the streamed (chunked) scene build: set chunk_resolution");
     TDAG_CHECK(cells < (1ull << 32), TDAG_ERR_ARG, "scene too large for the single-pass generator");
     auto prims = scenePrimitives(sc);
     std::vector<DevPrim> dp(prims.size());
@@ -1048,7 +1163,23 @@ int tdag_scene_svdag(tdag_ctx* ctx, const tdag_scene* scene, int toDag, tdag_svd
         Context& c = ctxOf(ctx);
         TDAG_CUDA(cudaSetDevice(c.device));
         auto h = std::make_unique<tdag_svdag>();
-        h->g = sceneSvdag(c, *scene, toDag != 0);
+        h->g = sceneSvdag(c, *scene, toDag != 0, nullptr);
+        *out = h.release();
+    });
+}
+
+int tdag_scene_svdag_checkpointed(tdag_ctx* ctx, const tdag_scene* scene, const char* checkpoint_path, uint32_t every_chunks, uint32_t stop_after_chunks,
+    tdag_svdag** out)
+{
+    if (!ctx || !scene || !out || !checkpoint_path || !checkpoint_path[0])
+        return failWith(TDAG_ERR_ARG, "null argument or empty checkpoint path");
+    *out = nullptr;
+    return guardedCall([&] {
+        Context& c = ctxOf(ctx);
+        TDAG_CUDA(cudaSetDevice(c.device));
+        StreamCheckpoint ck { checkpoint_path, every_chunks, stop_after_chunks };
+        auto h = std::make_unique<tdag_svdag>();
+        h->g = sceneSvdag(c, *scene, true, &ck);
         *out = h.release();
     });
 }

@@ -448,6 +448,20 @@ def scene_svdag(spec: SceneSpec, to_dag: bool = True, ctx: Optional[Context] = N
     return DeviceSvdag(h, ctx)
 
 
+def scene_svdag_checkpointed(spec: SceneSpec, path: str, every_chunks: int = 0, stop_after_chunks: int = 0,
+                             ctx: Optional[Context] = None) -> DeviceSvdag:
+    """scene_svdag of a streamed scene with checkpoints (tdag_scene_svdag_checkpointed): resumes from
+    `path` when it holds a checkpoint of the same scene, writes one every `every_chunks` chunks, and
+    with stop_after_chunks raises TDagError (TDAG_ERR_INTERRUPTED) after that many chunks, checkpoint
+    written."""
+    ctx = ctx or default_context()
+    h = ctypes.c_void_p()
+    c = spec.to_c()
+    _abi.check(lib().tdag_scene_svdag_checkpointed(ctx.handle, ctypes.byref(c), os.fsencode(path), every_chunks, stop_after_chunks,
+                                                   ctypes.byref(h)))
+    return DeviceSvdag(h, ctx)
+
+
 def svdag_from_dense(dense: np.ndarray, to_dag: bool = True, ctx: Optional[Context] = None) -> DeviceSvdag:
     """EditStructure(VoxelGrid) (+ toDAG) on the device; dense[z, y, x] (x fastest)."""
     ctx = ctx or default_context()

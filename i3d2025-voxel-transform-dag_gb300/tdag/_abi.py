@@ -16,9 +16,10 @@ TDAG_ERR_ALLOC = 4
 TDAG_ERR_CUDA = 5
 TDAG_ERR_CORRUPT = 6
 TDAG_ERR_NO_DEVICE = 7
+TDAG_ERR_INTERRUPTED = 8
 MAX_LEVELS = 32
 
-ERROR_NAMES = {1: "ARG", 2: "OOM", 3: "TABLE_FULL", 4: "ALLOC", 5: "CUDA", 6: "CORRUPT", 7: "NO_DEVICE"}
+ERROR_NAMES = {1: "ARG", 2: "OOM", 3: "TABLE_FULL", 4: "ALLOC", 5: "CUDA", 6: "CORRUPT", 7: "NO_DEVICE", 8: "INTERRUPTED"}
 
 
 class TDagError(RuntimeError):
@@ -126,7 +127,7 @@ EXPORTED = (
     "tdag_version", "tdag_last_error_message", "tdag_ctx_create", "tdag_ctx_destroy", "tdag_ctx_stream",
     "tdag_build", "tdag_build_device", "tdag_result_free", "tdag_find_duplicates_level", "tdag_build_hierarchical",
     "tdag_scene_primitives", "tdag_scene_svdag", "tdag_svdag_from_dense", "tdag_svdag_get_view", "tdag_svdag_voxel_count",
-    "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc",
+    "tdag_svdag_copy_level", "tdag_svdag_free", "tdag_find_duplicates_level_noalloc", "tdag_scene_svdag_checkpointed",
     "tdag_build_batched", "tdag_build_batched_device", "tdag_result_to_host",
     "tdag_find_duplicates_level_device", "tdag_build_device_proposed", "tdag_device_copy",
     "tdag_build_static", "tdag_static_result_free",
@@ -182,6 +183,7 @@ def lib(path: str = None):
                                                  ctypes.POINTER(LevelStats)]
         L.tdag_scene_primitives.argtypes = [ctypes.POINTER(Scene), ctypes.POINTER(Primitive), ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         L.tdag_scene_svdag.argtypes = [vp, ctypes.POINTER(Scene), ctypes.c_int, ctypes.POINTER(vp)]
+        L.tdag_scene_svdag_checkpointed.argtypes = [vp, ctypes.POINTER(Scene), ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(vp)]
         L.tdag_svdag_from_dense.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(vp)]
         L.tdag_svdag_get_view.argtypes = [vp, ctypes.POINTER(SvdagView)]
         L.tdag_svdag_voxel_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]

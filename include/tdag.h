@@ -31,6 +31,7 @@ extern "C" {
 #define TDAG_ERR_CUDA 5 /* a CUDA runtime call failed */
 #define TDAG_ERR_CORRUPT 6 /* malformed input structure (dangling child pointer, bad sizes) */
 #define TDAG_ERR_NO_DEVICE 7 /* no CUDA device / kernels not loadable for this GPU */
+#define TDAG_ERR_INTERRUPTED 8 /* a build stopped where the caller asked; its checkpoint is on disk */
 
 #define TDAG_MAX_LEVELS 32
 
@@ -316,6 +317,17 @@ typedef struct tdag_svdag tdag_svdag; /* device-resident EditStructure<void, uin
 int tdag_scene_primitives(const tdag_scene* scene, tdag_primitive* out, uint32_t capacity, uint32_t* count);
 /* Generate the scene on the device, build its SVO and, if to_dag, deduplicate it (toDAG). */
 int tdag_scene_svdag(tdag_ctx* ctx, const tdag_scene* scene, int to_dag, tdag_svdag** out);
+/* tdag_scene_svdag (to_dag = 1) of a streamed scene (chunk_resolution set, or above 4096^3) with
+ * checkpoints, for builds long enough to be interrupted (no counterpart in the reference, whose stage
+ * files are its only checkpoints). After every `every_chunks` finished chunks (0: never) the build
+ * writes its state -- the global levels' unique items, every finished chunk's root, the voxel count
+ * and the next chunk -- to checkpoint_path (through a temporary file and a rename). If
+ * checkpoint_path holds a checkpoint of the same scene, the build resumes from it; one of another
+ * scene or a damaged one returns TDAG_ERR_CORRUPT. stop_after_chunks > 0 stops the call after that
+ * many chunks, checkpoint written, with TDAG_ERR_INTERRUPTED. A resumed build's result is identical
+ * to an uninterrupted build's. The caller removes the file when done. */
+int tdag_scene_svdag_checkpointed(tdag_ctx* ctx, const tdag_scene* scene, const char* checkpoint_path, uint32_t every_chunks,
+    uint32_t stop_after_chunks, tdag_svdag** out);
 /* Same from a host dense grid: dense[x + res*y + res*res*z] != 0 means solid. */
 int tdag_svdag_from_dense(tdag_ctx* ctx, const uint8_t* dense, uint32_t resolution, int to_dag, tdag_svdag** out);
 /* Device-pointer view (valid until tdag_svdag_free), the number of solid voxels of the grid, and

@@ -109,3 +109,13 @@ def test_batch_graph_entry_points_reject_bad_arguments_without_a_device(tdaglib)
     res = (ctypes.POINTER(_abi.Result) * 1)()
     assert L.tdag_batch_graph_launch(None, res, None) == _abi.TDAG_ERR_ARG
     assert L.tdag_batch_graph_free(None) == _abi.TDAG_OK
+
+
+def test_checkpointed_scene_rejects_bad_arguments_without_a_device(tdaglib):
+    import ctypes
+    from tdag import _abi
+    L = tdaglib.lib()
+    out = ctypes.c_void_p()
+    sc = tdaglib.SceneSpec(kind=tdaglib.SCENE_PRIMITIVES, resolution=256, chunk_resolution=64).to_c()
+    assert L.tdag_scene_svdag_checkpointed(None, ctypes.byref(sc), b"x.ckpt", 1, 0, ctypes.byref(out)) == _abi.TDAG_ERR_ARG
+    assert L.tdag_scene_svdag_checkpointed(None, ctypes.byref(sc), None, 1, 0, ctypes.byref(out)) == _abi.TDAG_ERR_ARG

@@ -144,3 +144,31 @@ def test_device_scene_equals_cpu_scene_statement(oracle, tdaglib, gpu_ctx):
     _assert_same(got, _svo_struct(tdaglib, oracle, dense, True))
     sub = oracle.scene_dense(512, 13, 400, origin=(256, 128, 0), size=128)
     assert np.array_equal(sub, dense[0:128, 128:256, 256:384])
+
+
+def test_streamed_scene_resumes_from_its_checkpoints(tdaglib, gpu_ctx, tmp_path):
+    """A streamed scene build stopped twice on the host (TDAG_ERR_INTERRUPTED after a given number
+    of chunks, checkpoint written) and resumed from its checkpoint file ends with the SVDAG of an
+    uninterrupted build: same items, same order, same voxel count. A checkpoint of another scene or a
+    truncated one is refused (TDAG_ERR_CORRUPT), never read past its end."""
+    from tdag import _abi
+    base = dict(kind=tdaglib.SCENE_PRIMITIVES, resolution=512, seed=5, num_primitives=300, chunk_resolution=64)
+    whole = tdaglib.scene_svdag(tdaglib.SceneSpec(**base), to_dag=True, ctx=gpu_ctx)
+    path = str(tmp_path / "scene.ckpt")
+    for stop in (70, 150):
+        with pytest.raises(tdaglib.TDagError) as e:
+            tdaglib.scene_svdag_checkpointed(tdaglib.SceneSpec(**base), path, every_chunks=16, stop_after_chunks=stop, ctx=gpu_ctx)
+        assert e.value.code == _abi.TDAG_ERR_INTERRUPTED
+    saved = open(path, "rb").read()
+    resumed = tdaglib.scene_svdag_checkpointed(tdaglib.SceneSpec(**base), path, every_chunks=16, ctx=gpu_ctx)
+    _assert_same(resumed.to_host(), whole.to_host())
+    assert resumed.voxel_count == whole.voxel_count
+    # the same file for another scene, and a truncated copy
+    with pytest.raises(tdaglib.TDagError) as e:
+        tdaglib.scene_svdag_checkpointed(tdaglib.SceneSpec(**dict(base, seed=6)), path, ctx=gpu_ctx)
+    assert e.value.code == _abi.TDAG_ERR_CORRUPT
+    cut = str(tmp_path / "cut.ckpt")
+    open(cut, "wb").write(saved[: len(saved) // 2])
+    with pytest.raises(tdaglib.TDagError) as e:
+        tdaglib.scene_svdag_checkpointed(tdaglib.SceneSpec(**base), cut, ctx=gpu_ctx)
+    assert e.value.code == _abi.TDAG_ERR_CORRUPT
