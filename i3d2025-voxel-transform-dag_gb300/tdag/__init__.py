@@ -635,6 +635,32 @@ def construct_transform_dag16(dag, dag_config: TransformDAGConfig = TransformDAG
     return (data, stats) if return_stats else data
 
 
+def encoding_stats_json(stats: dict, total_size_in_bytes: int, dag_config: TransformDAGConfig = TransformDAGConfig(),
+                        encoding_config: TransformEncodingConfig = TransformEncodingConfig()) -> dict:
+    """The svdag_encoding tool's --stats JSON (DAGEncodingStats::write and LevelStats' conversion,
+    tools/svdag_encoding/src/transform_dag_encoding.cpp:58-82) from construct_transform_dag16's
+    stats: one entry per tree level 0 .. root (zeros below the leaves), the file size and both configs."""
+    root = max(stats["levels"]) if stats["levels"] else 0
+    pt = bool(encoding_config.pointer_tables)
+    levels = []
+    for l in range(root + 1):
+        st = stats["levels"].get(l)
+        if st is None:
+            levels.append({"num_table_pointers_of_size_u16": [0, 0, 0], "num_direct_pointers_of_size_u16": [0, 0, 0],
+                           "table_size_in_pointers": 0, "pointer_size_in_table": 0, "num_nodes": 0, "memory_in_bytes": 0})
+            continue
+        node_level = l >= 3  # the pointer statistics belong to the node level whose children they point to
+        levels.append({"num_table_pointers_of_size_u16": [int(v) for v in st["table_pointers"]],
+                       "num_direct_pointers_of_size_u16": [int(v) for v in st["direct_pointers"]],
+                       "table_size_in_pointers": int(st["table_size"]) if (pt and node_level) else 0,
+                       "pointer_size_in_table": 8 if (pt and node_level) else 0,
+                       "num_nodes": int(st["num_nodes"]), "memory_in_bytes": int(st["memory_in_bytes"])})
+    return {"levels": levels, "total_size_in_bytes": int(total_size_in_bytes), "pointer_tables": pt,
+            "huffman_code": bool(encoding_config.huffman_code), "symmetry": bool(dag_config.symmetry),
+            "axis_permutation": bool(dag_config.axis_permutation), "enable_translation": bool(dag_config.translation),
+            "translation_level": int(dag_config.max_translation_level)}
+
+
 def create_length_limited_huffman_code_table(frequencies, max_code_length: int = 16, lsb_first: bool = False):
     """createLengthLimitedHuffmanCodeTable (+ convertHuffmanToLSB when lsb_first) (huffman.cpp:165-182):
     a list of (code, bits) per symbol. Host computation in libtdag.so."""

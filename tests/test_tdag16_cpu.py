@@ -154,3 +154,26 @@ def test_library_huffman_matches_oracle(oracle, tdaglib, seed):
     for lsb in (False, True):
         want = oracle.huffman_codes(oracle.huffman_lengths(freq, 16), lsb=lsb)
         assert tdaglib.create_length_limited_huffman_code_table(freq, 16, lsb_first=lsb) == want
+
+
+def test_encoding_stats_json_has_the_reference_shape(tdaglib):
+    """encoding_stats_json writes the svdag_encoding tool's --stats document
+    (transform_dag_encoding.cpp:58-82): one entry per level from 0, the file size and both configs."""
+    lv = lambda n: {"num_nodes": n, "memory_in_bytes": 2 * n, "table_size": n // 2, "unique_pointers": n, "table_pointers": [n, 1, 0],  # noqa: E731
+                    "direct_pointers": [0, 2, 0]}
+    stats = {"levels": {2: lv(10), 3: lv(6), 4: lv(2)}}
+    enc = tdaglib.TransformEncodingConfig(pointer_tables=True, huffman_code=False)
+    cfg = tdaglib.TransformDAGConfig(True, False, True, 3)
+    j = tdaglib.encoding_stats_json(stats, 1234, cfg, enc)
+    assert set(j) == {"levels", "total_size_in_bytes", "pointer_tables", "huffman_code", "symmetry", "axis_permutation",
+                      "enable_translation", "translation_level"}
+    assert len(j["levels"]) == 5 and j["levels"][0]["num_nodes"] == 0
+    assert set(j["levels"][3]) == {"num_table_pointers_of_size_u16", "num_direct_pointers_of_size_u16", "table_size_in_pointers",
+                                   "pointer_size_in_table", "num_nodes", "memory_in_bytes"}
+    assert j["levels"][3]["pointer_size_in_table"] == 8 and j["levels"][3]["table_size_in_pointers"] == 3
+    assert j["levels"][2]["pointer_size_in_table"] == 0
+    assert (j["total_size_in_bytes"], j["pointer_tables"], j["huffman_code"], j["axis_permutation"], j["translation_level"]) == (1234, True, False, False, 3)
+    plain = tdaglib.encoding_stats_json(stats, 1, cfg, tdaglib.TransformEncodingConfig())
+    assert plain["levels"][3]["pointer_size_in_table"] == 0 and plain["levels"][3]["table_size_in_pointers"] == 0
+    import json
+    json.dumps(j)
