@@ -884,8 +884,9 @@ void writeCheckpoint(Context& ctx, const std::string& path, const tdag_scene& sc
     h.voxels = voxels;
     h.numChunks = chunkRoot.size();
     const std::string tmp = path + ".tmp";
-    FILE* f = std::fopen(tmp.c_str(), "wb");
-    TDAG_CHECK(f != nullptr, TDAG_ERR_ARG, "cannot write the checkpoint " + tmp);
+    std::unique_ptr<FILE, int (*)(FILE*)> file(std::fopen(tmp.c_str(), "wb"), &std::fclose);
+    TDAG_CHECK(file != nullptr, TDAG_ERR_ARG, "cannot write the checkpoint " + tmp);
+    FILE* f = file.get();
     bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
     std::vector<uint64_t> host;
     for (uint32_t l = 2; ok && l < glv.size(); ++l) {
@@ -898,7 +899,7 @@ void writeCheckpoint(Context& ctx, const std::string& path, const tdag_scene& sc
         ok = std::fwrite(meta, sizeof meta, 1, f) == 1 && (host.empty() || std::fwrite(host.data(), 8, host.size(), f) == host.size());
     }
     ok = ok && std::fwrite(chunkRoot.data(), 4, chunkRoot.size(), f) == chunkRoot.size();
-    ok = (std::fclose(f) == 0) && ok;
+    ok = (std::fclose(file.release()) == 0) && ok;
     TDAG_CHECK(ok, TDAG_ERR_ARG, "writing the checkpoint " + tmp + " failed");
     TDAG_CHECK(std::rename(tmp.c_str(), path.c_str()) == 0, TDAG_ERR_ARG, "cannot move the checkpoint to " + path);
 }
