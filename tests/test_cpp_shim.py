@@ -44,3 +44,29 @@ def test_shim_matches_oracle(tmp_path, oracle, tdaglib):
     # byte 3 of the trailing config is struct padding (transform_dag.h:157-160): compare it masked
     assert len(got) == len(ref)
     assert got[:-5] == ref[:-5] and got[-4:] == ref[-4:]
+
+
+def _build_graph_driver(tmp_path, tdaglib):
+    lib_dir = os.path.dirname(tdaglib.library_path())
+    exe = str(tmp_path / "batch_graph")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "batch_graph.cpp"),
+           "-L", lib_dir, "-ltdag", f"-Wl,-rpath,{lib_dir}", "-o", exe]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_batch_graph_driver_compiles_and_reports_missing_device(tmp_path, tdaglib):
+    """A C++ caller of the batch graph through the C ABI alone compiles against include/tdag.h."""
+    import torch
+    exe = _build_graph_driver(tmp_path, tdaglib)
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 10 + 7, r.stderr  # TDAG_ERR_NO_DEVICE
+
+
+@pytest.mark.gpu
+def test_batch_graph_driver_matches_the_eager_batch(tmp_path, tdaglib):
+    exe = _build_graph_driver(tmp_path, tdaglib)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
